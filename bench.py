@@ -1,0 +1,385 @@
+#!/usr/bin/env python
+"""Throughput benchmark of the fused advect -> bin -> pair -> interact step (microbe-steps/s).
+
+Workload (the README-scale configuration): 490,000 microbes on a 700 x 700 lattice over
+lon 200-205E, lat 25-30N, species i.i.d. uniform over {rock, paper, scissors}, p = 0.7,
+a seeded synthetic 32-mode streamfunction field on a 1/12 deg grid over lon 190-215E,
+lat 15-40N with hourly frames, RK4 dt = 1 h, interaction radius 0.01 deg (1 km), 720 steps.
+
+One bench step = one CUDA-graph launch of 24 fused steps (one simulated day); K = 30 bench steps
+run the configuration's 720 steps. Between timed bench steps a 512 MiB buffer is written to flush
+the 129 MB L2. Timing uses CUDA events on the stream the library launches on.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the CPU restatement of the reference's path (the oracle: float32 RK4 over
+threads, cell-list fixed-radius pairs, sequential rock-paper-scissors replay) on the host cores.
+With --gpus N > 1 (torchrun), every rank runs an independent replica (the path has no exchange).
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+N_MICROBES = 490_000
+LAT = (25.0, 30.0)
+LON = (200.0, 205.0)
+FIELD_BOX = (190.0, 215.0, 15.0, 40.0)
+RES = 1.0 / 12.0
+DT = 3600.0
+RADIUS = 0.01
+P_WIN = 0.7
+SEED = 2024
+STEPS_PER_LAUNCH = 24
+WORKLOAD = "490k microbes, 700x700 lattice lon 200-205E lat 25-30N, 1/12 deg hourly psi field, RK4 dt=1h, r=0.01 deg, p=0.7"
+
+
+def env_rank():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def make_inputs(n_frames: int):
+    import numpy as np
+
+    import lagrangian_microbes_gb300 as lm
+    from lagrangian_microbes_gb300.particle_advecter import uniform_particle_locations
+    fld = lm.synthetic_psi_field(*FIELD_BOX, RES, n_frames=n_frames, frame_seconds=DT, seed=SEED)
+    lons, lats = uniform_particle_locations(N_MICROBES, LAT[0], LAT[1], LON[0], LON[1])
+    species = np.random.default_rng(SEED).integers(1, 4, N_MICROBES).astype(np.int8)
+    return fld, lons, lats, species
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["clocks not sampled"], "samples": 0}
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+# Algorithmic bytes of one launch of each kernel (n = microbes, p = unordered pairs of the step,
+# g = grid nodes, frames = distinct frames read per step).
+def kernel_bytes(name: str, n: int, p: float, g: int, frames: int) -> float:
+    if name == "k_advect":
+        # read state 8 + status 1, write state 8 + position 8 + key/id 8, plus the frames read
+        return 33.0 * n + 8.0 * g * frames
+    if name == "k_radix_scatter":
+        return 16.0 * n  # read + write (key, id)
+    if name == "k_radix_hist":
+        return 4.0 * n
+    if name == "k_cells":
+        return 20.0 * n  # keys (4+4 neighbour), id 4, gather 8, write spos 8 (cell starts are O(cells touched))
+    if name == "k_sweep_count":
+        return 16.0 * n  # key 4 + spos 8 + deg 4 (neighbour reads hit L1/L2)
+    if name == "k_sweep_fill":
+        return 24.0 * n + 2 * p * 12.0  # key, spos, id, deg, off, want/head + per directed entry adj 4 + prio 8
+    if name == "k_rounds":
+        return 2 * p * 4.0 + 3.0 * p + 12.0 * n  # adjacency read once, species r/w per pair, per-vertex state
+    return 0.0
+
+
+def run_gb300(args):
+    import numpy as np
+    import torch
+
+    from lagrangian_microbes_gb300.engine import Simulation
+
+    rank, world, local = env_rank()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    K, W, spg = args.steps, args.warmup, STEPS_PER_LAUNCH
+    n_frames = max(K, W) * spg + 2
+    fld, lons, lats, species = make_inputs(n_frames)
+    n = lons.size
+
+    sim = Simulation(fld, lons, lats, species, radius=RADIUS, p_rs=P_WIN, p_pr=P_WIN, p_sp=P_WIN, seed=SEED,
+                     device=local)
+    stream = torch.cuda.current_stream()
+    sim.set_stream(stream.cuda_stream)
+    sim.capture(0.0, DT, spg, step0=0)
+    sim.run_graph(W, sync=True)  # warm-up (also grows neighbour lists if needed)
+
+    flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+
+    def reset():
+        sim.upload_particles(lons, lats, species)
+        sim.set_step(0)
+        sim.ctx.call("lm_stats_reset")
+
+    reset()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        for k in range(K):
+            flush.zero_()
+            starts[k].record(stream)
+            sim.run_graph(1, sync=False)
+            ends[k].record(stream)
+        torch.cuda.synchronize()
+    sim.sync()  # raises on any device-side error of the timed region
+    total_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    stats = sim.stats()
+    if world > 1:
+        t = torch.tensor([total_ms], dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    sim_steps = K * spg
+    value = world * n * sim_steps / (total_ms / 1e3)
+    pairs_per_step = stats["pairs_total"] / max(stats["steps_total"], 1)
+
+    # ---- plain per-step launches (the drop-in form), same workload and step count ----
+    reset()
+    plain_steps = min(sim_steps, args.plain_steps)
+    p0 = torch.cuda.Event(enable_timing=True)
+    p1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    p0.record(stream)
+    sim.step(0.0, DT, plain_steps, step0=0)
+    p1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = p0.elapsed_time(p1)
+    plain_value = n * plain_steps / (plain_ms / 1e3)
+
+    # ---- per-kernel timing (plain launches with CUDA events) for the roofline ----
+    reset()
+    sim.ctx.profile_enable(True)
+    prof_steps = min(48, sim_steps)
+    sim.step(0.0, DT, prof_steps, step0=0)
+    prof = sim.ctx.profile()
+    sim.ctx.profile_enable(False)
+    g = fld.u.shape[1] * fld.u.shape[2]
+    kernels = {}
+    for name, (ms, cnt) in prof.items():
+        if cnt:
+            kernels[name] = {"launches": cnt, "total_ms": ms, "avg_us": 1e3 * ms / cnt,
+                             "bytes_per_launch": kernel_bytes(name, n, pairs_per_step, g, 2)}
+    total_k = sum(v["total_ms"] for v in kernels.values()) or 1.0
+    for v in kernels.values():
+        v["share"] = v["total_ms"] / total_k
+    dom = max(kernels, key=lambda k: kernels[k]["total_ms"])
+    peak, peak_kind = measured_peaks()
+    dk = kernels[dom]
+    achieved = dk["bytes_per_launch"] / (dk["avg_us"] * 1e-6) / 1e9 if dk["bytes_per_launch"] else None
+    traffic = None
+    if args.traffic_json and os.path.exists(args.traffic_json):
+        with open(args.traffic_json) as f:
+            traffic = json.load(f).get(dom)
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": (achieved / peak) if achieved else None, "traffic": traffic, "peak_source": peak_kind,
+                "algorithmic_bytes_per_launch": dk["bytes_per_launch"], "avg_launch_us": dk["avg_us"]}
+    step_bytes = 42.0 * n + 16.0 * pairs_per_step + 8.0 * g * 2
+    whole = {"bytes_per_step": step_bytes, "gbs": step_bytes * sim_steps / (total_ms / 1e3) / 1e9}
+
+    # ---- end to end through the public API from host buffers ----
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(fld, lons, lats, species, K, spg, local, stream)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(fld, lons, lats, species, args.cpu_seconds)
+    clk = clocks.summary()
+    launches_per_step = (sum(v["launches"] for v in kernels.values()) / prof_steps) * spg
+    if rank == 0:
+        line = {
+            "metric": "microbe-steps/s (advect+interact), batched+graphed vs plain, 1 GB300, <=10 m err",
+            "value": value, "unit": "microbe-steps/s", "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 (positions), f64 (pair-boundary refine), int8 (species)", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "microbes": n, "sim_steps_per_bench_step": spg,
+                       "sim_steps_timed": sim_steps, "parallelism": f"replicas x{world}",
+                       "l2": "512 MiB buffer written between timed bench steps", "form": "cuda-graph, 24 steps/launch"},
+            "pairs_per_step": pairs_per_step,
+            "plain": {"value": plain_value, "unit": "microbe-steps/s", "sim_steps": plain_steps,
+                      "graph_speedup": value / world / plain_value},
+            "roofline": roofline, "whole_step": whole, "kernels": kernels,
+            "e2e": e2e, "cpu_baseline": cpu, "clocks": clk,
+            "gpu_launches": int(round(launches_per_step * K)),
+            "max_rounds": stats["max_rounds"],
+        }
+        print(json.dumps(line), flush=True)
+    sim.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_e2e(fld, lons, lats, species, K, spg, local, stream):
+    """Same job through the public API: host field/particles in, final state out, all timed."""
+    import numpy as np
+    import torch
+
+    from lagrangian_microbes_gb300.engine import Simulation
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sim = Simulation(fld, lons, lats, species, radius=RADIUS, p_rs=P_WIN, p_pr=P_WIN, p_sp=P_WIN, seed=SEED,
+                     device=local)
+    sim.capture(0.0, DT, spg, step0=0)
+    sim.run_graph(K, sync=True)
+    lon, lat, sp, st = sim.state()
+    t1 = time.perf_counter()
+    sim.close()
+    n = lons.size
+    h2d = fld.u.nbytes + fld.v.nbytes + lons.nbytes + lats.nbytes + species.nbytes
+    d2h = lon.nbytes + lat.nbytes + sp.nbytes + st.nbytes
+    return {"value": n * K * spg / (t1 - t0), "unit": "microbe-steps/s", "h2d_bytes_per_step": h2d / K,
+            "d2h_bytes_per_step": d2h / K, "seconds": t1 - t0,
+            "note": "setup (field + particles upload, graph capture) + 720 steps + state download, wall clock"}
+
+
+def cpu_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_baseline(fld, lons, lats, species, seconds):
+    """The oracle's fused CPU steps on the full 490k workload, as many steps as fit in ~`seconds`."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    oracle.build()
+    threads = cpu_threads()
+    lon = lons.astype(np.float32)
+    lat = lats.astype(np.float32)
+    sp = species.copy()
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        oracle.run(fld, lon, lat, sp, DT * steps, DT, 1, steps, RADIUS, 2, P_WIN, P_WIN, P_WIN, SEED, threads)
+        steps += 1
+        if time.perf_counter() - t0 > seconds or steps >= 720:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": lons.size * steps / dt, "unit": "microbe-steps/s", "cores": threads, "kind": "port",
+            "sample": f"{steps} fused steps of the full 490k workload (float32 RK4 on {threads} threads, "
+                      f"cell-list pairs, sequential RPS replay)", "seconds": dt}
+
+
+def run_reference(args):
+    rank, world, local = env_rank()
+    if rank != 0:
+        return
+    import numpy as np
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    oracle.build()
+    K, W = args.steps, args.warmup
+    fld, lons, lats, species = make_inputs(K + W + 2)
+    threads = cpu_threads()
+    lon = lons.astype(np.float32)
+    lat = lats.astype(np.float32)
+    sp = species.copy()
+    for s in range(W):
+        oracle.run(fld, lon, lat, sp, DT * s, DT, 1, s, RADIUS, 2, P_WIN, P_WIN, P_WIN, SEED, threads)
+    times = []
+    for s in range(W, W + K):
+        t0 = time.perf_counter()
+        oracle.run(fld, lon, lat, sp, DT * s, DT, 1, s, RADIUS, 2, P_WIN, P_WIN, P_WIN, SEED, threads)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = lons.size * K / total
+    line = {"impl": "reference", "metric": "microbe-steps/s (advect+interact), batched+graphed vs plain, 1 GB300, <=10 m err",
+            "value": value, "unit": "microbe-steps/s", "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": 1e3 * total / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 (positions), f64 (pair test), int8 (species)", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "microbes": lons.size, "sim_steps_per_bench_step": 1},
+            "cpu_baseline": {"value": value, "unit": "microbe-steps/s", "cores": threads, "kind": "port",
+                             "sample": f"{K} fused steps of the full 490k workload (one step per bench step)"},
+            "e2e": {"value": value, "unit": "microbe-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--plain-steps", type=int, default=240)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--traffic-json", default=os.path.join(REPO, "profiles", "traffic.json"))
+    args = ap.parse_args()
+    if args.warmup < 0 or args.steps < 1:
+        ap.error("--steps >= 1 and --warmup >= 0")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,163 @@
+/* lm_api.h - C ABI of liblmgb300: the GB300 hot path of lagrangian-microbes
+ * (advect -> bin -> pair -> interact), callable from ctypes / cffi / any C FFI.
+ *
+ * Plain pointers and sizes only. Host pointers are borrowed for the duration of the call
+ * (copy-in / copy-out); device memory is owned by the context. Every entry returns an int status
+ * (LM_OK = 0); nothing aborts or throws across the boundary. lm_last_error() gives the message of
+ * the last failing call on a context. One host thread per context; calls on a context are
+ * serialised on its CUDA stream; contexts are independent.
+ *
+ * Reference interfaces replaced (paths within ali-ramadhan/lagrangian-microbes):
+ *   particle_advecter.py:177-186  parcels RectilinearZGrid / Field / FieldSet / ParticleSet build
+ *   particle_advecter.py:220-244  pset.execute(parcels.AdvectionRK4, runtime=dt, dt=dt) loop,
+ *                                 position store loop and diffusion kick
+ *   interactions.py:43-54         rock_paper_scissors(N, pRS, pPR, pSP) parameters and species
+ *   interaction_simulator.py:93-98   cKDTree(X).query_pairs(r, p)
+ *   interaction_simulator.py:104-105 sequential pair loop calling rock_paper_scissors_interaction
+ *                                    (interactions.py:13-40)
+ */
+#ifndef LM_API_H
+#define LM_API_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LM_API_VERSION 1
+
+/* Status codes. */
+#define LM_OK 0
+#define LM_ERR_ARG 1            /* invalid argument */
+#define LM_ERR_CUDA 2           /* CUDA runtime error (message in lm_last_error) */
+#define LM_ERR_OOM 3            /* device allocation failed */
+#define LM_ERR_STATE 4          /* call out of order (no field / no particles / no parameters) */
+#define LM_ERR_OUT_OF_BOUNDS 5  /* particles left the field domain (they are frozen and excluded) */
+#define LM_ERR_NAN 6            /* non-finite positions */
+#define LM_ERR_ROUND_CAP 7      /* interaction round cap reached */
+#define LM_ERR_TIMEOUT 8        /* a bounded device wait gave up; the context stays usable */
+#define LM_ERR_TIME 9           /* a stage time fell outside the field's time axis */
+#define LM_ERR_GRID 10          /* field axes are not uniformly spaced / ascending */
+#define LM_ERR_CAPACITY 11      /* caller buffer too small (the needed size is returned) */
+
+/* Flags of lm_step / lm_graph_capture. */
+#define LM_STEP_ADVECT 1u     /* RK4 advection (+ diffusion kick when Kh > 0) */
+#define LM_STEP_INTERACT 2u   /* bin -> pair -> rock-paper-scissors rounds */
+#define LM_STEP_CENSUS 4u     /* species counts after each step */
+#define LM_STEP_LOG_PAIRS 8u  /* keep (i, j, round) of every pair applied in the last step */
+
+/* Norm codes for lm_set_interaction (cKDTree's Minkowski p). */
+#define LM_NORM_INF 0
+#define LM_NORM_L1 1
+#define LM_NORM_L2 2
+
+typedef struct lm_ctx lm_ctx;
+
+typedef struct lm_stats {
+  int64_t n_particles;
+  int64_t pairs;          /* unordered pairs found in the last interaction step */
+  int64_t rounds;         /* interaction rounds of the last step */
+  int64_t max_rounds;     /* max rounds over steps since the last lm_stats_reset */
+  int64_t out_of_bounds;  /* particles flagged out of domain or non-finite (sticky) */
+  int64_t step;           /* device step counter (next step index) */
+  int64_t census[4];      /* species counts after the last step: [0]=other, [1]=rock, [2]=paper, [3]=scissors */
+  int64_t adj_capacity;   /* neighbour-list capacity (directed entries) */
+  int64_t regrows;        /* neighbour-list regrowths since creation */
+  int64_t pairs_total;    /* unordered pairs summed over interaction steps since lm_stats_reset */
+  int64_t steps_total;    /* interaction steps since lm_stats_reset */
+} lm_stats;
+
+int lm_version(void);
+
+/* Create a context on CUDA device `device` with its own non-blocking stream. */
+int lm_ctx_create(int device, lm_ctx** out);
+int lm_ctx_destroy(lm_ctx* ctx);
+/* Copy the last error message of `ctx` (or of the last failed lm_ctx_create when ctx is NULL). */
+int lm_last_error(const lm_ctx* ctx, char* buf, size_t len);
+/* Run all further work of `ctx` on an external stream (a cudaStream_t passed as an integer); 0 restores
+ * the context's own stream. */
+int lm_ctx_set_stream(lm_ctx* ctx, uintptr_t stream);
+/* Block until all queued work of the context finished; returns the sticky device status. */
+int lm_sync(lm_ctx* ctx);
+
+/* Velocity field: u, v float32 [nt][ny][nx] in m/s on a rectilinear lon/lat grid whose axes are
+ * uniformly spaced and ascending (lon[nx], lat[ny] degrees, t_sec[nt] seconds, nt >= 2).
+ * Replaces parcels RectilinearZGrid + Field(interp_method="linear") + FieldSet
+ * (particle_advecter.py:177-184). */
+int lm_field_upload(lm_ctx* ctx, const float* u, const float* v, int nt, int ny, int nx, const double* lon,
+                    const double* lat, const double* t_sec);
+
+/* Particles: positions in degrees (float64, as uniform_particle_locations returns them) and species
+ * (int8, ROCK=1 PAPER=2 SCISSORS=3; NULL keeps all species at 0). Requires the field (the state is
+ * stored as float32 offsets from the field origin). Replaces ParticleSet.from_list
+ * (particle_advecter.py:186) and the species array of rock_paper_scissors (interactions.py:45). */
+int lm_particles_upload(lm_ctx* ctx, int64_t n, const double* lon, const double* lat, const int8_t* species);
+/* Current state: absolute float32 lon/lat (after any diffusion kick), species, status (0 ok,
+ * 1 out of domain, 2 non-finite). Any pointer may be NULL. */
+int lm_particles_download(lm_ctx* ctx, float* lon, float* lat, int8_t* species, uint8_t* status);
+/* Set the species array (int8[n]). With particles uploaded, n must match their count; without
+ * (the two-phase workflow, where positions arrive per step through lm_interact) it sizes the
+ * context for n microbes. */
+int lm_species_upload(lm_ctx* ctx, int64_t n, const int8_t* species);
+
+/* Interaction parameters: radius and norm of cKDTree.query_pairs (interaction_simulator.py:98),
+ * forward-win probabilities of rock_paper_scissors (interactions.py:43-54), Philox seed of the
+ * per-pair uniform (replaces np.random.rand at interactions.py:20). */
+int lm_set_interaction(lm_ctx* ctx, double radius, int norm, double p_rs, double p_pr, double p_sp,
+                       uint64_t seed);
+
+/* n_steps fused steps starting at field time t_sec with global step index step0. Each step:
+ * advect (flags & LM_STEP_ADVECT), then bin + pair + interact (flags & LM_STEP_INTERACT) on the
+ * advected positions. kh_deg2_s > 0 adds the diffusion kick of particle_advecter.py:239-244 after the
+ * positions are recorded. Optional host outputs, each [n_steps][N] (NULL to skip): rec_lon/rec_lat
+ * (positions before the kick, the reference's stored positions) and rec_species (species after the
+ * step). rec_census may be NULL or int64[n_steps][4]. */
+int lm_step(lm_ctx* ctx, double t_sec, double dt_sec, int n_steps, int64_t step0, uint32_t flags,
+            double kh_deg2_s, float* rec_lon, float* rec_lat, int8_t* rec_species, int64_t* rec_census);
+
+/* Pairs of externally supplied float32 positions: the unordered pairs (i < j) within radius/norm of
+ * lm_set_interaction. Replaces cKDTree(X).query_pairs(r, p) (interaction_simulator.py:93-98). Pairs are
+ * written in (i, j) ascending order when cap suffices; *n_pairs always receives the count
+ * (LM_ERR_CAPACITY if cap was too small). */
+int lm_query_pairs(lm_ctx* ctx, int64_t n, const float* lon, const float* lat, int32_t* pi, int32_t* pj,
+                   int64_t cap, int64_t* n_pairs);
+
+/* One interaction step on externally supplied float32 positions (the interaction phase of the
+ * reference, interaction_simulator.py:83-117: pairs + pair loop), updating the context's species in
+ * place; step_index keys the Philox draws. n must equal the particle count of the species array. */
+int lm_interact(lm_ctx* ctx, int64_t n, const float* lon, const float* lat, int64_t step_index,
+                uint32_t flags);
+
+/* Pairs applied by the last interaction step when LM_STEP_LOG_PAIRS was set, in application order
+ * (round by round; pairs of one round are disjoint). i < j are particle indices. */
+int lm_pairs_get(lm_ctx* ctx, int32_t* pi, int32_t* pj, int32_t* round, int64_t cap, int64_t* n);
+
+/* Capture `steps_per_graph` fused steps (flags as lm_step, Kh as lm_step) into a CUDA graph. The
+ * graph reads the step index from the device step counter, which lm_step / lm_graph_run advance,
+ * so t = t_start + (step - step0) * dt. */
+int lm_graph_capture(lm_ctx* ctx, double t_start, double dt_sec, int64_t step0, int steps_per_graph,
+                     uint32_t flags, double kh_deg2_s);
+/* Launch the captured graph n_launches times (n_launches * steps_per_graph steps). sync=1 waits and
+ * checks device status (regrowing neighbour lists and recapturing if a step overflowed them);
+ * sync=0 only enqueues. */
+int lm_graph_run(lm_ctx* ctx, int n_launches, int sync);
+/* Set the device step counter (the next step index). */
+int lm_set_step(lm_ctx* ctx, int64_t step);
+
+int lm_stats_get(lm_ctx* ctx, lm_stats* out);
+int lm_stats_reset(lm_ctx* ctx);
+
+/* Per-kernel CUDA-event timing of plain (non-graph) launches: enable (1) / disable (0) and reset the
+ * accumulators; read kernel k (0 <= k < lm_profile_count()): its name, summed duration and launch
+ * count. Used by the benchmark to time the dominant kernel; costs two event records per launch. */
+int lm_profile_enable(lm_ctx* ctx, int on);
+int lm_profile_get(lm_ctx* ctx, int kernel, char* name, size_t name_len, double* total_ms, int64_t* launches);
+int lm_profile_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LM_API_H */

@@ -1,0 +1,244 @@
+"""CPU oracle of the lagrangian-microbes hot path -- TEST INFRASTRUCTURE ONLY.
+
+Imported only by tests/, __graft_entry__.smoke() and bench.py (CPU baseline and the reference
+arm), as the checker and the timed CPU restatement; the product package never imports it.
+
+It wraps lm_oracle.c (built by ``build()`` with gcc, -ffp-contract=off so that the float64 pair
+test is exactly the reference's) and adds numpy restatements of the reference's lattice helper
+(utils.py:25-42, particle_advecter.py:26-35) used to cross-check the package.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD_DIR, "liblmoracle.so")
+SRC = os.path.join(HERE, "lm_oracle.c")
+CFLAGS = ["-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-std=c11"]
+
+
+def build(force: bool = False) -> str:
+    """Compile liblmoracle.so from lm_oracle.c (seconds; gcc only)."""
+    deps = [SRC, os.path.join(HERE, "lm_oracle.h")]
+    if not force and os.path.exists(LIB) and all(os.path.getmtime(d) <= os.path.getmtime(LIB) for d in deps):
+        return LIB
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    tmp = LIB + f".tmp{os.getpid()}"
+    cmd = ["gcc", *CFLAGS, "-D_GNU_SOURCE", "-I", HERE, SRC, "-o", tmp, "-lm"]
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n$ {' '.join(cmd)}\n{r.stdout}")
+    os.replace(tmp, LIB)
+    return LIB
+
+
+class OrcField(ctypes.Structure):
+    _fields_ = [("u", ctypes.c_void_p), ("v", ctypes.c_void_p), ("nx", ctypes.c_int), ("ny", ctypes.c_int),
+                ("nt", ctypes.c_int), ("lon0", ctypes.c_double), ("dlon", ctypes.c_double),
+                ("lat0", ctypes.c_double), ("dlat", ctypes.c_double), ("t0", ctypes.c_double),
+                ("dT", ctypes.c_double)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        P, I64, U32, U64, F64, I = (ctypes.c_void_p, ctypes.c_int64, ctypes.c_uint32, ctypes.c_uint64,
+                                    ctypes.c_double, ctypes.c_int)
+        sig = {
+            "orc_philox4x32_10": (None, [P, P, P]),
+            "orc_pair_draw": (None, [U32, U32, U32, U64, P, P]),
+            "orc_diffusion_draw": (None, [U32, U32, U64, P, P]),
+            "orc_prob_threshold": (U64, [F64]),
+            "orc_advect_f64": (I64, [P, I64, P, P, P, F64, F64, I, P, P]),
+            "orc_advect_f32": (I64, [P, I64, P, P, P, F64, F64, I, I]),
+            "orc_pairs": (I64, [I64, P, P, F64, I, I, P, P, I64]),
+            "orc_rps_apply": (None, [P, ctypes.c_int32, ctypes.c_int32, U64, U64, U64, U64]),
+            "orc_rps_replay": (None, [P, I64, P, P, U32, U64, U64, U64, U64]),
+            "orc_priority_order": (None, [I64, P, P, U32, U64]),
+            "orc_interact_step": (I64, [I64, P, P, P, F64, I, U64, U64, U64, U64, U32, I]),
+            "orc_run": (I64, [P, I64, P, P, P, P, F64, F64, I, U32, F64, I, U64, U64, U64, U64, I]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def norm_code(p) -> int:
+    if p == 2:
+        return 2
+    if p == 1:
+        return 1
+    if math.isinf(float(p)):
+        return 0
+    raise ValueError(p)
+
+
+# ---------------- random numbers ----------------
+
+def philox4x32_10(ctr, key):
+    c = np.ascontiguousarray(ctr, dtype=np.uint32)
+    k = np.ascontiguousarray(key, dtype=np.uint32)
+    out = np.zeros(4, np.uint32)
+    lib().orc_philox4x32_10(_p(c), _p(k), _p(out))
+    return out
+
+
+def pair_draw(i: int, j: int, step: int, seed: int):
+    u53 = ctypes.c_uint64()
+    prio = ctypes.c_uint64()
+    lib().orc_pair_draw(i, j, step, seed & 0xFFFFFFFFFFFFFFFF, ctypes.byref(u53), ctypes.byref(prio))
+    return u53.value, prio.value
+
+
+def pair_uniform(i: int, j: int, step: int, seed: int) -> float:
+    """The float64 r in [0, 1) that replaces np.random.rand() for pair (i, j) at `step`."""
+    return pair_draw(min(i, j), max(i, j), step, seed)[0] * 2.0 ** -53
+
+
+def diffusion_draw(p: int, step: int, seed: int):
+    a = ctypes.c_float()
+    b = ctypes.c_float()
+    lib().orc_diffusion_draw(p, step, seed & 0xFFFFFFFFFFFFFFFF, ctypes.byref(a), ctypes.byref(b))
+    return a.value, b.value
+
+
+def prob_threshold(p: float) -> int:
+    return lib().orc_prob_threshold(float(p))
+
+
+# ---------------- lattice (numpy restatement of particle_advecter.py:26-35, utils.py:25-42) ----------------
+
+def lattice_shape(n: int):
+    divs = [d for d in range(1, math.isqrt(n) + 1) if n % d == 0]
+    a = divs[-1]
+    return a, n // a
+
+
+def lattice(n: int, lat_min, lat_max, lon_min, lon_max):
+    n_lat, n_lon = lattice_shape(n)
+    lons = np.repeat(np.linspace(lon_min, lon_max, n_lon), n_lat)
+    lats = np.tile(np.linspace(lat_min, lat_max, n_lat), n_lon)
+    return lons, lats
+
+
+# ---------------- advection ----------------
+
+def _field_struct(fld):
+    u = np.ascontiguousarray(fld.u, dtype=np.float32)
+    v = np.ascontiguousarray(fld.v, dtype=np.float32)
+    nt, ny, nx = u.shape
+    s = OrcField(u.ctypes.data, v.ctypes.data, nx, ny, nt, float(fld.lon[0]), float((fld.lon[-1] - fld.lon[0]) / (nx - 1)),
+                 float(fld.lat[0]), float((fld.lat[-1] - fld.lat[0]) / (ny - 1)), float(fld.times[0]),
+                 float((fld.times[-1] - fld.times[0]) / (nt - 1)))
+    return s, (u, v)
+
+
+def advect_f64(fld, lons, lats, t0: float, dt: float, n_steps: int, record: bool = False):
+    """FP64 RK4 oracle: returns (lon, lat, status[, rec_lon, rec_lat])."""
+    s, keep = _field_struct(fld)
+    lon = np.array(lons, dtype=np.float64)
+    lat = np.array(lats, dtype=np.float64)
+    st = np.zeros(lon.size, np.uint8)
+    rl = np.empty((n_steps, lon.size)) if record else None
+    ra = np.empty((n_steps, lon.size)) if record else None
+    bad = lib().orc_advect_f64(ctypes.byref(s), lon.size, _p(lon), _p(lat), _p(st), float(t0), float(dt),
+                               int(n_steps), _p(rl), _p(ra))
+    if bad < 0:
+        raise ValueError("time outside the field's time axis")
+    return (lon, lat, st, rl, ra) if record else (lon, lat, st)
+
+
+def advect_f32(fld, lons, lats, t0: float, dt: float, n_steps: int, n_threads: int = 0):
+    s, keep = _field_struct(fld)
+    lon = np.array(lons, dtype=np.float32)
+    lat = np.array(lats, dtype=np.float32)
+    st = np.zeros(lon.size, np.uint8)
+    bad = lib().orc_advect_f32(ctypes.byref(s), lon.size, _p(lon), _p(lat), _p(st), float(t0), float(dt),
+                               int(n_steps), int(n_threads))
+    if bad < 0:
+        raise ValueError("time outside the field's time axis")
+    return lon, lat, st
+
+
+# ---------------- pairs and interaction ----------------
+
+def pairs(lon, lat, r: float, p=2, n_threads: int = 0):
+    lon = np.ascontiguousarray(lon, dtype=np.float32)
+    lat = np.ascontiguousarray(lat, dtype=np.float32)
+    m = lib().orc_pairs(lon.size, _p(lon), _p(lat), float(r), norm_code(p), int(n_threads), None, None, 0)
+    if m < 0:
+        raise MemoryError("oracle pair search failed")
+    pi = np.empty(m, np.int32)
+    pj = np.empty(m, np.int32)
+    lib().orc_pairs(lon.size, _p(lon), _p(lat), float(r), norm_code(p), int(n_threads), _p(pi), _p(pj), m)
+    return pi.astype(np.int64), pj.astype(np.int64)
+
+
+def priority_order(pi, pj, step: int, seed: int):
+    a = np.ascontiguousarray(pi, dtype=np.int32).copy()
+    b = np.ascontiguousarray(pj, dtype=np.int32).copy()
+    lib().orc_priority_order(a.size, _p(a), _p(b), int(step), seed & 0xFFFFFFFFFFFFFFFF)
+    return a.astype(np.int64), b.astype(np.int64)
+
+
+def rps_replay(species, pi, pj, step: int, seed: int, pRS: float, pPR: float, pSP: float):
+    """Sequential replay in the given order; returns the new species array."""
+    sp = np.array(species, dtype=np.int8)
+    a = np.ascontiguousarray(pi, dtype=np.int32)
+    b = np.ascontiguousarray(pj, dtype=np.int32)
+    lib().orc_rps_replay(_p(sp), a.size, _p(a), _p(b), int(step), seed & 0xFFFFFFFFFFFFFFFF, prob_threshold(pRS),
+                         prob_threshold(pPR), prob_threshold(pSP))
+    return sp
+
+
+def interact_step(lon, lat, species, r, p, pRS, pPR, pSP, seed, step, n_threads: int = 0):
+    """Pairs + priority-ordered replay: the species the GPU must produce."""
+    lon = np.ascontiguousarray(lon, dtype=np.float32)
+    lat = np.ascontiguousarray(lat, dtype=np.float32)
+    sp = np.array(species, dtype=np.int8)
+    m = lib().orc_interact_step(lon.size, _p(lon), _p(lat), _p(sp), float(r), norm_code(p), prob_threshold(pRS),
+                                prob_threshold(pPR), prob_threshold(pSP), seed & 0xFFFFFFFFFFFFFFFF, int(step),
+                                int(n_threads))
+    if m < 0:
+        raise MemoryError("oracle interaction failed")
+    return sp, m
+
+
+def run(fld, lon, lat, species, t0, dt, n_steps, step0, r, p, pRS, pPR, pSP, seed, n_threads: int = 0):
+    """CPU fused steps (float32 advection + pairs + interaction), in place; returns total pairs."""
+    s, keep = _field_struct(fld)
+    st = np.zeros(lon.size, np.uint8)
+    m = lib().orc_run(ctypes.byref(s), lon.size, _p(lon), _p(lat), _p(st), _p(species), float(t0), float(dt),
+                      int(n_steps), int(step0), float(r), norm_code(p), prob_threshold(pRS), prob_threshold(pPR),
+                      prob_threshold(pSP), seed & 0xFFFFFFFFFFFFFFFF, int(n_threads))
+    if m < 0:
+        raise RuntimeError("oracle run failed")
+    return m
+
+
+def great_circle_m(lon1, lat1, lon2, lat2, radius_km: float = 6371.228):
+    """Haversine distance in metres (float64)."""
+    p1, p2 = np.deg2rad(lat1), np.deg2rad(lat2)
+    dphi = p2 - p1
+    dl = np.deg2rad(np.asarray(lon2, np.float64) - np.asarray(lon1, np.float64))
+    a = np.sin(dphi / 2) ** 2 + np.cos(p1) * np.cos(p2) * np.sin(dl / 2) ** 2
+    return 2 * radius_km * 1e3 * np.arcsin(np.sqrt(np.minimum(a, 1.0)))
