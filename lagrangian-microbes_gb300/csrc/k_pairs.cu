@@ -14,9 +14,13 @@
 #include "lm_internal.h"
 #include "lm_philox.cuh"
 
+// the local insertion sort reads pr[y-1] / pid[y-1] only for y > 0, i.e. after they were written
+#pragma nv_diag_suppress 549
+
 namespace lm {
 
 constexpr int SW_THREADS = 256;
+constexpr uint32_t LOCAL_MAX = 16;  // neighbour lists up to this length are sorted in thread-local storage
 
 int sweep_blocks(uint32_t n) { return (int)((n + SW_THREADS - 1) / SW_THREADS); }
 
@@ -208,7 +212,8 @@ __global__ void __launch_bounds__(SW_THREADS) k_sweep_fill(CellGrid g, PairParam
                                                            const uint32_t* __restrict__ deg, uint32_t* __restrict__ off,
                                                            uint32_t* __restrict__ adj, unsigned long long* __restrict__ prio,
                                                            uint32_t* __restrict__ want0, uint32_t* __restrict__ head,
-                                                           uint32_t* __restrict__ act0, uint32_t n) {
+                                                           uint32_t* __restrict__ act0, uint32_t* __restrict__ level,
+                                                           uint32_t n) {
   if (ctrl->halt) return;
   __shared__ uint32_t ws[SW_THREADS / 32];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -230,22 +235,48 @@ __global__ void __launch_bounds__(SW_THREADS) k_sweep_fill(CellGrid g, PairParam
   if (s < n) {
     off[s] = o;
     head[s] = 0;
+    level[s] = 0;
     if (d > 0) {
       const uint32_t n_valid = ctrl->n_valid;
       const uint32_t ia = id[s];
-      uint32_t m = 0;
-      for_neighbours(g, pp, key, spos, cell_start, n_valid, s, [&](uint32_t t) {
-        if (m < d) {
-          uint32_t ib = id[t];
-          uint32_t i = min(ia, ib), j = max(ia, ib);
-          PairDraw pd = pair_draw(i, j, step, rp.seed_lo, rp.seed_hi);
-          adj[o + m] = t;
-          prio[o + m] = pd.prio;
-        }
-        ++m;
-      });
-      sort_segment(prio + o, adj + o, id, d);
-      want0[s] = adj[o];
+      if (d <= LOCAL_MAX) {
+        // short lists: collect and insertion-sort in thread-local storage, write the sorted list once
+        unsigned long long pr[LOCAL_MAX];
+        uint32_t nb[LOCAL_MAX], pid[LOCAL_MAX];
+        uint32_t m = 0;
+        for_neighbours(g, pp, key, spos, cell_start, n_valid, s, [&](uint32_t t) {
+          if (m < LOCAL_MAX) {
+            const uint32_t ib = id[t];
+            const PairDraw pd = pair_draw(min(ia, ib), max(ia, ib), step, rp.seed_lo, rp.seed_hi);
+            uint32_t y = m;
+            while (y > 0 && before(pd.prio, ib, pr[y - 1], pid[y - 1])) {
+              pr[y] = pr[y - 1];
+              nb[y] = nb[y - 1];
+              pid[y] = pid[y - 1];
+              --y;
+            }
+            pr[y] = pd.prio;
+            nb[y] = t;
+            pid[y] = ib;
+          }
+          ++m;
+        });
+        for (uint32_t k = 0; k < d; ++k) adj[o + k] = nb[k];
+        want0[s] = nb[0];
+      } else {
+        uint32_t m = 0;
+        for_neighbours(g, pp, key, spos, cell_start, n_valid, s, [&](uint32_t t) {
+          if (m < d) {
+            const uint32_t ib = id[t];
+            const PairDraw pd = pair_draw(min(ia, ib), max(ia, ib), step, rp.seed_lo, rp.seed_hi);
+            adj[o + m] = t;
+            prio[o + m] = pd.prio;
+          }
+          ++m;
+        });
+        sort_segment(prio + o, adj + o, id, d);
+        want0[s] = adj[o];
+      }
       active = true;
     }
   }
@@ -274,11 +305,11 @@ void launch_scan_blocks(uint32_t* block_sum, uint32_t nblocks, Ctrl* ctrl, cudaS
 void launch_sweep_fill(const CellGrid& g, const PairParams& pp, const RpsParams& rp, const StepArgs& a,
                        const uint32_t* key, const uint32_t* id, const float2* spos, const uint32_t* cell_start,
                        const uint32_t* block_sum, Ctrl* ctrl, const uint32_t* deg, uint32_t* off, uint32_t* adj,
-                       unsigned long long* prio, uint32_t* want0, uint32_t* head, uint32_t* act0, uint32_t n,
-                       cudaStream_t st) {
+                       unsigned long long* prio, uint32_t* want0, uint32_t* head, uint32_t* act0, uint32_t* level,
+                       uint32_t n, cudaStream_t st) {
   if (n == 0) return;
   k_sweep_fill<<<sweep_blocks(n), SW_THREADS, 0, st>>>(g, pp, rp, a, key, id, spos, cell_start, block_sum, ctrl, deg,
-                                                        off, adj, prio, want0, head, act0, n);
+                                                        off, adj, prio, want0, head, act0, level, n);
 }
 
 }  // namespace lm

@@ -7,26 +7,32 @@
 // pRS / pSP / pPR of that matchup, and the loser takes the winner's species. Updates cascade to
 // later pairs of the same step. The set order is an artifact of hashing, not a semantic.
 //
-// Here the order is fixed as descending pair priority (a Philox function of (seed, step, i, j)).
-// That order is applied in parallel without changing its result: in round r every vertex looks at
-// its highest-priority unprocessed pair; a pair whose two endpoints both look at it is the
-// earliest unprocessed pair at both, so all such pairs form a matching that commutes with itself
-// and precedes every pair it conflicts with. Applying rounds one after another is therefore the
-// same as applying the whole list in priority order, which the CPU oracle replays with the
-// reference's own pair function. r is drawn from the same Philox block (53-bit uniform), and
-// r < p is evaluated exactly as the integer test u53 < ceil(p * 2^53).
+// Here the order is fixed as descending pair priority (a Philox function of (seed, step, i, j)),
+// which the CPU oracle replays with a restatement of the reference's pair function. Pairs that
+// share no microbe commute, so any order that keeps the priority order at every microbe gives the
+// same species: a pair may be applied as soon as it is the highest-priority unprocessed pair of
+// both its microbes. r is drawn from the same Philox block (53-bit uniform), and r < p is
+// evaluated exactly as the integer test u53 < ceil(p * 2^53).
 //
-// One persistent cooperative launch runs all rounds, separated by a grid barrier whose waits are
-// bounded (error flag + return on timeout). When the active set drops below SOLO_VERTICES the
-// remaining rounds run in block 0 alone with block barriers.
+// All pairs are applied by one persistent cooperative launch without grid barriers. Each vertex v
+// publishes want[v], the partner of its highest-priority unprocessed pair (NONE when it has none).
+// A pair (v, u) is ready exactly when want[v] == u and want[u] == v; the thread that polls the
+// lower endpoint applies it and advances both heads. Only the applier of a vertex's current head
+// pair ever writes that vertex's head/want, so every write has a single owner. Species and head
+// writes are released before the want words that hand the vertices on; pollers read want with
+// acquire loads. The globally highest-priority pending pair is always ready, so the loop always
+// progresses; every wait is still bounded (error flag + return after a timeout).
+//
+// Each applied pair gets a level = 1 + max(level of the previous pair at either endpoint): pairs of
+// one level share no microbe, and (level, i, j) is a deterministic sequential order equal in
+// effect to the priority order. The pair log records it; the step's "rounds" is the max level.
 #include "lm_internal.h"
 #include "lm_philox.cuh"
 
 namespace lm {
 
-constexpr int RD_THREADS = 512;
-constexpr uint32_t SOLO_VERTICES = 2048;
-constexpr unsigned long long BARRIER_TIMEOUT_NS = 2000000000ull;  // 2 s
+constexpr int RD_THREADS = 256;
+constexpr unsigned long long ROUNDS_TIMEOUT_NS = 2000000000ull;  // 2 s
 
 __device__ __forceinline__ unsigned long long globaltimer() {
   unsigned long long t;
@@ -34,43 +40,14 @@ __device__ __forceinline__ unsigned long long globaltimer() {
   return t;
 }
 
-__device__ __forceinline__ uint32_t lanemask_lt_r() {
-  uint32_t m;
-  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
-  return m;
+__device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
 }
 
-// Sense-by-generation grid barrier. Returns false if the wait timed out (error bit set).
-__device__ bool grid_barrier(Ctrl* c, uint32_t nblocks) {
-  __shared__ int ok;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    volatile uint32_t* gen = &c->bar_gen;
-    uint32_t g = *gen;
-    __threadfence();
-    uint32_t arrived = atomicAdd(&c->bar_count, 1u);
-    int res = 1;
-    if (arrived == nblocks - 1) {
-      atomicExch(&c->bar_count, 0u);
-      __threadfence();
-      atomicAdd(&c->bar_gen, 1u);
-    } else {
-      unsigned long long t0 = globaltimer();
-      while (*gen == g) {
-        if (globaltimer() - t0 > BARRIER_TIMEOUT_NS) {
-          atomicOr(&c->err, (uint32_t)ERRB_TIMEOUT);
-          res = 0;
-          break;
-        }
-        __nanosleep(32);
-      }
-    }
-    __threadfence();
-    if (((volatile uint32_t*)&c->err)[0] & ERRB_TIMEOUT) res = 0;
-    ok = res;
-  }
-  __syncthreads();
-  return ok != 0;
+__device__ __forceinline__ void st_release(uint32_t* p, uint32_t v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
 __device__ __forceinline__ bool beats(int x, int y) {
@@ -78,13 +55,13 @@ __device__ __forceinline__ bool beats(int x, int y) {
   return (x == 1 && y == 3) || (x == 2 && y == 1) || (x == 3 && y == 2);
 }
 
-__device__ __forceinline__ void apply_pair(const RoundBufs& b, const RpsParams& rp, uint32_t step, uint32_t s,
-                                           uint32_t u, uint32_t round, Ctrl* ctrl) {
+// Apply pair (s, u), s < u in cell order, both heads pointing at it; returns its level.
+__device__ __forceinline__ uint32_t apply_pair(const RoundBufs& b, const RpsParams& rp, uint32_t step, uint32_t s,
+                                               uint32_t u, Ctrl* ctrl) {
   const uint32_t ia = b.id[s], ib = b.id[u];
   const uint32_t i = min(ia, ib), j = max(ia, ib);
   const int si = __ldcg(b.species + i), sj = __ldcg(b.species + j);
   if (si != sj) {
-    PairDraw d = pair_draw(i, j, step, rp.seed_lo, rp.seed_hi);
     unsigned long long t = 0;
     bool valid = true;
     if ((si == 1 && sj == 3) || (si == 3 && sj == 1)) t = rp.t_rs;
@@ -92,98 +69,68 @@ __device__ __forceinline__ void apply_pair(const RoundBufs& b, const RpsParams& 
     else if ((si == 3 && sj == 2) || (si == 2 && sj == 3)) t = rp.t_sp;
     else valid = false;  // species outside {1,2,3}: the reference's table has no case -> no change
     if (valid) {
-      const bool fwd_i = beats(si, sj);  // particle i is the cyclic (forward) winner
+      const PairDraw d = pair_draw(i, j, step, rp.seed_lo, rp.seed_hi);
       const bool fwd_wins = d.u53 < t;
-      const bool i_wins = (fwd_i == fwd_wins);
-      if (i_wins) b.species[j] = (int8_t)si;
-      else b.species[i] = (int8_t)sj;
+      const bool i_wins = (beats(si, sj) == fwd_wins);  // particle i is the cyclic winner xor it lost the draw
+      if (i_wins) __stcg(b.species + j, (int8_t)si);
+      else __stcg(b.species + i, (int8_t)sj);
     }
   }
+  const uint32_t level = max(__ldcg(b.level + s), __ldcg(b.level + u)) + 1u;
+  __stcg(b.level + s, level);
+  __stcg(b.level + u, level);
   if (b.plog) {
-    uint32_t k = atomicAdd(&ctrl->plog_n, 1u);
+    const uint32_t k = atomicAdd(&ctrl->plog_n, 1u);
     if (k < b.plog_cap) {
       b.plog[3 * k + 0] = i;
       b.plog[3 * k + 1] = j;
-      b.plog[3 * k + 2] = round;
+      b.plog[3 * k + 2] = level - 1u;
     }
   }
+  // hand both vertices on to their next pair
+  const uint32_t hu = __ldcg(b.head + u) + 1u, hs = __ldcg(b.head + s) + 1u;
+  __stcg(b.head + u, hu);
+  __stcg(b.head + s, hs);
+  const uint32_t nu = hu < b.deg[u] ? b.adj[b.off[u] + hu] : NONE;
+  const uint32_t ns = hs < b.deg[s] ? b.adj[b.off[s] + hs] : NONE;
+  __threadfence();
+  st_release(b.want[0] + u, nu);
+  st_release(b.want[0] + s, ns);
+  return level;
 }
 
 __global__ void __launch_bounds__(RD_THREADS) k_rounds(RoundBufs b, RpsParams rp, StepArgs a, Ctrl* ctrl,
                                                        uint32_t round_cap) {
+  (void)round_cap;
   if (((volatile uint32_t*)&ctrl->halt)[0]) return;
   const uint32_t step = a.use_ctrl_step ? ctrl->step : a.step0;
-  const uint32_t nblocks = gridDim.x;
-  const int lane = threadIdx.x & 31;
-  bool solo = (nblocks == 1);
-  uint32_t r = 0;
-  uint32_t cnt = ((volatile uint32_t*)ctrl->act_n)[0];
-  if (!solo && cnt <= SOLO_VERTICES) {
-    if (blockIdx.x != 0) return;
-    solo = true;
-  }
-  while (cnt > 0) {
-    if (r >= round_cap) {
-      if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&ctrl->err, (uint32_t)ERRB_ROUNDCAP);
+  const uint32_t cnt = ((volatile uint32_t*)ctrl->act_n)[0];
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t first = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t* L = b.act[0];
+  uint32_t* want = b.want[0];
+  uint32_t max_level = 0;
+  const unsigned long long t0 = globaltimer();
+  bool pending = first < cnt;
+  uint32_t polls = 0;
+  while (pending) {
+    pending = false;
+    for (uint32_t x = first; x < cnt; x += stride) {
+      const uint32_t s = L[x];
+      const uint32_t u = ld_acquire(want + s);
+      if (u == NONE) continue;
+      pending = true;
+      if (s < u && ld_acquire(want + u) == s) max_level = max(max_level, apply_pair(b, rp, step, s, u, ctrl));
+    }
+    if (pending && ((++polls & 63u) == 0u) && globaltimer() - t0 > ROUNDS_TIMEOUT_NS) {
+      atomicOr(&ctrl->err, (uint32_t)ERRB_TIMEOUT);
       break;
     }
-    const bool odd = (r & 1u) != 0;
-    const uint32_t* L = odd ? b.act[1] : b.act[0];
-    uint32_t* Ln = odd ? b.act[0] : b.act[1];
-    const uint32_t* cur = odd ? b.want[1] : b.want[0];
-    uint32_t* nxt = odd ? b.want[0] : b.want[1];
-    const uint32_t r3 = r % 3u;
-    uint32_t* ncnt = ctrl->act_n + (r3 == 2u ? 0u : r3 + 1u);
-    if (blockIdx.x == 0 && threadIdx.x == 0) ctrl->act_n[r3 == 0u ? 2u : r3 - 1u] = 0;
-    const uint32_t stride = solo ? blockDim.x : nblocks * blockDim.x;
-    const uint32_t first = solo ? threadIdx.x : blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t lim = (cnt + 31u) & ~31u;  // warp-uniform trip count
-    for (uint32_t x = first - lane + 0; x < lim; x += stride) {
-      const uint32_t xi = x + lane;
-      bool keep = false;
-      uint32_t s = 0;
-      if (xi < cnt) {
-        s = __ldcg(L + xi);
-        const uint32_t u = __ldcg(cur + s);
-        if (__ldcg(cur + u) == s) {
-          if (s < u) apply_pair(b, rp, step, s, u, r, ctrl);
-          const uint32_t h = b.head[s] + 1;
-          b.head[s] = h;
-          if (h < b.deg[s]) {
-            nxt[s] = b.adj[b.off[s] + h];
-            keep = true;
-          }
-        } else {
-          nxt[s] = u;
-          keep = true;
-        }
-      }
-      const uint32_t m = __ballot_sync(0xffffffffu, keep);
-      if (m) {
-        const int leader = __ffs(m) - 1;
-        uint32_t base = 0;
-        if (lane == leader) base = atomicAdd(ncnt, (uint32_t)__popc(m));
-        base = __shfl_sync(0xffffffffu, base, leader);
-        if (keep) Ln[base + __popc(m & lanemask_lt_r())] = s;
-      }
-    }
-    if (solo) {
-      __threadfence_block();
-      __syncthreads();
-    } else if (!grid_barrier(ctrl, nblocks)) {
-      return;
-    }
-    cnt = ((volatile uint32_t*)ncnt)[0];
-    ++r;
-    if (solo) __syncthreads();  // everyone has read cnt before thread 0 resets the next counter
-    if (!solo && cnt <= SOLO_VERTICES) {
-      if (blockIdx.x != 0) return;
-      solo = true;
-    }
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    ctrl->rounds = r;
-    if (r > ctrl->max_rounds) ctrl->max_rounds = r;
+  for (int o = 16; o > 0; o >>= 1) max_level = max(max_level, __shfl_xor_sync(0xffffffffu, max_level, o));
+  if ((threadIdx.x & 31) == 0 && max_level) {
+    atomicMax(&ctrl->rounds, max_level);
+    atomicMax(&ctrl->max_rounds, max_level);
   }
 }
 
@@ -192,7 +139,7 @@ int rounds_grid(int device, int* block) {
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rounds, RD_THREADS, 0);
   if (per_sm < 1) per_sm = 1;
-  if (per_sm > 2) per_sm = 2;
+  if (per_sm > 4) per_sm = 4;
   *block = RD_THREADS;
   return sms * per_sm;
 }

@@ -48,7 +48,7 @@ struct lm_ctx {
   uint8_t* status = nullptr;
   uint32_t *key[2] = {nullptr, nullptr}, *id[2] = {nullptr, nullptr};
   float2* spos = nullptr;
-  uint32_t *deg = nullptr, *off = nullptr, *block_sum = nullptr, *head = nullptr;
+  uint32_t *deg = nullptr, *off = nullptr, *block_sum = nullptr, *head = nullptr, *level = nullptr;
   uint32_t *want[2] = {nullptr, nullptr}, *act[2] = {nullptr, nullptr};
   uint32_t* sort_counts = nullptr;
   uint32_t* digit_total = nullptr;
@@ -210,7 +210,7 @@ int ensure_particles(lm_ctx* c, uint32_t n) {
       (r = dalloc(c, &c->plat, cap)) || (r = dalloc(c, &c->species, cap)) || (r = dalloc(c, &c->status, cap)) ||
       (r = dalloc(c, &c->key[0], cap)) || (r = dalloc(c, &c->key[1], cap)) || (r = dalloc(c, &c->id[0], cap)) ||
       (r = dalloc(c, &c->id[1], cap)) || (r = dalloc(c, &c->spos, cap)) || (r = dalloc(c, &c->deg, cap)) ||
-      (r = dalloc(c, &c->off, cap)) || (r = dalloc(c, &c->head, cap)) || (r = dalloc(c, &c->want[0], cap)) ||
+      (r = dalloc(c, &c->off, cap)) || (r = dalloc(c, &c->head, cap)) || (r = dalloc(c, &c->level, cap)) || (r = dalloc(c, &c->want[0], cap)) ||
       (r = dalloc(c, &c->want[1], cap)) || (r = dalloc(c, &c->act[0], cap)) || (r = dalloc(c, &c->act[1], cap)) ||
       (r = dalloc(c, &c->block_sum, (size_t)sweep_blocks(cap) + 1)) ||
       (r = dalloc(c, &c->sort_counts, (size_t)256 * sort_tiles(cap))) ||
@@ -353,7 +353,7 @@ cudaError_t enqueue_interaction(lm_ctx* c, const StepArgs& a, uint32_t flags, ui
   PROF(c, P_SCAN_BLOCKS, launch_scan_blocks(c->block_sum, (uint32_t)sweep_blocks(n), c->ctrl, st));
   PROF(c, P_SWEEP_FILL,
        launch_sweep_fill(c->grid, c->pp, c->rp, a, c->key[r], c->id[r], c->spos, c->cell_start, c->block_sum, c->ctrl,
-                         c->deg, c->off, c->adj, c->prio, c->want[0], c->head, c->act[0], n, st));
+                         c->deg, c->off, c->adj, c->prio, c->want[0], c->head, c->act[0], c->level, n, st));
   if (flags & LM_STEP_INTERACT) {
     RoundBufs rb;
     rb.off = c->off;
@@ -366,6 +366,7 @@ cudaError_t enqueue_interaction(lm_ctx* c, const StepArgs& a, uint32_t flags, ui
     rb.head = c->head;
     rb.act[0] = c->act[0];
     rb.act[1] = c->act[1];
+    rb.level = c->level;
     rb.plog = (flags & LM_STEP_LOG_PAIRS) ? c->plog : nullptr;
     rb.plog_cap = c->plog_cap;
     cudaEvent_t pa = prof_begin(c);
@@ -514,7 +515,7 @@ int lm_ctx_destroy(lm_ctx* c) {
   if (c->graph) cudaGraphDestroy(c->graph);
   void* bufs[] = {c->uv,          c->xo,      c->yo,      c->plon,   c->plat,      c->species,   c->status,
                   c->key[0],      c->key[1],  c->id[0],   c->id[1],  c->spos,      c->deg,       c->off,
-                  c->block_sum,   c->head,    c->want[0], c->want[1], c->act[0],   c->act[1],    c->sort_counts,
+                  c->block_sum,   c->head,    c->want[0], c->want[1], c->act[0],   c->act[1],    c->sort_counts, c->level,
                   c->digit_total, c->adj,     c->prio,    c->cell_start, c->ctrl,  c->plog};
   for (void* p : bufs)
     if (p) cudaFree(p);
@@ -818,10 +819,9 @@ int lm_query_pairs(lm_ctx* c, int64_t n, const float* lon, const float* lat, int
     }
   std::sort(pairs.begin(), pairs.end());
   *n_pairs = (int64_t)pairs.size();
-  if ((int64_t)pairs.size() > cap || (!pi || !pj)) {
-    if (pairs.empty()) return LM_OK;
+  if (!pi || !pj) return LM_OK;  // count query
+  if ((int64_t)pairs.size() > cap)
     return fail(c, LM_ERR_CAPACITY, "pair buffer holds %lld pairs, %zu needed", (long long)cap, pairs.size());
-  }
   for (size_t k = 0; k < pairs.size(); ++k) {
     pi[k] = (int32_t)(pairs[k] >> 32);
     pj[k] = (int32_t)(pairs[k] & 0xffffffffu);
@@ -868,7 +868,8 @@ int lm_pairs_get(lm_ctx* c, int32_t* pi, int32_t* pj, int32_t* round, int64_t ca
   uint32_t m = std::min(c->hctrl->plog_n, c->plog_cap);
   *n = m;
   if (m == 0) return LM_OK;
-  if (m > cap || !pi || !pj || !round) return fail(c, LM_ERR_CAPACITY, "pair log holds %u pairs", m);
+  if (!pi || !pj || !round) return LM_OK;  // count query
+  if ((int64_t)m > cap) return fail(c, LM_ERR_CAPACITY, "pair log holds %u pairs", m);
   std::vector<uint32_t> h((size_t)3 * m);
   CK(cudaMemcpyAsync(h.data(), c->plog, h.size() * 4, cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));

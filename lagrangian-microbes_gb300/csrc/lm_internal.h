@@ -14,7 +14,7 @@
 //              uint32 adj[cap]            (neighbour lists in cell-order indices, each list sorted by
 //                                          descending pair priority)
 //              uint64 prio[cap]           (pair priorities while the lists are sorted)
-//              uint32 want[2][N], head[N], act[2][N]  (interaction rounds)
+//              uint32 want[N], head[N], level[N], act[N]  (interaction dataflow)
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -130,8 +130,8 @@ void launch_scan_blocks(uint32_t* block_sum, uint32_t nblocks, Ctrl* ctrl, cudaS
 void launch_sweep_fill(const CellGrid& g, const PairParams& pp, const RpsParams& rp, const StepArgs& a,
                        const uint32_t* key, const uint32_t* id, const float2* spos, const uint32_t* cell_start,
                        const uint32_t* block_sum, Ctrl* ctrl, const uint32_t* deg, uint32_t* off, uint32_t* adj,
-                       unsigned long long* prio, uint32_t* want0, uint32_t* head, uint32_t* act0, uint32_t n,
-                       cudaStream_t st);
+                       unsigned long long* prio, uint32_t* want0, uint32_t* head, uint32_t* act0, uint32_t* level,
+                       uint32_t n, cudaStream_t st);
 
 // Interaction rounds (cooperative persistent kernel).
 struct RoundBufs {
@@ -143,7 +143,8 @@ struct RoundBufs {
   uint32_t* want[2];
   uint32_t* head;
   uint32_t* act[2];
-  uint32_t* plog;     // 3 x uint32 per logged pair (i, j, round) or nullptr
+  uint32_t* level;    // per vertex: level of its last applied pair
+  uint32_t* plog;     // 3 x uint32 per logged pair (i, j, level) or nullptr
   uint32_t plog_cap;  // entries
 };
 int rounds_grid(int device, int* block);

@@ -1,0 +1,145 @@
+"""Host-side logic and the C-ABI library surface (no GPU needed)."""
+
+import ctypes
+import os
+import re
+from datetime import datetime, timedelta
+
+import numpy as np
+import pytest
+from conftest import REPO
+
+
+def _declared_symbols():
+    with open(os.path.join(REPO, "include", "lm_api.h")) as f:
+        text = f.read()
+    return sorted(set(re.findall(r"^int\s+(lm_\w+)\s*\(", text, flags=re.M)))
+
+
+def test_library_builds_and_exports_every_declared_symbol(lm):
+    from lagrangian_microbes_gb300 import _lib
+    lib = _lib.load()
+    declared = _declared_symbols()
+    assert len(declared) >= 20
+    for name in declared:
+        assert hasattr(lib, name), name
+    assert set(declared) == set(_lib.SIGNATURES), "ctypes signatures must cover exactly the header"
+    assert lib.lm_version() == 1
+
+
+def test_library_has_sm103a_code(lm):
+    from lagrangian_microbes_gb300 import build
+    with open(build.LIB_PATH, "rb") as f:
+        blob = f.read()
+    assert b"sm_103a" in blob or b"sm_103" in blob
+
+
+def test_context_without_gpu_fails_cleanly(lm):
+    from lagrangian_microbes_gb300 import _lib
+    lib = _lib.load()
+    h = ctypes.c_void_p()
+    rc = lib.lm_ctx_create(0, ctypes.byref(h))
+    if rc == _lib.LM_OK:
+        lib.lm_ctx_destroy(h)
+        pytest.skip("a GPU is present")
+    assert rc in (_lib.LM_ERR_CUDA, _lib.LM_ERR_ARG)
+    buf = ctypes.create_string_buffer(256)
+    lib.lm_last_error(None, buf, 256)
+    assert buf.value
+    with pytest.raises(_lib.LMError):
+        _lib.Context(0)
+
+
+def test_null_context_is_rejected(lm):
+    from lagrangian_microbes_gb300 import _lib
+    lib = _lib.load()
+    assert lib.lm_sync(None) == _lib.LM_ERR_ARG
+    assert lib.lm_step(None, 0.0, 1.0, 1, 0, 1, 0.0, None, None, None, None) == _lib.LM_ERR_ARG
+
+
+def test_norm_codes(lm):
+    from lagrangian_microbes_gb300.engine import norm_code
+    assert norm_code(2) == 2 and norm_code(1) == 1 and norm_code(np.inf) == 0 and norm_code(float("inf")) == 0
+    with pytest.raises(ValueError):
+        norm_code(3)
+
+
+def test_rock_paper_scissors_surface(lm):
+    np.random.seed(0)
+    fn, params, props = lm.rock_paper_scissors(1000, 0.5, 0.6, 0.7)
+    sp = props["species"]
+    assert sp.dtype == np.int8 and set(np.unique(sp)) <= {1, 2, 3}
+    assert (params["pRS"], params["pPR"], params["pSP"]) == (0.5, 0.6, 0.7)
+    np.random.seed(0)
+    fn2, params2, props2 = lm.rock_paper_scissors(1000, 0.5, 0.6, 0.7)
+    np.testing.assert_array_equal(sp, props2["species"])
+    assert params["seed"] == params2["seed"]
+    assert fn is lm.rock_paper_scissors_interaction
+    with pytest.raises(NotImplementedError):
+        fn(params, props, 0, 1)
+    assert (lm.ROCK, lm.PAPER, lm.SCISSORS) == (1, 2, 3)
+
+
+def test_interaction_simulator_rejects_other_rules(lm, tmp_path):
+    from lagrangian_microbes_gb300.interaction_simulator import InteractionSimulator
+    with pytest.raises(NotImplementedError):
+        InteractionSimulator((lambda *a: None, {}, {"species": np.zeros(3, np.int8)}), 0.01, output_dir=str(tmp_path))
+    with pytest.raises(ValueError):
+        InteractionSimulator(lm.rock_paper_scissors(3, .5, .5, .5), 0.01, interaction_norm=3, output_dir=str(tmp_path))
+
+
+def test_particle_advecter_argument_checks(lm, tmp_path):
+    from lagrangian_microbes_gb300.particle_advecter import ParticleAdvecter, distribute_particles_across_tiles
+    fld = lm.uniform_field(195, 206, 20, 31, 0.25, 4)
+    lons, lats = np.linspace(200, 201, 12), np.linspace(25, 26, 12)
+    with pytest.raises(NotImplementedError):
+        ParticleAdvecter(lons, lats, N_procs=1, velocity_field="OSCAR", output_dir=str(tmp_path))
+    with pytest.raises(AssertionError):
+        ParticleAdvecter(lons, lats, N_procs=1, velocity_field="HYCOM", output_dir=str(tmp_path))
+    with pytest.raises(AssertionError):
+        ParticleAdvecter(lons, lats, N_procs=0, velocity_field=fld, output_dir=str(tmp_path))
+    with pytest.raises(AssertionError):
+        ParticleAdvecter(lons, lats, N_procs=5, velocity_field=fld, output_dir=str(tmp_path))
+    pa = ParticleAdvecter(lons, lats, N_procs=3, velocity_field=fld, output_dir=str(tmp_path / "out"), Kh=100)
+    assert pa.N_procs == min(3, os.cpu_count()) and pa.particles_per_tile * pa.N_procs == 12
+    assert pa.Kh == pytest.approx(1e-8) and os.path.isdir(tmp_path / "out")
+    tl, ta = distribute_particles_across_tiles(lons, lats, 4)
+    assert len(tl) == 4 and all(t.size == 3 for t in tl)
+    np.testing.assert_array_equal(np.concatenate(tl), lons)
+    with pytest.raises(AssertionError):
+        distribute_particles_across_tiles(lons, lats, 5)
+
+
+def test_velocity_field_descending_latitude_is_flipped(lm):
+    lon = np.array([0.0, 1.0, 2.0])
+    lat = np.array([2.0, 1.0])
+    u = np.arange(12, dtype=np.float32).reshape(2, 2, 3)
+    f = lm.VelocityField(lon, lat, np.array([0.0, 3600.0]), u, -u)
+    assert f.lat[0] == 1.0
+    np.testing.assert_array_equal(f.u[:, 0, :], u[:, 1, :])
+    assert f.seconds(f.epoch + timedelta(hours=2)) == 7200.0
+
+
+def test_netcdf_roundtrip(tmp_path):
+    from lagrangian_microbes_gb300.ncio import read_particle_file, write_particle_file
+    lon = np.random.default_rng(0).random((7, 4)).astype(np.float32)
+    sp = np.arange(28, dtype=np.int8).reshape(7, 4)
+    path = str(tmp_path / "m.nc")
+    write_particle_file(path, {"longitude": lon, "species": sp}, datetime(2017, 1, 1), np.arange(4) * 3600.0)
+    d = read_particle_file(path)
+    np.testing.assert_array_equal(d["longitude"], lon)
+    np.testing.assert_array_equal(d["species"], sp)
+    np.testing.assert_array_equal(d["particle number"], np.arange(1, 8))
+    np.testing.assert_array_equal(d["time"], np.arange(4) * 3600.0)
+
+
+def test_shard_partitions(lm):
+    from lagrangian_microbes_gb300.replicas import shard, shard_weighted
+    for n in (0, 1, 7, 256):
+        for w in (1, 2, 3, 8):
+            parts = [list(shard(n, w, r)) for r in range(w)]
+            assert sorted(sum(parts, [])) == list(range(n))
+            assert max(map(len, parts)) - min(map(len, parts)) <= 1
+    weights = np.random.default_rng(1).random(50).tolist()
+    got = sorted(sum((shard_weighted(weights, 4, r) for r in range(4)), []))
+    assert got == list(range(50))
