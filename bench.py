@@ -124,24 +124,24 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-# Algorithmic bytes of one launch of each kernel (n = microbes, p = unordered pairs of the step,
-# g = grid nodes, frames = distinct frames read per step).
-def kernel_bytes(name: str, n: int, p: float, g: int, frames: int) -> float:
+# Algorithmic bytes of one launch of each kernel: n = microbes, p = unordered pairs of the step,
+# g = grid nodes per frame, frames = distinct frames read per step, cells = binning cells used.
+def kernel_bytes(name: str, n: int, p: float, g: int, frames: int, cells: float) -> float:
     if name == "k_advect":
-        # read state 8 + status 1, write state 8 + position 8 + key/id 8, plus the frames read
-        return 33.0 * n + 8.0 * g * frames
-    if name == "k_radix_scatter":
-        return 16.0 * n  # read + write (key, id)
-    if name == "k_radix_hist":
-        return 4.0 * n
-    if name == "k_cells":
-        return 20.0 * n  # keys (4+4 neighbour), id 4, gather 8, write spos 8 (cell starts are O(cells touched))
-    if name == "k_sweep_count":
-        return 16.0 * n  # key 4 + spos 8 + deg 4 (neighbour reads hit L1/L2)
-    if name == "k_sweep_fill":
-        return 24.0 * n + 2 * p * 12.0  # key, spos, id, deg, off, want/head + per directed entry adj 4 + prio 8
+        # read offsets 8 + status 1, write offsets 8 + recorded position 8; plus the frames read
+        return 25.0 * n + 8.0 * g * frames
+    if name == "k_keys":
+        return 17.0 * n  # read position 8 + status 1, write key + rank 8
+    if name == "k_cscan":
+        return 12.0 * cells  # read counts (twice: reduce + scan) and write starts, 4 B per cell each
+    if name == "k_scatter":
+        return 40.0 * n  # read key, rank, position, cell start; write id, key, ensemble, position
+    if name == "k_sweep":
+        return 36.0 * n + 2 * p * 4.0  # vertex reads 20 + per-vertex state writes 16, list entries 4 B
     if name == "k_rounds":
-        return 2 * p * 4.0 + 3.0 * p + 12.0 * n  # adjacency read once, species r/w per pair, per-vertex state
+        return 2 * p * 4.0 + 3.0 * p + 12.0 * n  # list entries once, species r/r/w per pair, vertex state
+    if name == "k_census":
+        return 2.0 * n
     return 0.0
 
 
@@ -226,10 +226,11 @@ def run_gb300(args):
     sim.ctx.profile_enable(False)
     g = fld.u.shape[1] * fld.u.shape[2]
     kernels = {}
+    cells = float(sim.stats()["cells"])
     for name, (ms, cnt) in prof.items():
         if cnt:
             kernels[name] = {"launches": cnt, "total_ms": ms, "avg_us": 1e3 * ms / cnt,
-                             "bytes_per_launch": kernel_bytes(name, n, pairs_per_step, g, 2)}
+                             "bytes_per_launch": kernel_bytes(name, n, pairs_per_step, g, 2, cells)}
     total_k = sum(v["total_ms"] for v in kernels.values()) or 1.0
     for v in kernels.values():
         v["share"] = v["total_ms"] / total_k

@@ -63,10 +63,13 @@ typedef struct lm_stats {
   int64_t out_of_bounds;  /* particles flagged out of domain or non-finite (sticky) */
   int64_t step;           /* device step counter (next step index) */
   int64_t census[4];      /* species counts after the last step: [0]=other, [1]=rock, [2]=paper, [3]=scissors */
-  int64_t adj_capacity;   /* neighbour-list capacity (directed entries) */
+  int64_t adj_capacity;   /* capacity of the long neighbour-list area (entries) */
   int64_t regrows;        /* neighbour-list regrowths since creation */
   int64_t pairs_total;    /* unordered pairs summed over interaction steps since lm_stats_reset */
   int64_t steps_total;    /* interaction steps since lm_stats_reset */
+  int64_t cells;          /* binning cells of the last step (all ensembles) */
+  int64_t long_lists;     /* microbes of the last step with more than 8 neighbours */
+  int64_t n_ensembles;
 } lm_stats;
 
 int lm_version(void);
@@ -88,12 +91,24 @@ int lm_sync(lm_ctx* ctx);
  * (particle_advecter.py:177-184). */
 int lm_field_upload(lm_ctx* ctx, const float* u, const float* v, int nt, int ny, int nx, const double* lon,
                     const double* lat, const double* t_sec);
+/* n_fields fields on one shared grid: u, v float32 [n_fields][nt][ny][nx]. With several ensembles,
+ * ensemble e reads field e (n_fields == number of ensembles) or all read field 0 (n_fields == 1).
+ * Batched form of the per-tile field build of particle_advecter.py:177-184 (one field per
+ * ensemble of the sweep in sandbox/slurm_rock_paper_scissors.py). */
+int lm_field_upload_batch(lm_ctx* ctx, int n_fields, const float* u, const float* v, int nt, int ny, int nx,
+                          const double* lon, const double* lat, const double* t_sec);
 
 /* Particles: positions in degrees (float64, as uniform_particle_locations returns them) and species
  * (int8, ROCK=1 PAPER=2 SCISSORS=3; NULL keeps all species at 0). Requires the field (the state is
  * stored as float32 offsets from the field origin). Replaces ParticleSet.from_list
  * (particle_advecter.py:186) and the species array of rock_paper_scissors (interactions.py:45). */
 int lm_particles_upload(lm_ctx* ctx, int64_t n, const double* lon, const double* lat, const int8_t* species);
+/* n_ens independent ensembles in one context (counts[e] microbes each; positions and species
+ * concatenated in ensemble order). Every per-step kernel then covers all ensembles in one launch;
+ * microbes of different ensembles never pair. Replaces the per-job ensembles of
+ * sandbox/slurm_rock_paper_scissors.py:77-134 and the joblib tiles of particle_advecter.py:143-148. */
+int lm_ensembles_upload(lm_ctx* ctx, int n_ens, const int64_t* counts, const double* lon, const double* lat,
+                        const int8_t* species);
 /* Current state: absolute float32 lon/lat (after any diffusion kick), species, status (0 ok,
  * 1 out of domain, 2 non-finite). Any pointer may be NULL. */
 int lm_particles_download(lm_ctx* ctx, float* lon, float* lat, int8_t* species, uint8_t* status);
@@ -107,6 +122,13 @@ int lm_species_upload(lm_ctx* ctx, int64_t n, const int8_t* species);
  * per-pair uniform (replaces np.random.rand at interactions.py:20). */
 int lm_set_interaction(lm_ctx* ctx, double radius, int norm, double p_rs, double p_pr, double p_sp,
                        uint64_t seed);
+/* Per-ensemble forward probabilities and seeds (arrays of n_ens; radius and norm stay those of
+ * lm_set_interaction). Each ensemble draws from its own Philox stream keyed by its seed and its
+ * local microbe indices, so it evolves exactly as it would alone in a context. */
+int lm_set_ensemble_params(lm_ctx* ctx, int n_ens, const double* p_rs, const double* p_pr, const double* p_sp,
+                           const uint64_t* seeds);
+/* Binning cell size in units of the radius (default 1.004; any value >= 1.004 gives the same pairs). */
+int lm_set_cell_factor(lm_ctx* ctx, double factor);
 
 /* n_steps fused steps starting at field time t_sec with global step index step0. Each step:
  * advect (flags & LM_STEP_ADVECT), then bin + pair + interact (flags & LM_STEP_INTERACT) on the
@@ -130,8 +152,9 @@ int lm_query_pairs(lm_ctx* ctx, int64_t n, const float* lon, const float* lat, i
 int lm_interact(lm_ctx* ctx, int64_t n, const float* lon, const float* lat, int64_t step_index,
                 uint32_t flags);
 
-/* Pairs applied by the last interaction step when LM_STEP_LOG_PAIRS was set, in application order
- * (round by round; pairs of one round are disjoint). i < j are particle indices. */
+/* Pairs applied by the last interaction step when LM_STEP_LOG_PAIRS was set, in an application
+ * order equal in effect to the one used: by level (pairs of one level share no microbe), then
+ * (i, j). i < j are particle indices in upload order. */
 int lm_pairs_get(lm_ctx* ctx, int32_t* pi, int32_t* pj, int32_t* round, int64_t cap, int64_t* n);
 
 /* Capture `steps_per_graph` fused steps (flags as lm_step, Kh as lm_step) into a CUDA graph. The
@@ -148,6 +171,10 @@ int lm_set_step(lm_ctx* ctx, int64_t step);
 
 int lm_stats_get(lm_ctx* ctx, lm_stats* out);
 int lm_stats_reset(lm_ctx* ctx);
+/* Species counts of every ensemble after the last step run with LM_STEP_CENSUS:
+ * out[4*e + s] for species s (0 = values outside 1..3); cap >= 4 * n_ens. Replaces the species
+ * time series of analysis.py:20-35 computed from microbe_data.nc. */
+int lm_census_get(lm_ctx* ctx, int64_t* out, int64_t cap);
 
 /* Per-kernel CUDA-event timing of plain (non-graph) launches: enable (1) / disable (0) and reset the
  * accumulators; read kernel k (0 <= k < lm_profile_count()): its name, summed duration and launch

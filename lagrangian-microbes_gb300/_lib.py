@@ -69,6 +69,9 @@ class Stats(ctypes.Structure):
         ("regrows", ctypes.c_int64),
         ("pairs_total", ctypes.c_int64),
         ("steps_total", ctypes.c_int64),
+        ("cells", ctypes.c_int64),
+        ("long_lists", ctypes.c_int64),
+        ("n_ensembles", ctypes.c_int64),
     ]
 
     def as_dict(self) -> dict:
@@ -96,6 +99,11 @@ SIGNATURES = {
     "lm_ctx_set_stream": [P, ctypes.c_size_t],
     "lm_sync": [P],
     "lm_field_upload": [P, P, P, I32, I32, I32, P, P, P],
+    "lm_field_upload_batch": [P, I32, P, P, I32, I32, I32, P, P, P],
+    "lm_ensembles_upload": [P, I32, P, P, P, P],
+    "lm_set_ensemble_params": [P, I32, P, P, P, P],
+    "lm_set_cell_factor": [P, F64],
+    "lm_census_get": [P, P, I64],
     "lm_particles_upload": [P, I64, P, P, P],
     "lm_particles_download": [P, P, P, P, P],
     "lm_species_upload": [P, I64, P],
@@ -145,6 +153,8 @@ def ptr(a: np.ndarray | None):
         return None
     if not a.flags["C_CONTIGUOUS"]:
         raise ValueError("arrays passed to liblmgb300 must be C-contiguous")
+    if not a.dtype.isnative:
+        raise ValueError("arrays passed to liblmgb300 must be in native byte order")
     return a.ctypes.data_as(ctypes.c_void_p)
 
 

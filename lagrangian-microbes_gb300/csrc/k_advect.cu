@@ -9,8 +9,10 @@
 // (lat first, then lon, uniform in (-1,1) times sqrt(6 |dt| Kh)) is fused and applied after the
 // position is recorded, as in the reference.
 //
-// The same kernel writes the binning input of the pair search (cell key + particle id, absolute
-// float32 position), so the advected positions never make a separate trip through HBM.
+// One thread per particle slot; every 256-slot block belongs to one ensemble, whose field frames,
+// seed and slot base are loaded once per block. The block also reduces the bounding box of its
+// advected positions into its ensemble's box (ordered-int atomics), from which the binning grid
+// of this step is built.
 #include "lm_internal.h"
 #include "lm_philox.cuh"
 
@@ -53,15 +55,15 @@ __device__ __forceinline__ Stage stage_at(const FieldView& f, double t) {
 }
 
 // Velocity in deg/s at offset position (xo, yo). Returns false outside the grid or on NaN.
-__device__ __forceinline__ bool velocity(const FieldView& f, const Stage& s, float xo, float yo, float& dlon,
-                                         float& dlat) {
+__device__ __forceinline__ bool velocity(const FieldView& f, const float2* __restrict__ uv, const Stage& s, float xo,
+                                         float yo, float& dlon, float& dlat) {
   float fx = (xo - f.gx0) * f.inv_dx;
   float fy = (yo - f.gy0) * f.inv_dy;
   if (!(fx >= 0.f && fx <= f.max_fx && fy >= 0.f && fy <= f.max_fy)) return false;
   int i = min((int)fx, f.nx - 2);
   int j = min((int)fy, f.ny - 2);
   float a = fx - (float)i, b = fy - (float)j;
-  const float2* p = f.uv + ((size_t)s.k * f.ny + j) * f.nx + i;
+  const float2* p = uv + ((size_t)s.k * f.ny + j) * f.nx + i;
   float2 c00 = __ldg(p), c01 = __ldg(p + 1), c10 = __ldg(p + f.nx), c11 = __ldg(p + f.nx + 1);
   float w00 = (1.f - a) * (1.f - b), w01 = a * (1.f - b), w10 = (1.f - a) * b, w11 = a * b;
   float u = w00 * c00.x + w01 * c01.x + w10 * c10.x + w11 * c11.x;
@@ -82,22 +84,47 @@ __device__ __forceinline__ bool velocity(const FieldView& f, const Stage& s, flo
   return true;
 }
 
-__device__ __forceinline__ uint32_t cell_key(const CellGrid& g, float ax, float ay) {
-  float fx = (ax - g.x0) * g.inv_c;
-  float fy = (ay - g.y0) * g.inv_c;
-  fx = fminf(fmaxf(fx, 0.f), (float)(g.ncx - 1));
-  fy = fminf(fmaxf(fy, 0.f), (float)(g.ncy - 1));
-  return (uint32_t)(int)fy * (uint32_t)g.ncx + (uint32_t)(int)fx;
+// Block-level bounding box of valid positions, merged into the ensemble's box.
+__device__ __forceinline__ void block_bbox(bool valid, float x, float y, uint32_t* ebox_e) {
+  __shared__ float red[4][SLOT_BLOCK / 32];
+  float mnx = valid ? x : INFINITY, mny = valid ? y : INFINITY;
+  float mxx = valid ? x : -INFINITY, mxy = valid ? y : -INFINITY;
+  for (int o = 16; o > 0; o >>= 1) {
+    mnx = fminf(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
+    mny = fminf(mny, __shfl_xor_sync(0xffffffffu, mny, o));
+    mxx = fmaxf(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
+    mxy = fmaxf(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
+  }
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    red[0][w] = mnx;
+    red[1][w] = mny;
+    red[2][w] = mxx;
+    red[3][w] = mxy;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int k = 1; k < (int)(SLOT_BLOCK / 32); ++k) {
+      mnx = fminf(mnx, red[0][k]);
+      mny = fminf(mny, red[1][k]);
+      mxx = fmaxf(mxx, red[2][k]);
+      mxy = fmaxf(mxy, red[3][k]);
+    }
+    if (mnx <= mxx) {
+      atomicMin(ebox_e + 0, enc_f(mnx));
+      atomicMin(ebox_e + 1, enc_f(mny));
+      atomicMax(ebox_e + 2, enc_f(mxx));
+      atomicMax(ebox_e + 3, enc_f(mxy));
+    }
+  }
 }
 
-__global__ void __launch_bounds__(256) k_advect(FieldView f, CellGrid g, StepArgs a, Ctrl* ctrl,
-                                                float* __restrict__ xo, float* __restrict__ yo,
-                                                uint8_t* __restrict__ status, float* __restrict__ plon,
-                                                float* __restrict__ plat, uint32_t* __restrict__ key,
-                                                uint32_t* __restrict__ id, uint32_t n) {
+__global__ void __launch_bounds__(SLOT_BLOCK) k_advect(FieldView f, StepArgs a, Bufs b, Ctrl* ctrl) {
   __shared__ Stage sh[3];
   __shared__ uint32_t sh_step;
   __shared__ int sh_skip;
+  __shared__ EnsInfo sh_ens;
+  __shared__ uint32_t sh_e;
   if (threadIdx.x == 0) {
     uint32_t step = a.use_ctrl_step ? ctrl->step : a.step0;
     double t = a.t_start + (double)(int)(step - a.step0) * a.dt;
@@ -108,21 +135,27 @@ __global__ void __launch_bounds__(256) k_advect(FieldView f, CellGrid g, StepArg
     int ok = sh[0].ok && sh[1].ok && sh[2].ok;
     sh_skip = ctrl->halt != 0 || !ok;
     if (!ok && blockIdx.x == 0) atomicOr(&ctrl->err, ERRB_TIME);
+    sh_e = b.block_ens[blockIdx.x];
+    sh_ens = b.ens[sh_e];
   }
   __syncthreads();
   if (sh_skip) return;
-  uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= n) return;
+  const uint32_t p = blockIdx.x * SLOT_BLOCK + threadIdx.x;
+  const float2* uv = f.uv + sh_ens.field_off;
 
-  float x = xo[p], y = yo[p];
-  uint32_t st = status[p];
+  uint32_t st = (p < b.nslots) ? b.status[p] : STATUS_PAD;
+  float x = 0.f, y = 0.f;
+  if (st != STATUS_PAD) {
+    x = b.xo[p];
+    y = b.yo[p];
+  }
   const float dt = (float)a.dt;
-  if (st == 0) {
+  if (st == STATUS_OK) {
     float k1x, k1y, k2x, k2y, k3x, k3y, k4x, k4y;
-    bool ok = velocity(f, sh[0], x, y, k1x, k1y);
-    ok = ok && velocity(f, sh[1], x + 0.5f * dt * k1x, y + 0.5f * dt * k1y, k2x, k2y);
-    ok = ok && velocity(f, sh[1], x + 0.5f * dt * k2x, y + 0.5f * dt * k2y, k3x, k3y);
-    ok = ok && velocity(f, sh[2], x + dt * k3x, y + dt * k3y, k4x, k4y);
+    bool ok = velocity(f, uv, sh[0], x, y, k1x, k1y);
+    ok = ok && velocity(f, uv, sh[1], x + 0.5f * dt * k1x, y + 0.5f * dt * k1y, k2x, k2y);
+    ok = ok && velocity(f, uv, sh[1], x + 0.5f * dt * k2x, y + 0.5f * dt * k2y, k3x, k3y);
+    ok = ok && velocity(f, uv, sh[2], x + dt * k3x, y + dt * k3y, k4x, k4y);
     if (ok) {
       float nx = x + (k1x + 2.f * k2x + 2.f * k3x + k4x) * (dt * (1.0f / 6.0f));
       float ny = y + (k1y + 2.f * k2y + 2.f * k3y + k4y) * (dt * (1.0f / 6.0f));
@@ -130,61 +163,117 @@ __global__ void __launch_bounds__(256) k_advect(FieldView f, CellGrid g, StepArg
         x = nx;
         y = ny;
       } else {
-        st = 2u;
+        st = STATUS_NAN;
       }
     } else {
-      st = (isfinite(x) && isfinite(y)) ? 1u : 2u;
+      st = (isfinite(x) && isfinite(y)) ? STATUS_OOB : STATUS_NAN;
     }
-    if (st) {
+    if (st != STATUS_OK) {
       atomicAdd(&ctrl->oob, 1u);
-      atomicOr(&ctrl->err, st == 1u ? (uint32_t)ERRB_OOB : (uint32_t)ERRB_NAN);
-      status[p] = (uint8_t)st;
+      atomicOr(&ctrl->err, st == STATUS_OOB ? (uint32_t)ERRB_OOB : (uint32_t)ERRB_NAN);
+      b.status[p] = (uint8_t)st;
     }
   }
   // Recorded position (before the kick), absolute float32 as the reference stores it.
-  float ax = __fadd_rn(f.org_lon, x), ay = __fadd_rn(f.org_lat, y);
-  plon[p] = ax;
-  plat[p] = ay;
-  key[p] = st ? g.ncells : cell_key(g, ax, ay);
-  id[p] = p;
-  if (a.kick != 0.f && st == 0) {
-    float ulat, ulon;
-    diffusion_draw(p, sh_step, a.seed_lo, a.seed_hi, &ulat, &ulon);
-    y = y + ulat * a.kick;
-    x = x + ulon * a.kick;
-    xo[p] = x;
-    yo[p] = y;
-  } else if (st == 0) {
-    xo[p] = x;
-    yo[p] = y;
+  const float ax = __fadd_rn(f.org_lon, x), ay = __fadd_rn(f.org_lat, y);
+  if (st != STATUS_PAD) {
+    b.plon[p] = ax;
+    b.plat[p] = ay;
+  }
+  if (st == STATUS_OK) {
+    if (a.kick != 0.f) {
+      float ulat, ulon;
+      diffusion_draw(p - sh_ens.base, sh_step, sh_ens.seed_lo, sh_ens.seed_hi, &ulat, &ulon);
+      y = y + ulat * a.kick;
+      x = x + ulon * a.kick;
+    }
+    b.xo[p] = x;
+    b.yo[p] = y;
+  }
+  block_bbox(st == STATUS_OK, ax, ay, b.ebox + 4 * sh_e);
+}
+
+void launch_advect(const FieldView& f, const StepArgs& a, const Bufs& b, Ctrl* ctrl, cudaStream_t st) {
+  if (b.nslots == 0) return;
+  k_advect<<<(b.nslots + SLOT_BLOCK - 1) / SLOT_BLOCK, SLOT_BLOCK, 0, st>>>(f, a, b, ctrl);
+}
+
+// Bounding boxes from the recorded positions (two-phase interaction path and step re-runs).
+__global__ void __launch_bounds__(SLOT_BLOCK) k_bbox(Bufs b, Ctrl* ctrl, int use_status) {
+  if (ctrl->halt) return;
+  const uint32_t p = blockIdx.x * SLOT_BLOCK + threadIdx.x;
+  const uint32_t e = b.block_ens[blockIdx.x];
+  bool valid = p < b.nslots;
+  float x = 0.f, y = 0.f;
+  if (valid) {
+    valid = use_status ? (b.status[p] == STATUS_OK) : (p - b.ens[e].base < b.ens[e].n);
+    x = b.plon[p];
+    y = b.plat[p];
+    valid = valid && isfinite(x) && isfinite(y);
+  }
+  block_bbox(valid, x, y, b.ebox + 4 * e);
+}
+
+void launch_bbox(const Bufs& b, Ctrl* ctrl, bool use_status, cudaStream_t st) {
+  if (b.nslots == 0) return;
+  k_bbox<<<(b.nslots + SLOT_BLOCK - 1) / SLOT_BLOCK, SLOT_BLOCK, 0, st>>>(b, ctrl, use_status ? 1 : 0);
+}
+
+// Per-step bookkeeping: reset the per-step counters and the ensemble boxes (start), advance the
+// device step counter (end).
+__global__ void k_step_begin(Bufs b, Ctrl* ctrl) {
+  if (ctrl->halt) return;
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  for (uint32_t e = t; e < b.n_ens; e += gridDim.x * blockDim.x) {
+    b.ebox[4 * e + 0] = 0xffffffffu;  // min: start at the largest encoding
+    b.ebox[4 * e + 1] = 0xffffffffu;
+    b.ebox[4 * e + 2] = 0u;           // max: start at the smallest encoding
+    b.ebox[4 * e + 3] = 0u;
+    b.census[4 * e + 0] = b.census[4 * e + 1] = b.census[4 * e + 2] = b.census[4 * e + 3] = 0u;
+  }
+  if (t == 0) {
+    ctrl->act_n = 0;
+    ctrl->plog_n = 0;
+    ctrl->rounds = 0;
+    ctrl->n_valid = 0;
+    ctrl->n_dir = 0;
+    ctrl->n_long = 0;
+    ctrl->ovf_used = 0;
+    ctrl->census[0] = ctrl->census[1] = ctrl->census[2] = ctrl->census[3] = 0;
   }
 }
 
-void launch_advect(const FieldView& f, const CellGrid& g, const StepArgs& a, Ctrl* ctrl, float* xo, float* yo,
-                   uint8_t* status, float* plon, float* plat, uint32_t* key, uint32_t* id, uint32_t n,
-                   cudaStream_t st) {
-  if (n == 0) return;
-  k_advect<<<(n + 255) / 256, 256, 0, st>>>(f, g, a, ctrl, xo, yo, status, plon, plat, key, id, n);
-}
-
-// Binning input from externally supplied positions (the interaction phase of the two-phase
-// reference workflow, interaction_simulator.py:88-93, reads positions from particle_data.nc).
-__global__ void k_keys_from_pos(CellGrid g, Ctrl* ctrl, const float* __restrict__ lon, const float* __restrict__ lat,
-                                uint32_t* __restrict__ key, uint32_t* __restrict__ id, uint32_t n) {
+__global__ void k_step_end(Ctrl* ctrl, int interact) {
   if (ctrl->halt) return;
-  uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= n) return;
-  float ax = lon[p], ay = lat[p];
-  bool ok = isfinite(ax) && isfinite(ay);
-  key[p] = ok ? cell_key(g, ax, ay) : g.ncells;
-  id[p] = p;
-  if (!ok) atomicOr(&ctrl->err, (uint32_t)ERRB_NAN);
+  if (interact) {
+    ctrl->pairs_total += ctrl->n_dir / 2;
+    ctrl->steps_total += 1;
+  }
+  ctrl->step += 1;
 }
 
-void launch_keys_from_pos(const CellGrid& g, Ctrl* ctrl, const float* lon, const float* lat, uint32_t* key,
-                          uint32_t* id, uint32_t n, cudaStream_t st) {
-  if (n == 0) return;
-  k_keys_from_pos<<<(n + 255) / 256, 256, 0, st>>>(g, ctrl, lon, lat, key, id, n);
+void launch_step_begin(const Bufs& b, Ctrl* ctrl, cudaStream_t st) {
+  int grid = (int)((b.n_ens + 255) / 256);
+  if (grid < 1) grid = 1;
+  if (grid > 64) grid = 64;
+  k_step_begin<<<grid, 256, 0, st>>>(b, ctrl);
+}
+void launch_step_end(Ctrl* ctrl, bool interact, cudaStream_t st) { k_step_end<<<1, 1, 0, st>>>(ctrl, interact ? 1 : 0); }
+
+// Gathers from the padded slot layout into caller order (map[slot] = caller index or -1).
+template <class T>
+__global__ void k_unpad(const T* __restrict__ src, T* __restrict__ dst, const int32_t* __restrict__ map, uint32_t n) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const int32_t q = map[p];
+  if (q >= 0) dst[q] = src[p];
+}
+
+void launch_unpad(const float* src, float* dst, const int32_t* map, uint32_t nslots, cudaStream_t st) {
+  if (nslots) k_unpad<float><<<(nslots + 255) / 256, 256, 0, st>>>(src, dst, map, nslots);
+}
+void launch_unpad8(const int8_t* src, int8_t* dst, const int32_t* map, uint32_t nslots, cudaStream_t st) {
+  if (nslots) k_unpad<int8_t><<<(nslots + 255) / 256, 256, 0, st>>>(src, dst, map, nslots);
 }
 
 }  // namespace lm

@@ -1,24 +1,19 @@
-// K2: uniform-cell binning. A stable LSD radix sort of (cell key, particle id) with 8-bit digits,
-// then a pass that records the first sorted index of every occupied cell and gathers positions
-// into cell order. This replaces the KD-tree build of the reference, cKDTree(X)
+// K2: uniform-cell binning, replacing the KD-tree build of the reference, cKDTree(X)
 // (interaction_simulator.py:93); the fixed-radius query that follows is K3 (k_pairs.cu).
 //
-// Each pass is three kernels: per-tile digit histograms, a per-digit scan over tiles (one block per
-// digit, so the scan is parallel in the digit), and a stable scatter whose in-tile ranks come from
-// warp-level __match_any_sync multisplit. Tiles are 256 threads x 8 keys, warp-striped so that
-// loads are coalesced and the in-tile order equals the input order (stability).
+// Each step builds, per ensemble, a cell grid over the bounding box of its advected positions
+// (cell size = cell_factor * r >= r, so every pair within r lies in the 3x3 neighbourhood), then
+// sorts the particles by cell with a single counting pass on the full cell key (a one-digit
+// radix sort): a warp-aggregated atomic count gives each particle its rank inside its cell, an
+// exclusive scan over the cells gives the cell starts, and a scatter writes particle id, key,
+// ensemble and position into cell order. The order inside a cell follows the atomics and is not
+// deterministic; nothing downstream depends on it (pair lists are re-sorted by pair priority and
+// every pair-order tie is broken by particle ids).
 #include "lm_internal.h"
 
 namespace lm {
 
-constexpr int RS_THREADS = 256;
-constexpr int RS_ITEMS = 8;
-constexpr int RS_TILE = RS_THREADS * RS_ITEMS;
-constexpr int RS_WARPS = RS_THREADS / 32;
-
-int sort_tiles(uint32_t n) { return (int)((n + RS_TILE - 1) / RS_TILE); }
-
-int radix_passes(int bits) { return bits <= 8 ? 1 : (bits + 7) / 8; }
+constexpr int GRID_THREADS = 1024;
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
   uint32_t m;
@@ -26,172 +21,250 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
   return m;
 }
 
-__global__ void __launch_bounds__(RS_THREADS) k_radix_hist(const uint32_t* __restrict__ key, uint32_t n, int shift,
-                                                           uint32_t* __restrict__ counts,
-                                                           uint32_t* __restrict__ digit_total, uint32_t ntiles,
-                                                           const Ctrl* ctrl) {
-  if (ctrl->halt) return;
-  __shared__ uint32_t h[256];
-  h[threadIdx.x] = 0;
-  __syncthreads();
-  const uint32_t base = blockIdx.x * RS_TILE;
-#pragma unroll
-  for (int k = 0; k < RS_ITEMS; ++k) {
-    uint32_t idx = base + k * RS_THREADS + threadIdx.x;
-    if (idx < n) atomicAdd(&h[(key[idx] >> shift) & 255u], 1u);
+// Cells of one ensemble's grid at cell size c (1 for an empty ensemble).
+__device__ __forceinline__ double grid_dims(const uint32_t* box, double c, double* ncx, double* ncy) {
+  const float mnx = dec_f(box[0]), mny = dec_f(box[1]), mxx = dec_f(box[2]), mxy = dec_f(box[3]);
+  if (!(mnx <= mxx && mny <= mxy)) {
+    *ncx = *ncy = 1.0;
+    return 1.0;
   }
-  __syncthreads();
-  uint32_t c = h[threadIdx.x];
-  counts[threadIdx.x * ntiles + blockIdx.x] = c;
-  if (c) atomicAdd(&digit_total[threadIdx.x], c);
+  *ncx = floor(((double)mxx - (double)mnx) / c) + 3.0;
+  *ncy = floor(((double)mxy - (double)mny) / c) + 3.0;
+  return *ncx * *ncy;
 }
 
-// Block d: global start of digit d for every tile = sum of totals of smaller digits + prefix over tiles.
-__global__ void __launch_bounds__(1024) k_radix_scan(uint32_t* __restrict__ counts,
-                                                     const uint32_t* __restrict__ digit_total, uint32_t ntiles,
-                                                     const Ctrl* ctrl) {
+// One block: grid geometry of every ensemble and the global cell numbering. If the cells would
+// exceed the capacity, the cell size grows (pairs stay exact because only c >= r matters).
+__global__ void __launch_bounds__(GRID_THREADS) k_grid(Bufs b, PairParams pp, Ctrl* ctrl) {
   if (ctrl->halt) return;
-  __shared__ uint32_t warp_sums[32];
-  __shared__ uint32_t carry;
-  const int d = blockIdx.x;
+  __shared__ double ws[GRID_THREADS / 32];
+  __shared__ double total_sh;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  // base = sum_{d' < d} digit_total[d']
-  uint32_t v = (threadIdx.x < (unsigned)d) ? digit_total[threadIdx.x] : 0u;
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  if (lane == 0) warp_sums[wid] = v;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    uint32_t s = 0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += warp_sums[w];
-    carry = s;
+  double c = (double)pp.cell_factor * pp.r;
+  if (!(c > 0.0)) c = 1e-3;
+  // 1. cell size: total cells over all ensembles must fit the capacity
+  for (int attempt = 0; attempt < 16; ++attempt) {
+    double t = 0;
+    for (uint32_t e = threadIdx.x; e < b.n_ens; e += GRID_THREADS) {
+      double nx, ny;
+      t += grid_dims(b.ebox + 4 * e, c, &nx, &ny);
+    }
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) ws[wid] = t;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double s = 0;
+      for (int w = 0; w < GRID_THREADS / 32; ++w) s += ws[w];
+      total_sh = s;
+    }
+    __syncthreads();
+    const double total = total_sh;
+    __syncthreads();
+    if (total <= (double)b.cells_cap) break;
+    c = c * sqrt(total / (double)b.cells_cap) * 1.02;
   }
+  // 2. per-ensemble geometry and exclusive cell offsets
+  __shared__ double carry_sh;
+  if (threadIdx.x == 0) carry_sh = 0;
   __syncthreads();
-  uint32_t* row = counts + (size_t)d * ntiles;
-  for (uint32_t start = 0; start < ntiles; start += blockDim.x) {
-    uint32_t i = start + threadIdx.x;
-    uint32_t x = (i < ntiles) ? row[i] : 0u;
-    // inclusive warp scan
-    uint32_t y = x;
+  for (uint32_t e0 = 0; e0 < b.n_ens; e0 += GRID_THREADS) {
+    const uint32_t e = e0 + threadIdx.x;
+    double nx = 0, ny = 0, cells = 0;
+    if (e < b.n_ens) cells = grid_dims(b.ebox + 4 * e, c, &nx, &ny);
+    double y = cells;
     for (int o = 1; o < 32; o <<= 1) {
-      uint32_t t = __shfl_up_sync(0xffffffffu, y, o);
+      const double t = __shfl_up_sync(0xffffffffu, y, o);
       if (lane >= o) y += t;
     }
+    if (lane == 31) ws[wid] = y;
     __syncthreads();
-    if (lane == 31) warp_sums[wid] = y;
+    double wp = 0, tot = 0;
+    for (int w = 0; w < GRID_THREADS / 32; ++w) {
+      if (w < wid) wp += ws[w];
+      tot += ws[w];
+    }
+    const double base = carry_sh + wp + y - cells;
+    if (e < b.n_ens) {
+      EnsGrid g;
+      const uint32_t* box = b.ebox + 4 * e;
+      const bool empty = !(dec_f(box[0]) <= dec_f(box[2]));
+      g.c = (float)c;
+      g.inv_c = (float)(1.0 / c);
+      g.x0 = empty ? 0.f : (float)((double)dec_f(box[0]) - c);
+      g.y0 = empty ? 0.f : (float)((double)dec_f(box[1]) - c);
+      g.ncx = (int)fmin(nx, 2147483647.0);
+      g.ncy = (int)fmin(ny, 2147483647.0);
+      g.cell_base = (uint32_t)fmin(base, 4294967295.0);
+      g.pad = 0;
+      b.grids[e] = g;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) carry_sh += tot;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double total = carry_sh;
+    if (total > (double)b.cells_cap) {  // cannot happen unless ensembles vastly outnumber cells
+      ctrl->ncells = b.cells_cap;
+      ctrl->halt = 1;
+      ctrl->halt_step = ctrl->step;
+      atomicOr(&ctrl->err, (uint32_t)ERRB_OVERFLOW);
+    } else {
+      ctrl->ncells = (uint32_t)total;
+    }
+  }
+}
+
+void launch_grid(const Bufs& b, const PairParams& pp, Ctrl* ctrl, cudaStream_t st) {
+  k_grid<<<1, GRID_THREADS, 0, st>>>(b, pp, ctrl);
+}
+
+// Cell key of every valid particle + its rank inside the cell (warp-aggregated atomics).
+__global__ void __launch_bounds__(SLOT_BLOCK) k_keys(Bufs b, Ctrl* ctrl, int use_status) {
+  if (ctrl->halt) return;
+  __shared__ EnsGrid g;
+  __shared__ EnsInfo info;
+  if (threadIdx.x == 0) {
+    const uint32_t e = b.block_ens[blockIdx.x];
+    g = b.grids[e];
+    info = b.ens[e];
+  }
+  __syncthreads();
+  const uint32_t p = blockIdx.x * SLOT_BLOCK + threadIdx.x;
+  bool valid = p < b.nslots;
+  float x = 0.f, y = 0.f;
+  if (valid) {
+    valid = use_status ? (b.status[p] == STATUS_OK) : (p - info.base < info.n);
+    x = b.plon[p];
+    y = b.plat[p];
+    valid = valid && isfinite(x) && isfinite(y);
+  }
+  uint32_t key = NONE;
+  if (valid) {
+    const float fx = fminf(fmaxf((x - g.x0) * g.inv_c, 0.f), (float)(g.ncx - 1));
+    const float fy = fminf(fmaxf((y - g.y0) * g.inv_c, 0.f), (float)(g.ncy - 1));
+    key = g.cell_base + (uint32_t)(int)fy * (uint32_t)g.ncx + (uint32_t)(int)fx;
+  }
+  const uint32_t peers = __match_any_sync(0xffffffffu, key);
+  uint32_t rank = 0;
+  if (valid) {
+    const int leader = __ffs(peers) - 1;
+    const int lane = threadIdx.x & 31;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(b.ccount + key, (uint32_t)__popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    rank = base + __popc(peers & lanemask_lt());
+  }
+  if (p < b.nslots) {
+    b.key[p] = key;
+    b.rank[p] = rank;
+  }
+}
+
+void launch_keys(const Bufs& b, Ctrl* ctrl, bool use_status, cudaStream_t st) {
+  if (b.nslots == 0) return;
+  k_keys<<<(b.nslots + SLOT_BLOCK - 1) / SLOT_BLOCK, SLOT_BLOCK, 0, st>>>(b, ctrl, use_status ? 1 : 0);
+}
+
+// Exclusive scan of the cell counts in two launches over SCAN_BLOCKS fixed chunks:
+// (1) chunk sums, (2) per-chunk scan with the prefix of the chunk sums. The counts are zeroed
+// as they are consumed, ready for the next counting pass.
+__device__ __forceinline__ void chunk_of(uint32_t ncells, uint32_t* c0, uint32_t* c1) {
+  const uint32_t per = (ncells + SCAN_BLOCKS - 1) / SCAN_BLOCKS;
+  *c0 = min(ncells, blockIdx.x * per);
+  *c1 = min(ncells, *c0 + per);
+}
+
+__device__ __forceinline__ uint32_t block_sum(uint32_t v) {
+  __shared__ uint32_t bs[32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) bs[threadIdx.x >> 5] = v;
+  __syncthreads();
+  uint32_t t = 0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += bs[w];
+  __syncthreads();
+  return t;
+}
+
+__global__ void __launch_bounds__(1024) k_cscan_reduce(Bufs b, Ctrl* ctrl) {
+  if (ctrl->halt) return;
+  uint32_t c0, c1;
+  chunk_of(ctrl->ncells, &c0, &c1);
+  uint32_t s = 0;
+  for (uint32_t i = c0 + threadIdx.x; i < c1; i += blockDim.x) s += b.ccount[i];
+  s = block_sum(s);
+  if (threadIdx.x == 0) b.csum[blockIdx.x] = s;
+}
+
+__global__ void __launch_bounds__(1024) k_cscan_down(Bufs b, Ctrl* ctrl) {
+  if (ctrl->halt) return;
+  __shared__ uint32_t ws[32];
+  __shared__ uint32_t carry;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const uint32_t ncells = ctrl->ncells;
+  uint32_t c0, c1;
+  chunk_of(ncells, &c0, &c1);
+  uint32_t pre = 0;
+  for (uint32_t k = threadIdx.x; k < blockIdx.x; k += blockDim.x) pre += b.csum[k];
+  pre = block_sum(pre);
+  if (threadIdx.x == 0) carry = pre;
+  __syncthreads();
+  for (uint32_t start = c0; start < c1; start += blockDim.x) {
+    const uint32_t i = start + threadIdx.x;
+    const uint32_t x = (i < c1) ? b.ccount[i] : 0u;
+    if (i < c1) b.ccount[i] = 0u;
+    uint32_t y = x;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, y, o);
+      if (lane >= o) y += t;
+    }
+    if (lane == 31) ws[wid] = y;
     __syncthreads();
     if (wid == 0) {
-      uint32_t w = (lane < (int)(blockDim.x >> 5)) ? warp_sums[lane] : 0u;
+      uint32_t w = (lane < (int)(blockDim.x >> 5)) ? ws[lane] : 0u;
       for (int o = 1; o < 32; o <<= 1) {
-        uint32_t t = __shfl_up_sync(0xffffffffu, w, o);
+        const uint32_t t = __shfl_up_sync(0xffffffffu, w, o);
         if (lane >= o) w += t;
       }
-      warp_sums[lane] = w;  // inclusive
+      ws[lane] = w;
     }
     __syncthreads();
-    uint32_t warp_prefix = wid ? warp_sums[wid - 1] : 0u;
-    uint32_t c = carry;
-    if (i < ntiles) row[i] = c + warp_prefix + y - x;
+    const uint32_t c = carry + (wid ? ws[wid - 1] : 0u);
+    if (i < c1) b.cstart[i] = c + y - x;
     __syncthreads();
-    if (threadIdx.x == blockDim.x - 1) carry = c + warp_prefix + y;
+    if (threadIdx.x == blockDim.x - 1) carry = c + y;
     __syncthreads();
+  }
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {
+    uint32_t tot = 0;
+    for (int k = 0; k < SCAN_BLOCKS; ++k) tot += b.csum[k];
+    b.cstart[ncells] = tot;
+    ctrl->n_valid = tot;
   }
 }
 
-__global__ void __launch_bounds__(RS_THREADS) k_radix_scatter(const uint32_t* __restrict__ kin,
-                                                              const uint32_t* __restrict__ vin,
-                                                              uint32_t* __restrict__ kout, uint32_t* __restrict__ vout,
-                                                              uint32_t n, int shift,
-                                                              const uint32_t* __restrict__ offs, uint32_t ntiles,
-                                                              const Ctrl* ctrl) {
+void launch_cell_scan(const Bufs& b, Ctrl* ctrl, cudaStream_t st) {
+  k_cscan_reduce<<<SCAN_BLOCKS, 1024, 0, st>>>(b, ctrl);
+  k_cscan_down<<<SCAN_BLOCKS, 1024, 0, st>>>(b, ctrl);
+}
+
+// Particles into cell order: id, key, ensemble, position.
+__global__ void __launch_bounds__(SLOT_BLOCK) k_scatter(Bufs b, Ctrl* ctrl) {
   if (ctrl->halt) return;
-  __shared__ uint32_t wc[RS_WARPS][256];
-  __shared__ uint32_t toff[256];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-  for (int w = 0; w < RS_WARPS; ++w) wc[w][threadIdx.x] = 0;
-  toff[threadIdx.x] = offs[threadIdx.x * ntiles + blockIdx.x];
-  __syncthreads();
-
-  const uint32_t base = blockIdx.x * RS_TILE + warp * (32 * RS_ITEMS);
-  uint32_t kk[RS_ITEMS], vv[RS_ITEMS], rk[RS_ITEMS];
-  const uint32_t lt = lanemask_lt();
-#pragma unroll
-  for (int k = 0; k < RS_ITEMS; ++k) {
-    uint32_t idx = base + k * 32 + lane;
-    bool valid = idx < n;
-    kk[k] = valid ? kin[idx] : 0u;
-    vv[k] = valid ? vin[idx] : 0u;
-    uint32_t d = valid ? ((kk[k] >> shift) & 255u) : 256u;
-    uint32_t peers = __match_any_sync(0xffffffffu, d);
-    uint32_t prior = __popc(peers & lt);
-    uint32_t cnt = valid ? wc[warp][d] : 0u;
-    rk[k] = cnt + prior;
-    __syncwarp();
-    if (valid && prior == 0) wc[warp][d] = cnt + __popc(peers);
-    __syncwarp();
-  }
-  __syncthreads();
-  {
-    uint32_t run = 0;
-#pragma unroll
-    for (int w = 0; w < RS_WARPS; ++w) {
-      uint32_t c = wc[w][threadIdx.x];
-      wc[w][threadIdx.x] = run;
-      run += c;
-    }
-  }
-  __syncthreads();
-#pragma unroll
-  for (int k = 0; k < RS_ITEMS; ++k) {
-    uint32_t idx = base + k * 32 + lane;
-    if (idx < n) {
-      uint32_t d = (kk[k] >> shift) & 255u;
-      uint32_t dst = toff[d] + wc[warp][d] + rk[k];
-      kout[dst] = kk[k];
-      vout[dst] = vv[k];
-    }
-  }
+  const uint32_t p = blockIdx.x * SLOT_BLOCK + threadIdx.x;
+  if (p >= b.nslots) return;
+  const uint32_t key = b.key[p];
+  if (key == NONE) return;
+  const uint32_t s = b.cstart[key] + b.rank[p];
+  b.sid[s] = p;
+  b.skey[s] = key;
+  b.sens[s] = b.block_ens[blockIdx.x];
+  b.spos[s] = make_float2(b.plon[p], b.plat[p]);
 }
 
-void launch_radix_hist(const uint32_t* key, uint32_t n, int shift, SortScratch& s, uint32_t* digit_total, Ctrl* ctrl,
-                       cudaStream_t st) {
-  uint32_t ntiles = (uint32_t)sort_tiles(n);
-  k_radix_hist<<<ntiles, RS_THREADS, 0, st>>>(key, n, shift, s.counts, digit_total, ntiles, ctrl);
-}
-
-void launch_radix_scan(uint32_t n, SortScratch& s, const uint32_t* digit_total, Ctrl* ctrl, cudaStream_t st) {
-  k_radix_scan<<<256, 1024, 0, st>>>(s.counts, digit_total, (uint32_t)sort_tiles(n), ctrl);
-}
-
-void launch_radix_scatter(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout, uint32_t n,
-                          int shift, SortScratch& s, Ctrl* ctrl, cudaStream_t st) {
-  uint32_t ntiles = (uint32_t)sort_tiles(n);
-  k_radix_scatter<<<ntiles, RS_THREADS, 0, st>>>(kin, vin, kout, vout, n, shift, s.counts, ntiles, ctrl);
-}
-
-// Cell starts + gather of positions into cell order + count of valid (binned) particles.
-__global__ void k_cells(const uint32_t* __restrict__ key, const uint32_t* __restrict__ id,
-                        const float* __restrict__ plon, const float* __restrict__ plat, float2* __restrict__ spos,
-                        uint32_t* __restrict__ cell_start, Ctrl* ctrl, uint32_t n, uint32_t invalid) {
-  if (ctrl->halt) return;
-  uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= n) return;
-  uint32_t k = key[s];
-  uint32_t prev = s ? key[s - 1] : NONE;
-  if (k != invalid) {
-    if (k != prev) cell_start[k] = s;
-    const uint32_t p = id[s];
-    spos[s] = make_float2(plon[p], plat[p]);
-    if (s == n - 1) ctrl->n_valid = n;
-  } else if (prev != invalid) {
-    ctrl->n_valid = s;
-  }
-}
-
-void launch_cells(const uint32_t* key, const uint32_t* id, const float* plon, const float* plat, float2* spos,
-                  uint32_t* cell_start, Ctrl* ctrl, uint32_t n, uint32_t invalid_key, cudaStream_t st) {
-  if (n == 0) return;
-  k_cells<<<(n + 255) / 256, 256, 0, st>>>(key, id, plon, plat, spos, cell_start, ctrl, n, invalid_key);
+void launch_scatter(const Bufs& b, Ctrl* ctrl, cudaStream_t st) {
+  if (b.nslots == 0) return;
+  k_scatter<<<(b.nslots + SLOT_BLOCK - 1) / SLOT_BLOCK, SLOT_BLOCK, 0, st>>>(b, ctrl);
 }
 
 }  // namespace lm

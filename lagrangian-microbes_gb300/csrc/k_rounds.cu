@@ -7,12 +7,12 @@
 // pRS / pSP / pPR of that matchup, and the loser takes the winner's species. Updates cascade to
 // later pairs of the same step. The set order is an artifact of hashing, not a semantic.
 //
-// Here the order is fixed as descending pair priority (a Philox function of (seed, step, i, j)),
-// which the CPU oracle replays with a restatement of the reference's pair function. Pairs that
-// share no microbe commute, so any order that keeps the priority order at every microbe gives the
-// same species: a pair may be applied as soon as it is the highest-priority unprocessed pair of
-// both its microbes. r is drawn from the same Philox block (53-bit uniform), and r < p is
-// evaluated exactly as the integer test u53 < ceil(p * 2^53).
+// Here the order is fixed as descending pair priority (k_pairs.cu), which the CPU oracle replays
+// with a restatement of the reference's pair function. Pairs that share no microbe commute, so
+// any schedule that keeps the priority order at every microbe gives the same species: a pair may
+// be applied as soon as it is the highest-priority unprocessed pair of both its microbes.
+// r is drawn from a Philox block keyed by (ensemble seed, step, i, j) (53-bit uniform), and
+// r < p is evaluated exactly as the integer test u53 < ceil(p * 2^53).
 //
 // All pairs are applied by one persistent cooperative launch without grid barriers. Each vertex v
 // publishes want[v], the partner of its highest-priority unprocessed pair (NONE when it has none).
@@ -55,25 +55,32 @@ __device__ __forceinline__ bool beats(int x, int y) {
   return (x == 1 && y == 3) || (x == 2 && y == 1) || (x == 3 && y == 2);
 }
 
+// Partner of vertex s at list position h (NONE past the end).
+__device__ __forceinline__ uint32_t next_partner(const Bufs& b, uint32_t s, uint32_t h) {
+  const uint32_t d = b.deg[s];
+  if (h >= d) return NONE;
+  return d <= SLAB ? b.slab[(size_t)s * SLAB + h] : b.ovf[(size_t)b.off[s] + h];
+}
+
 // Apply pair (s, u), s < u in cell order, both heads pointing at it; returns its level.
-__device__ __forceinline__ uint32_t apply_pair(const RoundBufs& b, const RpsParams& rp, uint32_t step, uint32_t s,
-                                               uint32_t u, Ctrl* ctrl) {
-  const uint32_t ia = b.id[s], ib = b.id[u];
-  const uint32_t i = min(ia, ib), j = max(ia, ib);
-  const int si = __ldcg(b.species + i), sj = __ldcg(b.species + j);
+__device__ __forceinline__ uint32_t apply_pair(const Bufs& b, uint32_t step, uint32_t s, uint32_t u, Ctrl* ctrl) {
+  const EnsInfo& info = b.ens[b.sens[s]];
+  const uint32_t pa = b.sid[s], pb = b.sid[u];
+  const uint32_t pi = min(pa, pb), pj = max(pa, pb);  // slots; local ids are slot - base
+  const int si = __ldcg(b.species + pi), sj = __ldcg(b.species + pj);
   if (si != sj) {
     unsigned long long t = 0;
     bool valid = true;
-    if ((si == 1 && sj == 3) || (si == 3 && sj == 1)) t = rp.t_rs;
-    else if ((si == 2 && sj == 1) || (si == 1 && sj == 2)) t = rp.t_pr;
-    else if ((si == 3 && sj == 2) || (si == 2 && sj == 3)) t = rp.t_sp;
+    if ((si == 1 && sj == 3) || (si == 3 && sj == 1)) t = info.t_rs;
+    else if ((si == 2 && sj == 1) || (si == 1 && sj == 2)) t = info.t_pr;
+    else if ((si == 3 && sj == 2) || (si == 2 && sj == 3)) t = info.t_sp;
     else valid = false;  // species outside {1,2,3}: the reference's table has no case -> no change
     if (valid) {
-      const PairDraw d = pair_draw(i, j, step, rp.seed_lo, rp.seed_hi);
+      const PairDraw d = pair_draw(pi - info.base, pj - info.base, step, info.seed_lo, info.seed_hi);
       const bool fwd_wins = d.u53 < t;
-      const bool i_wins = (beats(si, sj) == fwd_wins);  // particle i is the cyclic winner xor it lost the draw
-      if (i_wins) __stcg(b.species + j, (int8_t)si);
-      else __stcg(b.species + i, (int8_t)sj);
+      const bool i_wins = (beats(si, sj) == fwd_wins);  // i is the cyclic winner and won, or lost and won anyway
+      if (i_wins) __stcg(b.species + pj, (int8_t)si);
+      else __stcg(b.species + pi, (int8_t)sj);
     }
   }
   const uint32_t level = max(__ldcg(b.level + s), __ldcg(b.level + u)) + 1u;
@@ -82,8 +89,8 @@ __device__ __forceinline__ uint32_t apply_pair(const RoundBufs& b, const RpsPara
   if (b.plog) {
     const uint32_t k = atomicAdd(&ctrl->plog_n, 1u);
     if (k < b.plog_cap) {
-      b.plog[3 * k + 0] = i;
-      b.plog[3 * k + 1] = j;
+      b.plog[3 * k + 0] = pi;
+      b.plog[3 * k + 1] = pj;
       b.plog[3 * k + 2] = level - 1u;
     }
   }
@@ -91,24 +98,20 @@ __device__ __forceinline__ uint32_t apply_pair(const RoundBufs& b, const RpsPara
   const uint32_t hu = __ldcg(b.head + u) + 1u, hs = __ldcg(b.head + s) + 1u;
   __stcg(b.head + u, hu);
   __stcg(b.head + s, hs);
-  const uint32_t nu = hu < b.deg[u] ? b.adj[b.off[u] + hu] : NONE;
-  const uint32_t ns = hs < b.deg[s] ? b.adj[b.off[s] + hs] : NONE;
+  const uint32_t nu = next_partner(b, u, hu);
+  const uint32_t ns = next_partner(b, s, hs);
   __threadfence();
-  st_release(b.want[0] + u, nu);
-  st_release(b.want[0] + s, ns);
+  st_release(b.want + u, nu);
+  st_release(b.want + s, ns);
   return level;
 }
 
-__global__ void __launch_bounds__(RD_THREADS) k_rounds(RoundBufs b, RpsParams rp, StepArgs a, Ctrl* ctrl,
-                                                       uint32_t round_cap) {
-  (void)round_cap;
+__global__ void __launch_bounds__(RD_THREADS) k_rounds(Bufs b, StepArgs a, Ctrl* ctrl) {
   if (((volatile uint32_t*)&ctrl->halt)[0]) return;
   const uint32_t step = a.use_ctrl_step ? ctrl->step : a.step0;
-  const uint32_t cnt = ((volatile uint32_t*)ctrl->act_n)[0];
+  const uint32_t cnt = ((volatile uint32_t*)&ctrl->act_n)[0];
   const uint32_t stride = gridDim.x * blockDim.x;
   const uint32_t first = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t* L = b.act[0];
-  uint32_t* want = b.want[0];
   uint32_t max_level = 0;
   const unsigned long long t0 = globaltimer();
   bool pending = first < cnt;
@@ -116,11 +119,11 @@ __global__ void __launch_bounds__(RD_THREADS) k_rounds(RoundBufs b, RpsParams rp
   while (pending) {
     pending = false;
     for (uint32_t x = first; x < cnt; x += stride) {
-      const uint32_t s = L[x];
-      const uint32_t u = ld_acquire(want + s);
+      const uint32_t s = b.act[x];
+      const uint32_t u = ld_acquire(b.want + s);
       if (u == NONE) continue;
       pending = true;
-      if (s < u && ld_acquire(want + u) == s) max_level = max(max_level, apply_pair(b, rp, step, s, u, ctrl));
+      if (s < u && ld_acquire(b.want + u) == s) max_level = max(max_level, apply_pair(b, step, s, u, ctrl));
     }
     if (pending && ((++polls & 63u) == 0u) && globaltimer() - t0 > ROUNDS_TIMEOUT_NS) {
       atomicOr(&ctrl->err, (uint32_t)ERRB_TIMEOUT);
@@ -144,9 +147,7 @@ int rounds_grid(int device, int* block) {
   return sms * per_sm;
 }
 
-cudaError_t launch_rounds(const RoundBufs& b, const RpsParams& rp, const StepArgs& a, Ctrl* ctrl, uint32_t n,
-                          int grid, int block, uint32_t round_cap, cudaStream_t st) {
-  (void)n;
+cudaError_t launch_rounds(const Bufs& b, const StepArgs& a, Ctrl* ctrl, int grid, int block, cudaStream_t st) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)grid);
   cfg.blockDim = dim3((unsigned)block);
@@ -157,56 +158,36 @@ cudaError_t launch_rounds(const RoundBufs& b, const RpsParams& rp, const StepArg
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, k_rounds, b, rp, a, ctrl, round_cap);
+  return cudaLaunchKernelEx(&cfg, k_rounds, b, a, ctrl);
 }
 
-// Per-step species census (counts of species 0..3 after the step; 0 collects anything else).
-__global__ void k_census(const int8_t* __restrict__ species, Ctrl* ctrl, uint32_t n) {
+// Species counts after the step, per ensemble and in total ([0] collects values outside 1..3).
+__global__ void __launch_bounds__(SLOT_BLOCK) k_census(Bufs b, Ctrl* ctrl) {
   if (ctrl->halt) return;
   __shared__ uint32_t h[4];
   if (threadIdx.x < 4) h[threadIdx.x] = 0;
   __syncthreads();
-  uint32_t c[4] = {0, 0, 0, 0};
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    int s = species[i];
-    c[(s >= 1 && s <= 3) ? s : 0]++;
+  const uint32_t p = blockIdx.x * SLOT_BLOCK + threadIdx.x;
+  int s = -1;
+  if (p < b.nslots && b.status[p] != STATUS_PAD) {
+    s = b.species[p];
+    s = (s >= 1 && s <= 3) ? s : 0;
   }
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    uint32_t v = c[k];
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    uint32_t v = __popc(__ballot_sync(0xffffffffu, s == k));
     if ((threadIdx.x & 31) == 0 && v) atomicAdd(&h[k], v);
   }
   __syncthreads();
-  if (threadIdx.x < 4 && h[threadIdx.x]) atomicAdd(&ctrl->census[threadIdx.x], h[threadIdx.x]);
+  if (threadIdx.x < 4 && h[threadIdx.x]) {
+    atomicAdd(&b.census[4 * b.block_ens[blockIdx.x] + threadIdx.x], h[threadIdx.x]);
+    atomicAdd(&ctrl->census[threadIdx.x], h[threadIdx.x]);
+  }
 }
 
-void launch_census(const int8_t* species, Ctrl* ctrl, uint32_t n, cudaStream_t st) {
-  int grid = (int)((n + 255) / 256);
-  if (grid > 152 * 8) grid = 152 * 8;
-  if (grid < 1) grid = 1;
-  k_census<<<grid, 256, 0, st>>>(species, ctrl, n);
+void launch_census(const Bufs& b, Ctrl* ctrl, cudaStream_t st) {
+  if (b.nslots == 0) return;
+  k_census<<<(b.nslots + SLOT_BLOCK - 1) / SLOT_BLOCK, SLOT_BLOCK, 0, st>>>(b, ctrl);
 }
-
-// Per-step bookkeeping: reset per-step counters (start), advance the device step counter (end).
-__global__ void k_step_begin(Ctrl* ctrl) {
-  if (ctrl->halt) return;
-  ctrl->act_n[0] = ctrl->act_n[1] = ctrl->act_n[2] = 0;
-  ctrl->plog_n = 0;
-  ctrl->rounds = 0;
-  ctrl->applied = 0;
-  ctrl->n_valid = 0;
-  ctrl->n_dir = 0;
-  ctrl->bar_count = 0;
-  ctrl->census[0] = ctrl->census[1] = ctrl->census[2] = ctrl->census[3] = 0;
-}
-
-__global__ void k_step_end(Ctrl* ctrl) {
-  if (ctrl->halt) return;
-  ctrl->step += 1;
-}
-
-void launch_step_begin(Ctrl* ctrl, cudaStream_t st) { k_step_begin<<<1, 1, 0, st>>>(ctrl); }
-void launch_step_end(Ctrl* ctrl, cudaStream_t st) { k_step_end<<<1, 1, 0, st>>>(ctrl); }
 
 }  // namespace lm

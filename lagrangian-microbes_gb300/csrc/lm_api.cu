@@ -1,6 +1,6 @@
-// C-ABI of liblmgb300 (declared in include/lm_api.h): context, device buffers, step orchestration,
-// neighbour-list regrowth and CUDA-graph capture. Kernels live in k_advect.cu (K1), k_bin.cu (K2),
-// k_pairs.cu (K3) and k_rounds.cu (K4/K5).
+// C-ABI of liblmgb300 (declared in include/lm_api.h): context, ensembles, device buffers, step
+// orchestration, capacity regrowth and CUDA-graph capture. Kernels live in k_advect.cu (K1),
+// k_bin.cu (K2), k_pairs.cu (K3) and k_rounds.cu (K4/K5).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -17,15 +17,20 @@
 using namespace lm;
 
 namespace {
-
-constexpr uint32_t ROUND_CAP = 1u << 22;
-constexpr uint64_t MAX_CELLS = 1ull << 26;
 thread_local std::string g_create_error;
 
+enum ProfId {
+  P_ADVECT, P_BBOX, P_GRID, P_KEYS, P_CELL_SCAN, P_SCATTER, P_SWEEP, P_SWEEP_LONG, P_ROUNDS, P_CENSUS,
+  P_BOOKKEEPING, P_COUNT
+};
+const char* const kProfNames[P_COUNT] = {"k_advect",     "k_bbox",       "k_grid",   "k_keys",
+                                         "k_cscan",      "k_scatter",    "k_sweep",  "k_sweep_long",
+                                         "k_rounds",     "k_census",     "k_step_begin_end"};
 }  // namespace
 
 struct lm_ctx {
   int device = 0;
+  int sms = 0;
   cudaStream_t own = nullptr;
   cudaStream_t st = nullptr;
   std::string err;
@@ -33,55 +38,67 @@ struct lm_ctx {
   // field
   float2* uv = nullptr;
   size_t uv_n = 0;
+  size_t field_elems = 0;  // nt * ny * nx
+  int n_fields = 0;
   FieldView fv{};
   bool has_field = false;
-  double lon0 = 0, lat0 = 0, dlon = 0, dlat = 0, lon1 = 0, lat1 = 0, t_first = 0, t_last = 0;
-  double org_lon = 0, org_lat = 0;
+  double lon0 = 0, lat0 = 0, lon1 = 0, lat1 = 0, t_first = 0, t_last = 0, org_lon = 0, org_lat = 0;
 
-  // particles and per-particle scratch
-  uint32_t n = 0;       // particles in the state
-  uint32_t ncap = 0;    // capacity of per-particle buffers
+  // ensembles and slots
+  uint32_t n_ens = 0;
+  std::vector<uint32_t> counts, base;
+  uint32_t nslots = 0, ntotal = 0;
+  std::vector<int32_t> hmap;  // slot -> caller index (or -1)
+  std::vector<EnsInfo> ens_h;
+  EnsInfo* ens_d = nullptr;
+  uint32_t* block_ens = nullptr;
+  int32_t* map_d = nullptr;
   bool has_particles = false;  // positions + species (fused path)
   bool has_species = false;    // species only (two-phase interaction path)
+
+  // per-slot buffers
+  uint32_t slot_cap = 0;
   float *xo = nullptr, *yo = nullptr, *plon = nullptr, *plat = nullptr;
   int8_t* species = nullptr;
   uint8_t* status = nullptr;
-  uint32_t *key[2] = {nullptr, nullptr}, *id[2] = {nullptr, nullptr};
+  uint32_t *key = nullptr, *rank = nullptr, *sid = nullptr, *skey = nullptr, *sens = nullptr, *deg = nullptr;
+  uint32_t *slab = nullptr, *off = nullptr, *longv = nullptr, *want = nullptr, *head = nullptr, *level = nullptr;
+  uint32_t* act = nullptr;
   float2* spos = nullptr;
-  uint32_t *deg = nullptr, *off = nullptr, *block_sum = nullptr, *head = nullptr, *level = nullptr;
-  uint32_t *want[2] = {nullptr, nullptr}, *act[2] = {nullptr, nullptr};
-  uint32_t* sort_counts = nullptr;
-  uint32_t* digit_total = nullptr;
-  size_t sort_counts_cap = 0;
-
-  // neighbour lists
-  uint32_t* adj = nullptr;
-  unsigned long long* prio = nullptr;
-  size_t adj_cap = 0;
-  int64_t regrows = 0;
+  float *rlon = nullptr, *rlat = nullptr;  // caller-order staging (E > 1)
+  int8_t* rsp = nullptr;
+  uint32_t ens_cap = 0;
+  EnsGrid* grids = nullptr;
+  uint32_t* ebox = nullptr;
+  uint32_t* census = nullptr;
 
   // cells
-  uint32_t* cell_start = nullptr;
-  size_t cells_cap = 0;
-  CellGrid grid{};
-  int key_bits = 1;
+  uint32_t cells_cap = 0;
+  uint32_t *ccount = nullptr, *cstart = nullptr, *csum = nullptr;
+
+  // long lists
+  size_t ovf_cap = 0;
+  uint32_t* ovf = nullptr;
+  unsigned long long* oprio = nullptr;
+  int64_t regrows = 0;
 
   // interaction parameters
   bool has_params = false;
   PairParams pp{};
-  RpsParams rp{};
+  double cell_factor = 1.004;
+  std::vector<double> p_rs, p_pr, p_sp;
+  std::vector<uint64_t> seeds;
 
   // control block
   Ctrl* ctrl = nullptr;
-  Ctrl* hctrl = nullptr;  // pinned mirror
-  uint32_t* hstage = nullptr;  // pinned staging (census)
+  Ctrl* hctrl = nullptr;
+  uint32_t* hstage = nullptr;
   size_t hstage_n = 0;
 
   // pair log
   uint32_t* plog = nullptr;
   uint32_t plog_cap = 0;
 
-  // rounds launch shape
   int rgrid = 0, rblock = 0;
 
   // graph
@@ -91,9 +108,9 @@ struct lm_ctx {
   int64_t g_step0 = 0;
   int g_spg = 0;
   uint32_t g_flags = 0;
-  int64_t next_step = 0;  // host mirror of the device step counter
+  int64_t next_step = 0;
 
-  // per-kernel CUDA-event timing of plain launches (lm_profile_enable)
+  // per-kernel CUDA-event timing of plain launches
   bool prof_on = false;
   bool capturing = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -102,19 +119,29 @@ struct lm_ctx {
     cudaEvent_t a, b;
   };
   std::vector<Pend> pend;
-  double prof_ms[32] = {};
-  int64_t prof_n[32] = {};
+  double prof_ms[P_COUNT] = {};
+  int64_t prof_n[P_COUNT] = {};
 };
 
 namespace {
 
-enum ProfId {
-  P_ADVECT, P_KEYS, P_HIST, P_SCAN, P_SCATTER, P_CELLS, P_SWEEP_COUNT, P_SCAN_BLOCKS, P_SWEEP_FILL, P_ROUNDS,
-  P_CENSUS, P_BOOKKEEPING, P_COUNT
-};
-const char* const kProfNames[P_COUNT] = {"k_advect",      "k_keys_from_pos", "k_radix_hist", "k_radix_scan",
-                                         "k_radix_scatter", "k_cells",       "k_sweep_count", "k_scan_blocks",
-                                         "k_sweep_fill",  "k_rounds",        "k_census",      "k_step_begin_end"};
+int fail(lm_ctx* c, int code, const char* fmt, ...) __attribute__((format(printf, 3, 4)));
+int fail(lm_ctx* c, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (c) c->err = buf;
+  else g_create_error = buf;
+  return code;
+}
+
+#define CK(call)                                                                                 \
+  do {                                                                                           \
+    cudaError_t e_ = (call);                                                                     \
+    if (e_ != cudaSuccess) return fail(c, LM_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
 
 cudaEvent_t prof_begin(lm_ctx* c) {
   if (!c->prof_on || c->capturing) return nullptr;
@@ -145,7 +172,6 @@ void prof_end(lm_ctx* c, int id, cudaEvent_t a) {
   c->pend.push_back({id, a, b});
 }
 
-// Accumulate the timings of completed launches (call after a stream synchronisation).
 void prof_collect(lm_ctx* c) {
   for (auto& p : c->pend) {
     float ms = 0.f;
@@ -161,29 +187,11 @@ void prof_collect(lm_ctx* c) {
   c->pend.clear();
 }
 
-#define PROF(c, id, stmt)              \
-  do {                                 \
-    cudaEvent_t pa_ = prof_begin(c);   \
-    stmt;                              \
-    prof_end(c, id, pa_);              \
-  } while (0)
-
-int fail(lm_ctx* c, int code, const char* fmt, ...) __attribute__((format(printf, 3, 4)));
-int fail(lm_ctx* c, int code, const char* fmt, ...) {
-  char buf[512];
-  va_list ap;
-  va_start(ap, fmt);
-  vsnprintf(buf, sizeof(buf), fmt, ap);
-  va_end(ap);
-  if (c) c->err = buf;
-  else g_create_error = buf;
-  return code;
-}
-
-#define CK(call)                                                                                 \
-  do {                                                                                           \
-    cudaError_t e_ = (call);                                                                     \
-    if (e_ != cudaSuccess) return fail(c, LM_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+#define PROF(c, id, stmt)            \
+  do {                               \
+    cudaEvent_t pa_ = prof_begin(c); \
+    stmt;                            \
+    prof_end(c, id, pa_);            \
   } while (0)
 
 template <class T>
@@ -202,79 +210,168 @@ int dalloc(lm_ctx* c, T** p, size_t count) {
   return LM_OK;
 }
 
-int ensure_particles(lm_ctx* c, uint32_t n) {
-  if (n <= c->ncap && c->xo) return LM_OK;
-  uint32_t cap = std::max<uint32_t>(n, 1024);
-  int r = LM_OK;
-  if ((r = dalloc(c, &c->xo, cap)) || (r = dalloc(c, &c->yo, cap)) || (r = dalloc(c, &c->plon, cap)) ||
-      (r = dalloc(c, &c->plat, cap)) || (r = dalloc(c, &c->species, cap)) || (r = dalloc(c, &c->status, cap)) ||
-      (r = dalloc(c, &c->key[0], cap)) || (r = dalloc(c, &c->key[1], cap)) || (r = dalloc(c, &c->id[0], cap)) ||
-      (r = dalloc(c, &c->id[1], cap)) || (r = dalloc(c, &c->spos, cap)) || (r = dalloc(c, &c->deg, cap)) ||
-      (r = dalloc(c, &c->off, cap)) || (r = dalloc(c, &c->head, cap)) || (r = dalloc(c, &c->level, cap)) || (r = dalloc(c, &c->want[0], cap)) ||
-      (r = dalloc(c, &c->want[1], cap)) || (r = dalloc(c, &c->act[0], cap)) || (r = dalloc(c, &c->act[1], cap)) ||
-      (r = dalloc(c, &c->block_sum, (size_t)sweep_blocks(cap) + 1)) ||
-      (r = dalloc(c, &c->sort_counts, (size_t)256 * sort_tiles(cap))) ||
-      (r = dalloc(c, &c->digit_total, (size_t)256 * 4)))
-    return r;
-  c->ncap = cap;
+uint32_t next_pow2(uint64_t x) {
+  uint64_t p = 1;
+  while (p < x) p <<= 1;
+  return (uint32_t)std::min<uint64_t>(p, 1ull << 31);
+}
+
+int set_cells_capacity(lm_ctx* c, uint32_t cap) {
+  int r;
+  if ((r = dalloc(c, &c->ccount, (size_t)cap + 1)) || (r = dalloc(c, &c->cstart, (size_t)cap + 1))) return r;
+  CK(cudaMemsetAsync(c->ccount, 0, ((size_t)cap + 1) * sizeof(uint32_t), c->st));
+  CK(cudaStreamSynchronize(c->st));
+  c->cells_cap = cap;
   return LM_OK;
 }
 
-int set_adj_capacity(lm_ctx* c, size_t cap) {
+int set_ovf_capacity(lm_ctx* c, size_t cap) {
   int r;
-  if (cap > 0xfffffff0ull) cap = 0xfffffff0ull;
-  if ((r = dalloc(c, &c->adj, cap)) || (r = dalloc(c, &c->prio, cap))) return r;
-  c->adj_cap = cap;
+  cap = std::min<size_t>(cap, 0xfffffff0ull);
+  if ((r = dalloc(c, &c->ovf, cap)) || (r = dalloc(c, &c->oprio, cap))) return r;
+  c->ovf_cap = cap;
   unsigned long long cv = cap;
-  CK(cudaMemcpyAsync(&c->ctrl->cap, &cv, sizeof(cv), cudaMemcpyHostToDevice, c->st));
-  // the pair log holds at most one entry per unordered pair
-  c->plog_cap = (uint32_t)std::min<size_t>(cap / 2 + 1, 0x7fffffffu);
-  if ((r = dalloc(c, &c->plog, (size_t)3 * c->plog_cap))) return r;
+  CK(cudaMemcpyAsync(&c->ctrl->ovf_cap, &cv, sizeof(cv), cudaMemcpyHostToDevice, c->st));
   CK(cudaStreamSynchronize(c->st));
   return LM_OK;
 }
 
-int ensure_adj(lm_ctx* c, uint32_t n) {
-  size_t want = std::max<size_t>((size_t)16 * n, (size_t)1 << 16);
-  if (c->adj && c->adj_cap >= want) return LM_OK;
-  return set_adj_capacity(c, want);
-}
-
-// Cell grid over [x0, x1] x [y0, y1] with one margin cell per side; cell size >= radius.
-int set_grid(lm_ctx* c, double x0, double y0, double x1, double y1) {
-  double r = c->pp.r;
-  double cs = r * 1.004;
-  double w = std::max(x1 - x0, 0.0), h = std::max(y1 - y0, 0.0);
-  if (!(cs > 0) || !std::isfinite(cs)) cs = std::max(std::max(w, h), 1e-6);
-  double ncx = std::floor(w / cs) + 3, ncy = std::floor(h / cs) + 3;
-  if (ncx * ncy > (double)MAX_CELLS - 1) {
-    cs = std::sqrt(std::max(w * h, 1e-300) / (double)(MAX_CELLS / 2));
-    cs = std::max(cs, r * 1.004);
-    ncx = std::floor(w / cs) + 3;
-    ncy = std::floor(h / cs) + 3;
+// Per-slot and per-ensemble buffers for `slots` slots and `n_ens` ensembles.
+int ensure_slots(lm_ctx* c, uint32_t slots, uint32_t n_ens) {
+  int r;
+  if (slots > c->slot_cap || !c->xo) {
+    const uint32_t cap = std::max<uint32_t>(slots, 1024);
+    const size_t nblk = (cap + SLOT_BLOCK - 1) / SLOT_BLOCK + 1;
+    if ((r = dalloc(c, &c->xo, cap)) || (r = dalloc(c, &c->yo, cap)) || (r = dalloc(c, &c->plon, cap)) ||
+        (r = dalloc(c, &c->plat, cap)) || (r = dalloc(c, &c->species, cap)) || (r = dalloc(c, &c->status, cap)) ||
+        (r = dalloc(c, &c->key, cap)) || (r = dalloc(c, &c->rank, cap)) || (r = dalloc(c, &c->sid, cap)) ||
+        (r = dalloc(c, &c->skey, cap)) || (r = dalloc(c, &c->sens, cap)) || (r = dalloc(c, &c->deg, cap)) ||
+        (r = dalloc(c, &c->slab, (size_t)cap * SLAB)) || (r = dalloc(c, &c->off, cap)) ||
+        (r = dalloc(c, &c->longv, cap)) || (r = dalloc(c, &c->want, cap)) || (r = dalloc(c, &c->head, cap)) ||
+        (r = dalloc(c, &c->level, cap)) || (r = dalloc(c, &c->act, cap)) || (r = dalloc(c, &c->spos, cap)) ||
+        (r = dalloc(c, &c->rlon, cap)) || (r = dalloc(c, &c->rlat, cap)) || (r = dalloc(c, &c->rsp, cap)) ||
+        (r = dalloc(c, &c->map_d, cap)) || (r = dalloc(c, &c->block_ens, nblk)))
+      return r;
+    c->slot_cap = cap;
+    if ((r = set_cells_capacity(c, std::max<uint32_t>(1u << 20, next_pow2((uint64_t)4 * cap)))) ||
+        (r = set_ovf_capacity(c, std::max<size_t>((size_t)2 * cap, (size_t)1 << 16))))
+      return r;
+    if (!c->csum && (r = dalloc(c, &c->csum, SCAN_BLOCKS))) return r;
   }
-  CellGrid g;
-  g.x0 = (float)(x0 - cs);
-  g.y0 = (float)(y0 - cs);
-  g.inv_c = (float)(1.0 / cs);
-  g.ncx = (int)ncx;
-  g.ncy = (int)ncy;
-  g.ncells = (uint32_t)(ncx * ncy);
-  int bits = 1;
-  while (bits < 32 && ((uint64_t)1 << bits) <= (uint64_t)g.ncells) ++bits;  // ncells itself = invalid key
-  if (g.ncells + 1 > c->cells_cap) {
-    int rr = dalloc(c, &c->cell_start, (size_t)g.ncells + 1);
-    if (rr) return rr;
-    c->cells_cap = (size_t)g.ncells + 1;
+  if (n_ens > c->ens_cap || !c->ens_d) {
+    const uint32_t cap = std::max<uint32_t>(n_ens, 1);
+    if ((r = dalloc(c, &c->ens_d, cap)) || (r = dalloc(c, &c->grids, cap)) || (r = dalloc(c, &c->ebox, (size_t)4 * cap)) ||
+        (r = dalloc(c, &c->census, (size_t)4 * cap)))
+      return r;
+    CK(cudaMemsetAsync(c->census, 0, sizeof(uint32_t) * 4 * cap, c->st));
+    c->ens_cap = cap;
   }
-  c->grid = g;
-  c->key_bits = bits;
+  if ((uint64_t)16 * n_ens > c->cells_cap && (r = set_cells_capacity(c, next_pow2((uint64_t)16 * n_ens)))) return r;
   return LM_OK;
 }
 
-int set_field_grid(lm_ctx* c) {
-  // Cells are addressed in absolute degrees over the field domain.
-  return set_grid(c, c->lon0, c->lat0, c->lon1, c->lat1);
+// Ensemble layout: counts -> slot bases (padded to SLOT_BLOCK when n_ens > 1), maps, block table.
+int layout(lm_ctx* c, uint32_t n_ens, const int64_t* counts) {
+  std::vector<uint32_t> cnt(n_ens), base(n_ens);
+  uint64_t slot = 0, total = 0;
+  for (uint32_t e = 0; e < n_ens; ++e) {
+    if (counts[e] < 0) return fail(c, LM_ERR_ARG, "negative count for ensemble %u", e);
+    cnt[e] = (uint32_t)counts[e];
+    if (n_ens > 1) slot = (slot + SLOT_BLOCK - 1) / SLOT_BLOCK * SLOT_BLOCK;
+    base[e] = (uint32_t)slot;
+    slot += cnt[e];
+    total += cnt[e];
+    if (slot > 0x7fffff00ull) return fail(c, LM_ERR_ARG, "too many particles");
+  }
+  int r;
+  if ((r = ensure_slots(c, (uint32_t)slot, n_ens))) return r;
+  c->n_ens = n_ens;
+  c->counts = cnt;
+  c->base = base;
+  c->nslots = (uint32_t)slot;
+  c->ntotal = (uint32_t)total;
+  c->hmap.assign(slot, -1);
+  std::vector<uint32_t> bens((slot + SLOT_BLOCK - 1) / SLOT_BLOCK + 1, 0);
+  uint64_t idx = 0;
+  for (uint32_t e = 0; e < n_ens; ++e) {
+    for (uint32_t k = 0; k < cnt[e]; ++k) c->hmap[base[e] + k] = (int32_t)(idx + k);
+    idx += cnt[e];
+    if (cnt[e]) {
+      const uint32_t b0 = base[e] / SLOT_BLOCK, b1 = (base[e] + cnt[e] - 1) / SLOT_BLOCK;
+      for (uint32_t b = b0; b <= b1; ++b) bens[b] = e;
+    }
+  }
+  if (slot) CK(cudaMemcpyAsync(c->map_d, c->hmap.data(), slot * sizeof(int32_t), cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(c->block_ens, bens.data(), bens.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return LM_OK;
+}
+
+unsigned long long prob_threshold(double p) {
+  if (!(p > 0)) return 0ull;  // also NaN: r < NaN is false
+  if (p >= 1.0) return 1ull << 53;
+  return (unsigned long long)std::ceil(std::ldexp(p, 53));
+}
+
+// Per-ensemble constants to the device (parameters default to the last lm_set_interaction).
+int upload_ens(lm_ctx* c) {
+  c->ens_h.assign(c->n_ens, EnsInfo{});
+  for (uint32_t e = 0; e < c->n_ens; ++e) {
+    EnsInfo& x = c->ens_h[e];
+    const size_t k = e < c->p_rs.size() ? e : 0;
+    x.t_rs = c->p_rs.empty() ? 0 : prob_threshold(c->p_rs[k]);
+    x.t_pr = c->p_pr.empty() ? 0 : prob_threshold(c->p_pr[k]);
+    x.t_sp = c->p_sp.empty() ? 0 : prob_threshold(c->p_sp[k]);
+    const uint64_t seed = c->seeds.empty() ? 0 : c->seeds[e < c->seeds.size() ? e : 0];
+    x.seed_lo = (uint32_t)seed;
+    x.seed_hi = (uint32_t)(seed >> 32);
+    x.base = c->base[e];
+    x.n = c->counts[e];
+    x.field_off = (c->n_fields > 1) ? (unsigned long long)e * c->field_elems : 0ull;
+  }
+  if (c->n_ens) CK(cudaMemcpyAsync(c->ens_d, c->ens_h.data(), c->n_ens * sizeof(EnsInfo), cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return LM_OK;
+}
+
+Bufs bufs(const lm_ctx* c, bool log) {
+  Bufs b;
+  b.ens = c->ens_d;
+  b.block_ens = c->block_ens;
+  b.n_ens = c->n_ens;
+  b.nslots = c->nslots;
+  b.cells_cap = c->cells_cap;
+  b.xo = c->xo;
+  b.yo = c->yo;
+  b.species = c->species;
+  b.status = c->status;
+  b.plon = c->plon;
+  b.plat = c->plat;
+  b.ebox = c->ebox;
+  b.grids = c->grids;
+  b.key = c->key;
+  b.rank = c->rank;
+  b.ccount = c->ccount;
+  b.cstart = c->cstart;
+  b.csum = c->csum;
+  b.sid = c->sid;
+  b.skey = c->skey;
+  b.sens = c->sens;
+  b.spos = c->spos;
+  b.deg = c->deg;
+  b.slab = c->slab;
+  b.off = c->off;
+  b.ovf = c->ovf;
+  b.oprio = c->oprio;
+  b.longv = c->longv;
+  b.want = c->want;
+  b.head = c->head;
+  b.level = c->level;
+  b.act = c->act;
+  b.census = c->census;
+  b.plog = log ? c->plog : nullptr;
+  b.plog_cap = c->plog_cap;
+  return b;
 }
 
 int read_ctrl(lm_ctx* c) {
@@ -292,26 +389,24 @@ int write_ctrl_step(lm_ctx* c, int64_t step) {
   return LM_OK;
 }
 
-int clear_halt(lm_ctx* c) {
-  // halt = 0 and the overflow bit cleared; other sticky bits are kept
-  c->hctrl->halt = 0;
-  c->hctrl->err &= ~(uint32_t)ERRB_OVERFLOW;
-  CK(cudaMemcpyAsync(&c->ctrl->halt, &c->hctrl->halt, sizeof(uint32_t), cudaMemcpyHostToDevice, c->st));
+int write_err(lm_ctx* c, uint32_t err, uint32_t halt) {
+  c->hctrl->err = err;
+  c->hctrl->halt = halt;
   CK(cudaMemcpyAsync(&c->ctrl->err, &c->hctrl->err, sizeof(uint32_t), cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(&c->ctrl->halt, &c->hctrl->halt, sizeof(uint32_t), cudaMemcpyHostToDevice, c->st));
   CK(cudaStreamSynchronize(c->st));
   return LM_OK;
 }
 
+int clear_err_bits(lm_ctx* c, uint32_t mask) { return write_err(c, c->hctrl->err & ~mask, c->hctrl->halt); }
+
 // Map and clear the sticky device error bits.
 int consume_errors(lm_ctx* c) {
-  uint32_t e = c->hctrl->err;
+  const uint32_t e = c->hctrl->err;
   if (!e) return LM_OK;
-  uint32_t zero = 0;
-  CK(cudaMemcpyAsync(&c->ctrl->err, &zero, sizeof(zero), cudaMemcpyHostToDevice, c->st));
-  CK(cudaStreamSynchronize(c->st));
-  c->hctrl->err = 0;
-  if (e & ERRB_TIMEOUT) return fail(c, LM_ERR_TIMEOUT, "a device barrier wait timed out");
-  if (e & ERRB_ROUNDCAP) return fail(c, LM_ERR_ROUND_CAP, "interaction round cap (%u) reached", ROUND_CAP);
+  int r;
+  if ((r = write_err(c, 0u, c->hctrl->halt))) return r;
+  if (e & ERRB_TIMEOUT) return fail(c, LM_ERR_TIMEOUT, "a bounded device wait timed out");
   if (e & ERRB_TIME) return fail(c, LM_ERR_TIME, "a stage time fell outside the field's time axis");
   if (e & ERRB_NAN) return fail(c, LM_ERR_NAN, "non-finite particle positions (%u flagged in total)", c->hctrl->oob);
   if (e & ERRB_OOB)
@@ -320,83 +415,63 @@ int consume_errors(lm_ctx* c) {
   return LM_OK;
 }
 
-StepArgs step_args(const lm_ctx* c, double t, double dt, int64_t step, double kh, bool graph) {
+// Regrow after a halted step: long-list area and/or cell capacity, then clear the halt.
+int regrow(lm_ctx* c) {
+  int r;
+  const Ctrl& h = *c->hctrl;
+  if (h.ovf_used > c->ovf_cap) {
+    size_t need = (size_t)h.ovf_used;
+    if ((r = set_ovf_capacity(c, std::max(need + need / 4 + 4096, c->ovf_cap * 2)))) return r;
+  }
+  if (h.ncells >= c->cells_cap && h.halt) {
+    if ((r = set_cells_capacity(c, (uint32_t)std::min<uint64_t>((uint64_t)c->cells_cap * 2, 1ull << 31)))) return r;
+  }
+  c->regrows++;
+  return write_err(c, h.err & ~(uint32_t)ERRB_OVERFLOW, 0u);
+}
+
+StepArgs step_args(double t, double dt, int64_t step, double kh, bool graph) {
   StepArgs a;
   a.t_start = t;
   a.dt = dt;
   a.step0 = (uint32_t)step;
   a.use_ctrl_step = graph ? 1 : 0;
   a.kick = kh > 0 ? (float)std::sqrt(6.0 * std::fabs(dt) * kh) : 0.f;
-  a.seed_lo = c->rp.seed_lo;
-  a.seed_hi = c->rp.seed_hi;
   return a;
 }
 
-cudaError_t enqueue_interaction(lm_ctx* c, const StepArgs& a, uint32_t flags, uint32_t n) {
+// bin -> pair -> (interact). `positions_only`: the boxes come from plon/plat (no advection ran).
+cudaError_t enqueue_interaction(lm_ctx* c, const StepArgs& a, uint32_t flags, bool positions_only, bool use_status) {
   cudaStream_t st = c->st;
-  SortScratch ss{c->sort_counts, c->digit_total, (uint32_t)sort_tiles(c->ncap)};
-  const int passes = radix_passes(c->key_bits);
-  cudaError_t e = cudaMemsetAsync(c->digit_total, 0, sizeof(uint32_t) * 256 * passes, st);
-  if (e != cudaSuccess) return e;
-  int r = 0;
-  for (int p = 0; p < passes; ++p) {
-    uint32_t* dt = c->digit_total + 256 * p;
-    PROF(c, P_HIST, launch_radix_hist(c->key[r], n, 8 * p, ss, dt, c->ctrl, st));
-    PROF(c, P_SCAN, launch_radix_scan(n, ss, dt, c->ctrl, st));
-    PROF(c, P_SCATTER, launch_radix_scatter(c->key[r], c->id[r], c->key[r ^ 1], c->id[r ^ 1], n, 8 * p, ss, c->ctrl, st));
-    r ^= 1;
-  }
-  PROF(c, P_CELLS,
-       launch_cells(c->key[r], c->id[r], c->plon, c->plat, c->spos, c->cell_start, c->ctrl, n, c->grid.ncells, st));
-  PROF(c, P_SWEEP_COUNT,
-       launch_sweep_count(c->grid, c->pp, c->key[r], c->spos, c->cell_start, c->ctrl, c->deg, c->block_sum, n, st));
-  PROF(c, P_SCAN_BLOCKS, launch_scan_blocks(c->block_sum, (uint32_t)sweep_blocks(n), c->ctrl, st));
-  PROF(c, P_SWEEP_FILL,
-       launch_sweep_fill(c->grid, c->pp, c->rp, a, c->key[r], c->id[r], c->spos, c->cell_start, c->block_sum, c->ctrl,
-                         c->deg, c->off, c->adj, c->prio, c->want[0], c->head, c->act[0], c->level, n, st));
+  const Bufs b = bufs(c, (flags & LM_STEP_LOG_PAIRS) != 0);
+  if (positions_only) PROF(c, P_BBOX, launch_bbox(b, c->ctrl, use_status, st));
+  PROF(c, P_GRID, launch_grid(b, c->pp, c->ctrl, st));
+  PROF(c, P_KEYS, launch_keys(b, c->ctrl, use_status, st));
+  PROF(c, P_CELL_SCAN, launch_cell_scan(b, c->ctrl, st));
+  PROF(c, P_SCATTER, launch_scatter(b, c->ctrl, st));
+  PROF(c, P_SWEEP, launch_sweep(b, c->pp, a, c->ctrl, st));
+  PROF(c, P_SWEEP_LONG, launch_sweep_long(b, c->pp, a, c->ctrl, c->sms, st));
   if (flags & LM_STEP_INTERACT) {
-    RoundBufs rb;
-    rb.off = c->off;
-    rb.deg = c->deg;
-    rb.adj = c->adj;
-    rb.id = c->id[r];
-    rb.species = c->species;
-    rb.want[0] = c->want[0];
-    rb.want[1] = c->want[1];
-    rb.head = c->head;
-    rb.act[0] = c->act[0];
-    rb.act[1] = c->act[1];
-    rb.level = c->level;
-    rb.plog = (flags & LM_STEP_LOG_PAIRS) ? c->plog : nullptr;
-    rb.plog_cap = c->plog_cap;
     cudaEvent_t pa = prof_begin(c);
-    e = launch_rounds(rb, c->rp, a, c->ctrl, n, c->rgrid, c->rblock, ROUND_CAP, st);
+    cudaError_t e = launch_rounds(b, a, c->ctrl, c->rgrid, c->rblock, st);
     prof_end(c, P_ROUNDS, pa);
     if (e != cudaSuccess) return e;
   }
   return cudaGetLastError();
 }
 
-// One fused step; `advect` false re-runs only the interaction part (overflow recovery).
+// One fused step; `advect` false re-runs only the interaction part of an advected step.
 cudaError_t enqueue_step(lm_ctx* c, const StepArgs& a, uint32_t flags, bool advect) {
-  PROF(c, P_BOOKKEEPING, launch_step_begin(c->ctrl, c->st));
-  if (advect && (flags & LM_STEP_ADVECT))
-    PROF(c, P_ADVECT, launch_advect(c->fv, c->grid, a, c->ctrl, c->xo, c->yo, c->status, c->plon, c->plat,
-                                    c->key[0], c->id[0], c->n, c->st));
+  const Bufs b = bufs(c, false);
+  PROF(c, P_BOOKKEEPING, launch_step_begin(b, c->ctrl, c->st));
+  if (advect) PROF(c, P_ADVECT, launch_advect(c->fv, a, b, c->ctrl, c->st));
   if (flags & LM_STEP_INTERACT) {
-    cudaError_t e = enqueue_interaction(c, a, flags, c->n);
+    cudaError_t e = enqueue_interaction(c, a, flags, !advect, true);
     if (e != cudaSuccess) return e;
   }
-  if (flags & LM_STEP_CENSUS) PROF(c, P_CENSUS, launch_census(c->species, c->ctrl, c->n, c->st));
-  PROF(c, P_BOOKKEEPING, launch_step_end(c->ctrl, c->st));
+  if (flags & LM_STEP_CENSUS) PROF(c, P_CENSUS, launch_census(b, c->ctrl, c->st));
+  PROF(c, P_BOOKKEEPING, launch_step_end(c->ctrl, (flags & LM_STEP_INTERACT) != 0, c->st));
   return cudaGetLastError();
-}
-
-int clear_err_bits(lm_ctx* c, uint32_t mask) {
-  c->hctrl->err &= ~mask;
-  CK(cudaMemcpyAsync(&c->ctrl->err, &c->hctrl->err, sizeof(uint32_t), cudaMemcpyHostToDevice, c->st));
-  CK(cudaStreamSynchronize(c->st));
-  return LM_OK;
 }
 
 int ensure_hstage(lm_ctx* c, size_t n) {
@@ -408,25 +483,16 @@ int ensure_hstage(lm_ctx* c, size_t n) {
   return LM_OK;
 }
 
-int regrow(lm_ctx* c) {
-  size_t need = (size_t)c->hctrl->n_dir;
-  size_t cap = std::max(need + need / 4 + 1024, c->adj_cap * 2);
-  int r = set_adj_capacity(c, cap);
-  if (r) return r;
-  c->regrows++;
-  return clear_halt(c);
-}
-
-int check_time(lm_ctx* c, double t, double dt, int n_steps) {
-  double lo = std::min(t, t + dt * n_steps), hi = std::max(t, t + dt * n_steps);
-  double tol = 1e-9 * std::fabs(c->fv.dT);
+int check_time(lm_ctx* c, double t, double dt, int64_t n_steps) {
+  const double lo = std::min(t, t + dt * n_steps), hi = std::max(t, t + dt * n_steps);
+  const double tol = 1e-9 * std::fabs(c->fv.dT);
   if (lo < c->t_first - tol || hi > c->t_last + tol)
     return fail(c, LM_ERR_TIME, "time window [%.9g, %.9g] s is outside the field's [%.9g, %.9g] s", lo, hi,
                 c->t_first, c->t_last);
   return LM_OK;
 }
 
-int set_pair_params(lm_ctx* c, double r, int norm) {
+void set_pair_params(lm_ctx* c, double r, int norm) {
   PairParams& pp = c->pp;
   pp.r = r;
   pp.r2 = r * r;
@@ -441,23 +507,126 @@ int set_pair_params(lm_ctx* c, double r, int norm) {
     pp.r2f_lo = pp.rf_lo = -1.f;
     pp.r2f_hi = pp.rf_hi = INFINITY;
   }
-  return LM_OK;
-}
-
-unsigned long long prob_threshold(double p) {
-  if (!(p > 0)) return 0ull;  // also NaN: r < NaN is false
-  if (p >= 1.0) return 1ull << 53;
-  return (unsigned long long)std::ceil(std::ldexp(p, 53));
+  pp.inv2r = r > 0 ? (float)(0.5 / r) : 0.f;
+  pp.cell_factor = (float)c->cell_factor;
 }
 
 bool uniform_axis(const double* a, int n, double* d) {
   if (n < 2) return false;
-  double step = (a[n - 1] - a[0]) / (n - 1);
+  const double step = (a[n - 1] - a[0]) / (n - 1);
   if (!(step > 0) || !std::isfinite(step)) return false;
   for (int k = 0; k < n; ++k)
     if (std::fabs(a[k] - (a[0] + step * k)) > 1e-6 * step) return false;
   *d = step;
   return true;
+}
+
+// Copies of one step's records into caller-order host arrays.
+int record_step(lm_ctx* c, int64_t k, float* rec_lon, float* rec_lat, int8_t* rec_species) {
+  const uint32_t n = c->ntotal;
+  if (!n) return LM_OK;
+  const bool direct = (c->n_ens == 1);
+  if (rec_lon) {
+    if (!direct) launch_unpad(c->plon, c->rlon, c->map_d, c->nslots, c->st);
+    CK(cudaMemcpyAsync(rec_lon + k * n, direct ? c->plon : c->rlon, n * sizeof(float), cudaMemcpyDeviceToHost, c->st));
+  }
+  if (rec_lat) {
+    if (!direct) launch_unpad(c->plat, c->rlat, c->map_d, c->nslots, c->st);
+    CK(cudaMemcpyAsync(rec_lat + k * n, direct ? c->plat : c->rlat, n * sizeof(float), cudaMemcpyDeviceToHost, c->st));
+  }
+  if (rec_species) {
+    if (!direct) launch_unpad8(c->species, c->rsp, c->map_d, c->nslots, c->st);
+    CK(cudaMemcpyAsync(rec_species + k * n, direct ? c->species : c->rsp, n, cudaMemcpyDeviceToHost, c->st));
+  }
+  return LM_OK;
+}
+
+int run_steps(lm_ctx* c, double t, double dt, int64_t n_steps, int64_t step0, uint32_t flags, double kh,
+              float* rec_lon, float* rec_lat, int8_t* rec_species, int64_t* rec_census) {
+  int r;
+  if ((r = write_ctrl_step(c, step0))) return r;
+  if (rec_census && (r = ensure_hstage(c, (size_t)4 * n_steps))) return r;
+  int64_t s = 0;
+  bool redo = false;
+  while (s < n_steps) {
+    for (int64_t k = s; k < n_steps; ++k) {
+      const StepArgs a = step_args(t + dt * k, dt, step0 + k, kh, false);
+      CK(enqueue_step(c, a, flags, !(redo && k == s)));
+      if ((r = record_step(c, k, rec_lon, rec_lat, rec_species))) return r;
+      if (rec_census)
+        CK(cudaMemcpyAsync(c->hstage + 4 * k, c->ctrl->census, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->st));
+    }
+    CK(cudaGetLastError());
+    if ((r = read_ctrl(c))) return r;
+    if (c->hctrl->halt) {
+      const int64_t k = (int64_t)c->hctrl->halt_step - step0;
+      if ((r = regrow(c))) return r;
+      if ((r = write_ctrl_step(c, step0 + k))) return r;
+      s = k;
+      redo = true;  // the halted step was advected already
+      continue;
+    }
+    break;
+  }
+  c->next_step = step0 + n_steps;
+  if (rec_census)
+    for (int64_t k = 0; k < 4 * n_steps; ++k) rec_census[k] = c->hstage[k];
+  return consume_errors(c);
+}
+
+// Positions supplied by the caller (float32, E = 1): the two-phase interaction path.
+int stage_positions(lm_ctx* c, int64_t n, const float* lon, const float* lat) {
+  if (c->n_ens != 1 || c->ntotal != (uint32_t)n) {
+    const int64_t cnt = n;
+    int r = layout(c, 1, &cnt);
+    if (r) return r;
+    if ((r = upload_ens(c))) return r;
+  }
+  if (n) {
+    CK(cudaMemcpyAsync(c->plon, lon, n * sizeof(float), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(c->plat, lat, n * sizeof(float), cudaMemcpyHostToDevice, c->st));
+  }
+  return LM_OK;
+}
+
+int capture(lm_ctx* c) {
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  if (c->graph) cudaGraphDestroy(c->graph);
+  c->gexec = nullptr;
+  c->graph = nullptr;
+  CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
+  c->capturing = true;
+  for (int k = 0; k < c->g_spg; ++k) {
+    const StepArgs a = step_args(c->g_t_start, c->g_dt, c->g_step0, c->g_kh, true);
+    const cudaError_t le = enqueue_step(c, a, c->g_flags, true);
+    if (le != cudaSuccess) {
+      c->capturing = false;
+      cudaGraph_t g = nullptr;
+      cudaStreamEndCapture(c->st, &g);
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();
+      return fail(c, LM_ERR_CUDA, "launch during capture failed: %s", cudaGetErrorString(le));
+    }
+  }
+  cudaGraph_t g = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(c->st, &g);
+  c->capturing = false;
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(c, LM_ERR_CUDA, "stream capture failed: %s", cudaGetErrorString(e));
+  }
+  c->graph = g;
+  CK(cudaGraphInstantiate(&c->gexec, c->graph, 0));
+  return LM_OK;
+}
+
+int check_ready(lm_ctx* c, uint32_t flags) {
+  if (!(flags & LM_STEP_ADVECT)) return fail(c, LM_ERR_ARG, "steps need LM_STEP_ADVECT (use lm_interact)");
+  if (!c->has_field || !c->has_particles) return fail(c, LM_ERR_STATE, "field and particles must be uploaded first");
+  if ((flags & LM_STEP_INTERACT) && !c->has_params) return fail(c, LM_ERR_STATE, "call lm_set_interaction first");
+  if (c->n_fields != 1 && c->n_fields != (int)c->n_ens)
+    return fail(c, LM_ERR_STATE, "%d fields for %u ensembles (need 1 or one per ensemble)", c->n_fields, c->n_ens);
+  return LM_OK;
 }
 
 }  // namespace
@@ -471,8 +640,7 @@ int lm_ctx_create(int device, lm_ctx** out) {
   *out = nullptr;
   int ndev = 0;
   cudaError_t e = cudaGetDeviceCount(&ndev);
-  if (e != cudaSuccess || ndev == 0)
-    return fail(nullptr, LM_ERR_CUDA, "no CUDA device: %s", cudaGetErrorString(e));
+  if (e != cudaSuccess || ndev == 0) return fail(nullptr, LM_ERR_CUDA, "no CUDA device: %s", cudaGetErrorString(e));
   if (device < 0 || device >= ndev) return fail(nullptr, LM_ERR_ARG, "device %d out of range [0, %d)", device, ndev);
   lm_ctx* c = new lm_ctx();
   c->device = device;
@@ -481,28 +649,21 @@ int lm_ctx_create(int device, lm_ctx** out) {
     lm_ctx_destroy(c);
     return code;
   };
-  if ((e = cudaSetDevice(device)) != cudaSuccess) {
-    fail(c, LM_ERR_CUDA, "cudaSetDevice: %s", cudaGetErrorString(e));
-    return bail(LM_ERR_CUDA);
-  }
-  if ((e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking)) != cudaSuccess) {
-    fail(c, LM_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
-    return bail(LM_ERR_CUDA);
-  }
+  if ((e = cudaSetDevice(device)) != cudaSuccess) return bail(fail(c, LM_ERR_CUDA, "cudaSetDevice: %s", cudaGetErrorString(e)));
+  if ((e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking)) != cudaSuccess)
+    return bail(fail(c, LM_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e)));
   c->st = c->own;
+  cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device);
   int r = dalloc(c, &c->ctrl, 1);
   if (r) return bail(r);
-  if ((e = cudaMallocHost((void**)&c->hctrl, sizeof(Ctrl))) != cudaSuccess) {
-    fail(c, LM_ERR_CUDA, "cudaMallocHost: %s", cudaGetErrorString(e));
-    return bail(LM_ERR_CUDA);
-  }
+  if ((e = cudaMallocHost((void**)&c->hctrl, sizeof(Ctrl))) != cudaSuccess)
+    return bail(fail(c, LM_ERR_CUDA, "cudaMallocHost: %s", cudaGetErrorString(e)));
   memset(c->hctrl, 0, sizeof(Ctrl));
   if ((e = cudaMemsetAsync(c->ctrl, 0, sizeof(Ctrl), c->st)) != cudaSuccess ||
-      (e = cudaStreamSynchronize(c->st)) != cudaSuccess) {
-    fail(c, LM_ERR_CUDA, "ctrl init: %s", cudaGetErrorString(e));
-    return bail(LM_ERR_CUDA);
-  }
+      (e = cudaStreamSynchronize(c->st)) != cudaSuccess)
+    return bail(fail(c, LM_ERR_CUDA, "ctrl init: %s", cudaGetErrorString(e)));
   c->rgrid = rounds_grid(device, &c->rblock);
+  set_pair_params(c, 0.0, LM_NORM_L2);
   *out = c;
   return LM_OK;
 }
@@ -513,11 +674,12 @@ int lm_ctx_destroy(lm_ctx* c) {
   if (c->st) cudaStreamSynchronize(c->st);
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
   if (c->graph) cudaGraphDestroy(c->graph);
-  void* bufs[] = {c->uv,          c->xo,      c->yo,      c->plon,   c->plat,      c->species,   c->status,
-                  c->key[0],      c->key[1],  c->id[0],   c->id[1],  c->spos,      c->deg,       c->off,
-                  c->block_sum,   c->head,    c->want[0], c->want[1], c->act[0],   c->act[1],    c->sort_counts, c->level,
-                  c->digit_total, c->adj,     c->prio,    c->cell_start, c->ctrl,  c->plog};
-  for (void* p : bufs)
+  void* bufs_[] = {c->uv,     c->xo,    c->yo,     c->plon,   c->plat,   c->species, c->status, c->key,
+                   c->rank,   c->sid,   c->skey,   c->sens,   c->deg,    c->slab,    c->off,    c->longv,
+                   c->want,   c->head,  c->level,  c->act,    c->spos,   c->rlon,    c->rlat,   c->rsp,
+                   c->map_d,  c->block_ens, c->ens_d, c->grids, c->ebox, c->census,  c->ccount, c->cstart,
+                   c->csum,   c->ovf,   c->oprio,  c->ctrl,   c->plog};
+  for (void* p : bufs_)
     if (p) cudaFree(p);
   if (c->hctrl) cudaFreeHost(c->hctrl);
   if (c->hstage) cudaFreeHost(c->hstage);
@@ -553,40 +715,51 @@ int lm_sync(lm_ctx* c) {
   return consume_errors(c);
 }
 
-int lm_field_upload(lm_ctx* c, const float* u, const float* v, int nt, int ny, int nx, const double* lon,
-                    const double* lat, const double* t_sec) {
+int lm_field_upload_batch(lm_ctx* c, int n_fields, const float* u, const float* v, int nt, int ny, int nx,
+                          const double* lon, const double* lat, const double* t_sec) {
   if (!c || !u || !v || !lon || !lat || !t_sec) return fail(c, LM_ERR_ARG, "NULL argument");
+  if (n_fields < 1) return fail(c, LM_ERR_ARG, "n_fields must be >= 1");
   if (nt < 2 || ny < 2 || nx < 2) return fail(c, LM_ERR_ARG, "field needs nt, ny, nx >= 2 (got %d, %d, %d)", nt, ny, nx);
   double dx, dy, dT;
   if (!uniform_axis(lon, nx, &dx)) return fail(c, LM_ERR_GRID, "longitude axis is not uniform and ascending");
   if (!uniform_axis(lat, ny, &dy)) return fail(c, LM_ERR_GRID, "latitude axis is not uniform and ascending");
   if (!uniform_axis(t_sec, nt, &dT)) return fail(c, LM_ERR_GRID, "time axis is not uniform and ascending");
   CK(cudaSetDevice(c->device));
-  size_t n = (size_t)nt * ny * nx;
+  const size_t per = (size_t)nt * ny * nx;
+  const size_t n = per * (size_t)n_fields;
   int r;
   if (n > c->uv_n || !c->uv) {
     if ((r = dalloc(c, &c->uv, n))) return r;
     c->uv_n = n;
   }
-  // stage u and v through a temporary device buffer, then interleave
+  // stage u and v through a bounded temporary device buffer, one chunk of frames at a time
+  const size_t chunk = std::min<size_t>(n, (size_t)64 << 20);
   float* tmp = nullptr;
-  if ((r = dalloc(c, &tmp, 2 * n))) return r;
-  CK(cudaMemcpyAsync(tmp, u, n * sizeof(float), cudaMemcpyHostToDevice, c->st));
-  CK(cudaMemcpyAsync(tmp + n, v, n * sizeof(float), cudaMemcpyHostToDevice, c->st));
-  launch_interleave(tmp, tmp + n, c->uv, n, c->st);
+  if ((r = dalloc(c, &tmp, 2 * chunk))) return r;
+  for (size_t o = 0; o < n; o += chunk) {
+    const size_t m = std::min(chunk, n - o);
+    CK(cudaMemcpyAsync(tmp, u + o, m * sizeof(float), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(tmp + chunk, v + o, m * sizeof(float), cudaMemcpyHostToDevice, c->st));
+    launch_interleave(tmp, tmp + chunk, c->uv + o, m, c->st);
+  }
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(c->st));
   cudaFree(tmp);
+  c->n_fields = n_fields;
+  c->field_elems = per;
   c->lon0 = lon[0];
   c->lat0 = lat[0];
   c->lon1 = lon[nx - 1];
   c->lat1 = lat[ny - 1];
-  c->dlon = dx;
-  c->dlat = dy;
   c->t_first = t_sec[0];
   c->t_last = t_sec[nt - 1];
-  c->org_lon = (double)(float)lon[0];
-  c->org_lat = (double)(float)lat[0];
+  const double new_org_lon = (double)(float)lon[0], new_org_lat = (double)(float)lat[0];
+  if (c->has_particles && (new_org_lon != c->org_lon || new_org_lat != c->org_lat)) {
+    c->has_particles = false;  // offsets are relative to the field origin: positions must be re-uploaded
+    c->has_species = false;
+  }
+  c->org_lon = new_org_lon;
+  c->org_lat = new_org_lat;
   FieldView& f = c->fv;
   f.uv = c->uv;
   f.nx = nx;
@@ -603,53 +776,73 @@ int lm_field_upload(lm_ctx* c, const float* u, const float* v, int nt, int ny, i
   f.t0 = t_sec[0];
   f.dT = dT;
   c->has_field = true;
-  if (c->has_particles) {  // offsets are relative to the field origin: positions must be re-uploaded
-    c->has_particles = false;
-    c->has_species = false;
-  }
+  if (c->n_ens) return upload_ens(c);
   return LM_OK;
 }
 
-int lm_particles_upload(lm_ctx* c, int64_t n, const double* lon, const double* lat, const int8_t* species) {
-  if (!c || (n > 0 && (!lon || !lat))) return fail(c, LM_ERR_ARG, "NULL argument");
-  if (n < 0 || n > 0x7fffffff) return fail(c, LM_ERR_ARG, "particle count %lld out of range", (long long)n);
+int lm_field_upload(lm_ctx* c, const float* u, const float* v, int nt, int ny, int nx, const double* lon,
+                    const double* lat, const double* t_sec) {
+  return lm_field_upload_batch(c, 1, u, v, nt, ny, nx, lon, lat, t_sec);
+}
+
+int lm_ensembles_upload(lm_ctx* c, int n_ens, const int64_t* counts, const double* lon, const double* lat,
+                        const int8_t* species) {
+  if (!c || n_ens < 1 || !counts) return fail(c, LM_ERR_ARG, "need n_ens >= 1 and counts");
   if (!c->has_field) return fail(c, LM_ERR_STATE, "upload the velocity field before the particles");
+  int64_t total = 0;
+  for (int e = 0; e < n_ens; ++e) total += counts[e];
+  if (total > 0 && (!lon || !lat)) return fail(c, LM_ERR_ARG, "NULL positions");
   CK(cudaSetDevice(c->device));
   int r;
-  if ((r = ensure_particles(c, (uint32_t)n)) || (r = ensure_adj(c, (uint32_t)n))) return r;
-  std::vector<float> xo(n), yo(n);
-  for (int64_t k = 0; k < n; ++k) {
-    xo[k] = (float)(lon[k] - c->org_lon);
-    yo[k] = (float)(lat[k] - c->org_lat);
+  if ((r = layout(c, (uint32_t)n_ens, counts))) return r;
+  const uint32_t S = c->nslots;
+  std::vector<float> xo(S, 0.f), yo(S, 0.f);
+  std::vector<int8_t> sp(S, 0);
+  std::vector<uint8_t> st(S, STATUS_PAD);
+  for (uint32_t k = 0; k < S; ++k) {
+    const int32_t q = c->hmap[k];
+    if (q < 0) continue;
+    xo[k] = (float)(lon[q] - c->org_lon);
+    yo[k] = (float)(lat[q] - c->org_lat);
+    sp[k] = species ? species[q] : 0;
+    st[k] = STATUS_OK;
   }
-  if (n > 0) {
-    CK(cudaMemcpyAsync(c->xo, xo.data(), n * sizeof(float), cudaMemcpyHostToDevice, c->st));
-    CK(cudaMemcpyAsync(c->yo, yo.data(), n * sizeof(float), cudaMemcpyHostToDevice, c->st));
-    if (species) CK(cudaMemcpyAsync(c->species, species, n, cudaMemcpyHostToDevice, c->st));
-    else CK(cudaMemsetAsync(c->species, 0, n, c->st));
-    CK(cudaMemsetAsync(c->status, 0, n, c->st));
+  if (S) {
+    CK(cudaMemcpyAsync(c->xo, xo.data(), S * sizeof(float), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(c->yo, yo.data(), S * sizeof(float), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(c->species, sp.data(), S, cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(c->status, st.data(), S, cudaMemcpyHostToDevice, c->st));
   }
-  uint32_t zero = 0;
+  const uint32_t zero = 0;
   CK(cudaMemcpyAsync(&c->ctrl->oob, &zero, sizeof(zero), cudaMemcpyHostToDevice, c->st));
   CK(cudaStreamSynchronize(c->st));
-  c->n = (uint32_t)n;
+  if ((r = upload_ens(c))) return r;
   c->has_particles = true;
   c->has_species = true;
   return LM_OK;
 }
 
+int lm_particles_upload(lm_ctx* c, int64_t n, const double* lon, const double* lat, const int8_t* species) {
+  if (!c) return LM_ERR_ARG;
+  if (n < 0 || n > 0x7fffff00) return fail(c, LM_ERR_ARG, "particle count %lld out of range", (long long)n);
+  return lm_ensembles_upload(c, 1, &n, lon, lat, species);
+}
+
 int lm_species_upload(lm_ctx* c, int64_t n, const int8_t* species) {
   if (!c || (n > 0 && !species)) return fail(c, LM_ERR_ARG, "NULL argument");
-  if (n < 0 || n > 0x7fffffff) return fail(c, LM_ERR_ARG, "species count out of range");
-  if (c->has_particles && n != (int64_t)c->n)
-    return fail(c, LM_ERR_ARG, "n = %lld but the context holds %u particles", (long long)n, c->n);
+  if (n < 0 || n > 0x7fffff00) return fail(c, LM_ERR_ARG, "species count out of range");
   CK(cudaSetDevice(c->device));
   int r;
-  if (!c->has_particles) {
-    if ((r = ensure_particles(c, (uint32_t)n)) || (r = ensure_adj(c, (uint32_t)n))) return r;
-    c->n = (uint32_t)n;
+  if (c->has_particles) {
+    if (n != (int64_t)c->ntotal)
+      return fail(c, LM_ERR_ARG, "n = %lld but the context holds %u particles", (long long)n, c->ntotal);
+  } else if (c->n_ens != 1 || c->ntotal != (uint32_t)n) {
+    if ((r = layout(c, 1, &n)) || (r = upload_ens(c))) return r;
   }
-  if (n) CK(cudaMemcpyAsync(c->species, species, n, cudaMemcpyHostToDevice, c->st));
+  std::vector<int8_t> sp(c->nslots, 0);
+  for (uint32_t k = 0; k < c->nslots; ++k)
+    if (c->hmap[k] >= 0) sp[k] = species[c->hmap[k]];
+  if (c->nslots) CK(cudaMemcpyAsync(c->species, sp.data(), c->nslots, cudaMemcpyHostToDevice, c->st));
   CK(cudaStreamSynchronize(c->st));
   c->has_species = true;
   return LM_OK;
@@ -659,18 +852,26 @@ int lm_particles_download(lm_ctx* c, float* lon, float* lat, int8_t* species, ui
   if (!c) return LM_ERR_ARG;
   if (!c->has_particles && (lon || lat || status || !c->has_species)) return fail(c, LM_ERR_STATE, "no particles");
   CK(cudaSetDevice(c->device));
-  uint32_t n = c->n;
-  std::vector<float> xo(lon ? n : 0), yo(lat ? n : 0);
-  if (n) {
-    if (lon) CK(cudaMemcpyAsync(xo.data(), c->xo, n * sizeof(float), cudaMemcpyDeviceToHost, c->st));
-    if (lat) CK(cudaMemcpyAsync(yo.data(), c->yo, n * sizeof(float), cudaMemcpyDeviceToHost, c->st));
-    if (species) CK(cudaMemcpyAsync(species, c->species, n, cudaMemcpyDeviceToHost, c->st));
-    if (status) CK(cudaMemcpyAsync(status, c->status, n, cudaMemcpyDeviceToHost, c->st));
+  const uint32_t S = c->nslots;
+  std::vector<float> xo(lon ? S : 0), yo(lat ? S : 0);
+  std::vector<int8_t> sp(species ? S : 0);
+  std::vector<uint8_t> st(status ? S : 0);
+  if (S) {
+    if (lon) CK(cudaMemcpyAsync(xo.data(), c->xo, S * sizeof(float), cudaMemcpyDeviceToHost, c->st));
+    if (lat) CK(cudaMemcpyAsync(yo.data(), c->yo, S * sizeof(float), cudaMemcpyDeviceToHost, c->st));
+    if (species) CK(cudaMemcpyAsync(sp.data(), c->species, S, cudaMemcpyDeviceToHost, c->st));
+    if (status) CK(cudaMemcpyAsync(st.data(), c->status, S, cudaMemcpyDeviceToHost, c->st));
   }
   CK(cudaStreamSynchronize(c->st));
   const float ox = (float)c->org_lon, oy = (float)c->org_lat;
-  for (uint32_t k = 0; lon && k < n; ++k) lon[k] = ox + xo[k];  // same single rounding as the device
-  for (uint32_t k = 0; lat && k < n; ++k) lat[k] = oy + yo[k];
+  for (uint32_t k = 0; k < S; ++k) {
+    const int32_t q = c->hmap[k];
+    if (q < 0) continue;
+    if (lon) lon[q] = ox + xo[k];  // same single rounding as the device
+    if (lat) lat[q] = oy + yo[k];
+    if (species) species[q] = sp[k];
+    if (status) status[q] = st[k];
+  }
   return LM_OK;
 }
 
@@ -679,118 +880,71 @@ int lm_set_interaction(lm_ctx* c, double radius, int norm, double p_rs, double p
   if (!(radius >= 0) || !std::isfinite(radius)) return fail(c, LM_ERR_ARG, "radius must be finite and >= 0");
   if (norm != LM_NORM_INF && norm != LM_NORM_L1 && norm != LM_NORM_L2)
     return fail(c, LM_ERR_ARG, "norm must be 1, 2 or infinity (code 0); got %d", norm);
+  CK(cudaSetDevice(c->device));
   set_pair_params(c, radius, norm);
-  c->rp.t_rs = prob_threshold(p_rs);
-  c->rp.t_pr = prob_threshold(p_pr);
-  c->rp.t_sp = prob_threshold(p_sp);
-  c->rp.seed_lo = (uint32_t)seed;
-  c->rp.seed_hi = (uint32_t)(seed >> 32);
+  c->p_rs.assign(1, p_rs);
+  c->p_pr.assign(1, p_pr);
+  c->p_sp.assign(1, p_sp);
+  c->seeds.assign(1, seed);
   c->has_params = true;
+  if (c->n_ens) return upload_ens(c);
   return LM_OK;
 }
 
-static int run_steps(lm_ctx* c, double t, double dt, int n_steps, int64_t step0, uint32_t flags, double kh,
-                     float* rec_lon, float* rec_lat, int8_t* rec_species, int64_t* rec_census) {
-  const uint32_t n = c->n;
-  int r;
-  if ((r = write_ctrl_step(c, step0))) return r;
-  if (rec_census && (r = ensure_hstage(c, (size_t)4 * n_steps))) return r;
-  int64_t s = 0;
-  bool redo_interaction_only = false;
-  while (s < n_steps) {
-    for (int64_t k = s; k < n_steps; ++k) {
-      StepArgs a = step_args(c, t + dt * k, dt, step0 + k, kh, false);
-      CK(enqueue_step(c, a, flags, !(redo_interaction_only && k == s)));
-      if (n) {
-        if (rec_lon) CK(cudaMemcpyAsync(rec_lon + k * n, c->plon, n * sizeof(float), cudaMemcpyDeviceToHost, c->st));
-        if (rec_lat) CK(cudaMemcpyAsync(rec_lat + k * n, c->plat, n * sizeof(float), cudaMemcpyDeviceToHost, c->st));
-        if (rec_species) CK(cudaMemcpyAsync(rec_species + k * n, c->species, n, cudaMemcpyDeviceToHost, c->st));
-      }
-      if (rec_census)
-        CK(cudaMemcpyAsync(c->hstage + 4 * k, c->ctrl->census, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->st));
-    }
-    CK(cudaGetLastError());
-    if ((r = read_ctrl(c))) return r;
-    if (c->hctrl->halt) {
-      int64_t k = (int64_t)c->hctrl->halt_step - step0;
-      if ((r = regrow(c))) return r;
-      if ((r = write_ctrl_step(c, step0 + k))) return r;
-      s = k;
-      redo_interaction_only = true;  // the halted step was advected already
-      continue;
-    }
-    break;
-  }
-  c->next_step = step0 + n_steps;
-  if (rec_census)
-    for (int64_t k = 0; k < 4 * (int64_t)n_steps; ++k) rec_census[k] = c->hstage[k];
-  return consume_errors(c);
+int lm_set_ensemble_params(lm_ctx* c, int n_ens, const double* p_rs, const double* p_pr, const double* p_sp,
+                           const uint64_t* seeds) {
+  if (!c || !p_rs || !p_pr || !p_sp || !seeds) return fail(c, LM_ERR_ARG, "NULL argument");
+  if (!c->has_params) return fail(c, LM_ERR_STATE, "call lm_set_interaction first (radius and norm)");
+  if (n_ens != (int)c->n_ens) return fail(c, LM_ERR_ARG, "%d parameter sets for %u ensembles", n_ens, c->n_ens);
+  CK(cudaSetDevice(c->device));
+  c->p_rs.assign(p_rs, p_rs + n_ens);
+  c->p_pr.assign(p_pr, p_pr + n_ens);
+  c->p_sp.assign(p_sp, p_sp + n_ens);
+  c->seeds.assign(seeds, seeds + n_ens);
+  return upload_ens(c);
+}
+
+int lm_set_cell_factor(lm_ctx* c, double factor) {
+  if (!c) return LM_ERR_ARG;
+  if (!(factor >= 1.004) || !(factor <= 64.0)) return fail(c, LM_ERR_ARG, "cell factor must be in [1.004, 64]");
+  c->cell_factor = factor;
+  c->pp.cell_factor = (float)factor;
+  return LM_OK;
 }
 
 int lm_step(lm_ctx* c, double t_sec, double dt_sec, int n_steps, int64_t step0, uint32_t flags, double kh_deg2_s,
             float* rec_lon, float* rec_lat, int8_t* rec_species, int64_t* rec_census) {
   if (!c) return LM_ERR_ARG;
   if (n_steps < 0) return fail(c, LM_ERR_ARG, "n_steps < 0");
-  if (!(flags & LM_STEP_ADVECT)) return fail(c, LM_ERR_ARG, "lm_step needs LM_STEP_ADVECT (use lm_interact)");
-  if (!c->has_field || !c->has_particles) return fail(c, LM_ERR_STATE, "field and particles must be uploaded first");
-  if ((flags & LM_STEP_INTERACT) && !c->has_params) return fail(c, LM_ERR_STATE, "call lm_set_interaction first");
+  int r;
+  if ((r = check_ready(c, flags))) return r;
   if (!(dt_sec != 0) || !std::isfinite(dt_sec)) return fail(c, LM_ERR_ARG, "dt must be finite and nonzero");
   if (!(kh_deg2_s >= 0)) return fail(c, LM_ERR_ARG, "Kh must be >= 0");
   CK(cudaSetDevice(c->device));
-  int r;
   if ((r = check_time(c, t_sec, dt_sec, n_steps))) return r;
-  if (!c->has_params) set_pair_params(c, 0.0, LM_NORM_L2);
-  if ((r = set_field_grid(c))) return r;
   if (n_steps == 0) return LM_OK;
+  if ((flags & LM_STEP_LOG_PAIRS) && c->plog_cap < (uint64_t)8 * c->nslots + 1024) {
+    c->plog_cap = (uint32_t)std::min<uint64_t>((uint64_t)8 * c->nslots + 1024, 0x7fffffffull);
+    if ((r = dalloc(c, &c->plog, (size_t)3 * c->plog_cap))) return r;
+  }
   return run_steps(c, t_sec, dt_sec, n_steps, step0, flags, kh_deg2_s, rec_lon, rec_lat, rec_species, rec_census);
-}
-
-// Bounding box of finite positions (host loop; the positions come from the host anyway).
-static void bbox(const float* lon, const float* lat, int64_t n, double* x0, double* y0, double* x1, double* y1) {
-  float a = INFINITY, b = INFINITY, cmax = -INFINITY, d = -INFINITY;
-  for (int64_t k = 0; k < n; ++k) {
-    float x = lon[k], y = lat[k];
-    if (!std::isfinite(x) || !std::isfinite(y)) continue;
-    a = std::min(a, x);
-    cmax = std::max(cmax, x);
-    b = std::min(b, y);
-    d = std::max(d, y);
-  }
-  if (!(a <= cmax)) a = cmax = b = d = 0.f;
-  *x0 = a;
-  *y0 = b;
-  *x1 = cmax;
-  *y1 = d;
-}
-
-static int stage_positions(lm_ctx* c, int64_t n, const float* lon, const float* lat) {
-  int r;
-  if ((r = ensure_particles(c, (uint32_t)n)) || (r = ensure_adj(c, (uint32_t)n))) return r;
-  double x0, y0, x1, y1;
-  bbox(lon, lat, n, &x0, &y0, &x1, &y1);
-  if ((r = set_grid(c, x0, y0, x1, y1))) return r;
-  if (n) {
-    CK(cudaMemcpyAsync(c->plon, lon, n * sizeof(float), cudaMemcpyHostToDevice, c->st));
-    CK(cudaMemcpyAsync(c->plat, lat, n * sizeof(float), cudaMemcpyHostToDevice, c->st));
-  }
-  return LM_OK;
 }
 
 int lm_query_pairs(lm_ctx* c, int64_t n, const float* lon, const float* lat, int32_t* pi, int32_t* pj, int64_t cap,
                    int64_t* n_pairs) {
   if (!c || !n_pairs || (n > 0 && (!lon || !lat))) return fail(c, LM_ERR_ARG, "NULL argument");
-  if (n < 0 || n > 0x7fffffff) return fail(c, LM_ERR_ARG, "particle count out of range");
+  if (n < 0 || n > 0x7fffff00) return fail(c, LM_ERR_ARG, "particle count out of range");
   if (!c->has_params) return fail(c, LM_ERR_STATE, "call lm_set_interaction first");
   CK(cudaSetDevice(c->device));
   *n_pairs = 0;
   if (n == 0) return LM_OK;
   int r;
   if ((r = stage_positions(c, n, lon, lat))) return r;
+  c->has_particles = false;  // positions now hold query points, not an advected state
+  const StepArgs a = step_args(0.0, 1.0, 0, 0.0, false);
   for (;;) {
-    StepArgs a = step_args(c, 0.0, 1.0, 0, 0.0, false);
-    launch_step_begin(c->ctrl, c->st);
-    PROF(c, P_KEYS, launch_keys_from_pos(c->grid, c->ctrl, c->plon, c->plat, c->key[0], c->id[0], (uint32_t)n, c->st));
-    CK(enqueue_interaction(c, a, 0u, (uint32_t)n));
+    PROF(c, P_BOOKKEEPING, launch_step_begin(bufs(c, false), c->ctrl, c->st));
+    CK(enqueue_interaction(c, a, 0u, true, false));
     if ((r = read_ctrl(c))) return r;
     if (c->hctrl->halt) {
       if ((r = regrow(c))) return r;
@@ -798,24 +952,25 @@ int lm_query_pairs(lm_ctx* c, int64_t n, const float* lon, const float* lat, int
     }
     break;
   }
-  if ((r = clear_err_bits(c, ERRB_NAN))) return r;  // non-finite query points are simply never paired
-  uint32_t nv = c->hctrl->n_valid;
-  size_t ndir = (size_t)c->hctrl->n_dir;
-  int sorted = radix_passes(c->key_bits) & 1;
-  std::vector<uint32_t> deg(nv), off(nv), ids(nv), adj(ndir);
+  if ((r = clear_err_bits(c, ERRB_NAN))) return r;  // non-finite query points are never paired
+  const uint32_t nv = c->hctrl->n_valid;
+  const size_t novf = (size_t)c->hctrl->ovf_used;
+  std::vector<uint32_t> deg(nv), off(nv), ids(nv), slab((size_t)nv * SLAB), ovf(novf);
   if (nv) {
     CK(cudaMemcpyAsync(deg.data(), c->deg, nv * 4, cudaMemcpyDeviceToHost, c->st));
     CK(cudaMemcpyAsync(off.data(), c->off, nv * 4, cudaMemcpyDeviceToHost, c->st));
-    CK(cudaMemcpyAsync(ids.data(), c->id[sorted], nv * 4, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaMemcpyAsync(ids.data(), c->sid, nv * 4, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaMemcpyAsync(slab.data(), c->slab, (size_t)nv * SLAB * 4, cudaMemcpyDeviceToHost, c->st));
   }
-  if (ndir) CK(cudaMemcpyAsync(adj.data(), c->adj, ndir * 4, cudaMemcpyDeviceToHost, c->st));
+  if (novf) CK(cudaMemcpyAsync(ovf.data(), c->ovf, novf * 4, cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
   std::vector<uint64_t> pairs;
-  pairs.reserve(ndir / 2);
+  pairs.reserve((size_t)c->hctrl->n_dir / 2);
   for (uint32_t s = 0; s < nv; ++s)
-    for (uint32_t x = off[s]; x < off[s] + deg[s]; ++x) {
-      uint32_t a = ids[s], b = ids[adj[x]];
-      if (a < b) pairs.push_back(((uint64_t)a << 32) | b);
+    for (uint32_t h = 0; h < deg[s]; ++h) {
+      const uint32_t t = deg[s] <= SLAB ? slab[(size_t)s * SLAB + h] : ovf[(size_t)off[s] + h];
+      const uint32_t a_ = ids[s], b_ = ids[t];
+      if (a_ < b_) pairs.push_back(((uint64_t)a_ << 32) | b_);
     }
   std::sort(pairs.begin(), pairs.end());
   *n_pairs = (int64_t)pairs.size();
@@ -833,19 +988,24 @@ int lm_interact(lm_ctx* c, int64_t n, const float* lon, const float* lat, int64_
   if (!c || (n > 0 && (!lon || !lat))) return fail(c, LM_ERR_ARG, "NULL argument");
   if (!c->has_params) return fail(c, LM_ERR_STATE, "call lm_set_interaction first");
   if (!c->has_species) return fail(c, LM_ERR_STATE, "upload species (lm_particles_upload or lm_species_upload) first");
-  if (n != (int64_t)c->n) return fail(c, LM_ERR_ARG, "n = %lld but the context holds %u species", (long long)n, c->n);
+  if (n != (int64_t)c->ntotal) return fail(c, LM_ERR_ARG, "n = %lld but the context holds %u species", (long long)n, c->ntotal);
+  if (c->n_ens != 1) return fail(c, LM_ERR_STATE, "lm_interact works on a single ensemble");
   CK(cudaSetDevice(c->device));
   if (n == 0) return LM_OK;
   int r;
   if ((r = stage_positions(c, n, lon, lat))) return r;
+  if ((flags & LM_STEP_LOG_PAIRS) && c->plog_cap < (uint64_t)8 * c->nslots + 1024) {
+    c->plog_cap = (uint32_t)std::min<uint64_t>((uint64_t)8 * c->nslots + 1024, 0x7fffffffull);
+    if ((r = dalloc(c, &c->plog, (size_t)3 * c->plog_cap))) return r;
+  }
   if ((r = write_ctrl_step(c, step_index))) return r;
+  const StepArgs a = step_args(0.0, 1.0, step_index, 0.0, false);
+  const Bufs b = bufs(c, false);
   for (;;) {
-    StepArgs a = step_args(c, 0.0, 1.0, step_index, 0.0, false);
-    launch_step_begin(c->ctrl, c->st);
-    PROF(c, P_KEYS, launch_keys_from_pos(c->grid, c->ctrl, c->plon, c->plat, c->key[0], c->id[0], (uint32_t)n, c->st));
-    CK(enqueue_interaction(c, a, flags | LM_STEP_INTERACT, (uint32_t)n));
-    if (flags & LM_STEP_CENSUS) launch_census(c->species, c->ctrl, c->n, c->st);
-    launch_step_end(c->ctrl, c->st);
+    PROF(c, P_BOOKKEEPING, launch_step_begin(b, c->ctrl, c->st));
+    CK(enqueue_interaction(c, a, flags | LM_STEP_INTERACT, true, false));
+    if (flags & LM_STEP_CENSUS) PROF(c, P_CENSUS, launch_census(b, c->ctrl, c->st));
+    PROF(c, P_BOOKKEEPING, launch_step_end(c->ctrl, true, c->st));
     CK(cudaGetLastError());
     if ((r = read_ctrl(c))) return r;
     if (c->hctrl->halt) {  // halted before the rounds ran: species untouched, safe to redo
@@ -857,6 +1017,7 @@ int lm_interact(lm_ctx* c, int64_t n, const float* lon, const float* lat, int64_
   }
   if ((r = clear_err_bits(c, ERRB_NAN))) return r;  // non-finite positions are excluded from pairing
   c->next_step = step_index + 1;
+  if (c->plog && c->hctrl->plog_n > c->plog_cap) return fail(c, LM_ERR_CAPACITY, "pair log truncated");
   return consume_errors(c);
 }
 
@@ -865,10 +1026,9 @@ int lm_pairs_get(lm_ctx* c, int32_t* pi, int32_t* pj, int32_t* round, int64_t ca
   CK(cudaSetDevice(c->device));
   int r;
   if ((r = read_ctrl(c))) return r;
-  uint32_t m = std::min(c->hctrl->plog_n, c->plog_cap);
+  const uint32_t m = std::min(c->hctrl->plog_n, c->plog_cap);
   *n = m;
-  if (m == 0) return LM_OK;
-  if (!pi || !pj || !round) return LM_OK;  // count query
+  if (m == 0 || !pi || !pj || !round) return LM_OK;  // count query
   if ((int64_t)m > cap) return fail(c, LM_ERR_CAPACITY, "pair log holds %u pairs", m);
   std::vector<uint32_t> h((size_t)3 * m);
   CK(cudaMemcpyAsync(h.data(), c->plog, h.size() * 4, cudaMemcpyDeviceToHost, c->st));
@@ -876,49 +1036,18 @@ int lm_pairs_get(lm_ctx* c, int32_t* pi, int32_t* pj, int32_t* round, int64_t ca
   std::vector<uint32_t> order(m);
   for (uint32_t k = 0; k < m; ++k) order[k] = k;
   std::sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) {
-    const uint32_t* a = &h[3 * x];
-    const uint32_t* b = &h[3 * y];
+    const uint32_t* a = &h[3 * (size_t)x];
+    const uint32_t* b = &h[3 * (size_t)y];
     if (a[2] != b[2]) return a[2] < b[2];
     if (a[0] != b[0]) return a[0] < b[0];
     return a[1] < b[1];
   });
   for (uint32_t k = 0; k < m; ++k) {
-    const uint32_t* e = &h[3 * order[k]];
-    pi[k] = (int32_t)e[0];
-    pj[k] = (int32_t)e[1];
+    const uint32_t* e = &h[3 * (size_t)order[k]];
+    pi[k] = c->hmap[e[0]];  // slots -> caller indices
+    pj[k] = c->hmap[e[1]];
     round[k] = (int32_t)e[2];
   }
-  return LM_OK;
-}
-
-static int capture(lm_ctx* c) {
-  if (c->gexec) cudaGraphExecDestroy(c->gexec);
-  if (c->graph) cudaGraphDestroy(c->graph);
-  c->gexec = nullptr;
-  c->graph = nullptr;
-  CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
-  c->capturing = true;
-  for (int k = 0; k < c->g_spg; ++k) {
-    StepArgs a = step_args(c, c->g_t_start, c->g_dt, c->g_step0, c->g_kh, true);
-    cudaError_t le = enqueue_step(c, a, c->g_flags, true);
-    if (le != cudaSuccess) {
-      c->capturing = false;
-      cudaGraph_t g = nullptr;
-      cudaStreamEndCapture(c->st, &g);
-      if (g) cudaGraphDestroy(g);
-      cudaGetLastError();
-      return fail(c, LM_ERR_CUDA, "launch during capture failed: %s", cudaGetErrorString(le));
-    }
-  }
-  cudaGraph_t g = nullptr;
-  cudaError_t e = cudaStreamEndCapture(c->st, &g);
-  c->capturing = false;
-  if (e != cudaSuccess) {
-    cudaGetLastError();
-    return fail(c, LM_ERR_CUDA, "stream capture failed: %s", cudaGetErrorString(e));
-  }
-  c->graph = g;
-  CK(cudaGraphInstantiate(&c->gexec, c->graph, 0));
   return LM_OK;
 }
 
@@ -926,14 +1055,10 @@ int lm_graph_capture(lm_ctx* c, double t_start, double dt_sec, int64_t step0, in
                      double kh_deg2_s) {
   if (!c) return LM_ERR_ARG;
   if (steps_per_graph < 1) return fail(c, LM_ERR_ARG, "steps_per_graph must be >= 1");
-  if (!(flags & LM_STEP_ADVECT)) return fail(c, LM_ERR_ARG, "graph steps need LM_STEP_ADVECT");
-  if (!c->has_field || !c->has_particles) return fail(c, LM_ERR_STATE, "field and particles must be uploaded first");
-  if ((flags & LM_STEP_INTERACT) && !c->has_params) return fail(c, LM_ERR_STATE, "call lm_set_interaction first");
+  int r;
+  if ((r = check_ready(c, flags))) return r;
   if (!(dt_sec != 0) || !std::isfinite(dt_sec)) return fail(c, LM_ERR_ARG, "dt must be finite and nonzero");
   CK(cudaSetDevice(c->device));
-  if (!c->has_params) set_pair_params(c, 0.0, LM_NORM_L2);
-  int r;
-  if ((r = set_field_grid(c))) return r;
   c->g_t_start = t_start;
   c->g_dt = dt_sec;
   c->g_step0 = step0;
@@ -952,24 +1077,24 @@ int lm_graph_run(lm_ctx* c, int n_launches, int sync) {
   const int64_t first = c->next_step;
   const int64_t total = (int64_t)n_launches * c->g_spg;
   int r;
-  if ((r = check_time(c, c->g_t_start + (first - c->g_step0) * c->g_dt, c->g_dt, (int)total))) return r;
+  if ((r = check_time(c, c->g_t_start + (first - c->g_step0) * c->g_dt, c->g_dt, total))) return r;
   for (int k = 0; k < n_launches; ++k) CK(cudaGraphLaunch(c->gexec, c->st));
   c->next_step = first + total;
   if (!sync) return LM_OK;
   if ((r = read_ctrl(c))) return r;
   if (c->hctrl->halt) {
-    // A step overflowed its neighbour lists: the graph halted at that step (already advected).
-    // Regrow, finish that step and the rest with plain launches, then recapture for later runs.
-    int64_t k = (int64_t)c->hctrl->halt_step;
+    // A step overflowed a capacity: the graph halted at that step (already advected). Regrow,
+    // finish that step and the rest with plain launches, then recapture for later runs.
+    const int64_t k = (int64_t)c->hctrl->halt_step;
     if ((r = regrow(c))) return r;
     if ((r = write_ctrl_step(c, k))) return r;
-    StepArgs a = step_args(c, c->g_t_start + (k - c->g_step0) * c->g_dt, c->g_dt, k, c->g_kh, false);
+    const StepArgs a = step_args(c->g_t_start + (k - c->g_step0) * c->g_dt, c->g_dt, k, c->g_kh, false);
     CK(enqueue_step(c, a, c->g_flags, false));
     if ((r = read_ctrl(c))) return r;
-    if (c->hctrl->halt) return fail(c, LM_ERR_CAPACITY, "neighbour lists overflowed again after regrowth");
-    int64_t rest = first + total - (k + 1);
+    if (c->hctrl->halt) return fail(c, LM_ERR_CAPACITY, "capacity exceeded again after regrowth");
+    const int64_t rest = first + total - (k + 1);
     if (rest > 0) {
-      r = run_steps(c, c->g_t_start + (k + 1 - c->g_step0) * c->g_dt, c->g_dt, (int)rest, k + 1, c->g_flags, c->g_kh,
+      r = run_steps(c, c->g_t_start + (k + 1 - c->g_step0) * c->g_dt, c->g_dt, rest, k + 1, c->g_flags, c->g_kh,
                     nullptr, nullptr, nullptr, nullptr);
       if (r) return r;
     }
@@ -991,29 +1116,43 @@ int lm_stats_get(lm_ctx* c, lm_stats* out) {
   int r;
   if ((r = read_ctrl(c))) return r;
   const Ctrl& h = *c->hctrl;
-  out->n_particles = c->n;
+  out->n_particles = c->ntotal;
   out->pairs = (int64_t)(h.n_dir / 2);
   out->rounds = h.rounds;
   out->max_rounds = h.max_rounds;
   out->out_of_bounds = h.oob;
   out->step = h.step;
   for (int k = 0; k < 4; ++k) out->census[k] = h.census[k];
-  out->adj_capacity = (int64_t)c->adj_cap;
+  out->adj_capacity = (int64_t)c->ovf_cap;
   out->regrows = c->regrows;
   out->pairs_total = (int64_t)h.pairs_total;
   out->steps_total = (int64_t)h.steps_total;
+  out->cells = h.ncells;
+  out->long_lists = h.n_long;
+  out->n_ensembles = c->n_ens;
   return LM_OK;
 }
 
 int lm_stats_reset(lm_ctx* c) {
   if (!c) return LM_ERR_ARG;
   CK(cudaSetDevice(c->device));
-  uint32_t zero = 0;
-  unsigned long long z64 = 0;
+  const uint32_t zero = 0;
+  const unsigned long long z64 = 0;
   CK(cudaMemcpyAsync(&c->ctrl->max_rounds, &zero, sizeof(zero), cudaMemcpyHostToDevice, c->st));
   CK(cudaMemcpyAsync(&c->ctrl->pairs_total, &z64, sizeof(z64), cudaMemcpyHostToDevice, c->st));
   CK(cudaMemcpyAsync(&c->ctrl->steps_total, &z64, sizeof(z64), cudaMemcpyHostToDevice, c->st));
   CK(cudaStreamSynchronize(c->st));
+  return LM_OK;
+}
+
+int lm_census_get(lm_ctx* c, int64_t* out, int64_t cap) {
+  if (!c || !out) return LM_ERR_ARG;
+  if (cap < 4 * (int64_t)c->n_ens) return fail(c, LM_ERR_CAPACITY, "need %u entries", 4 * c->n_ens);
+  CK(cudaSetDevice(c->device));
+  std::vector<uint32_t> h((size_t)4 * c->n_ens);
+  if (!h.empty()) CK(cudaMemcpyAsync(h.data(), c->census, h.size() * 4, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  for (size_t k = 0; k < h.size(); ++k) out[k] = h[k];
   return LM_OK;
 }
 

@@ -1,20 +1,21 @@
 // Internal declarations shared by the CUDA translation units of liblmgb300.
 //
-// Data layout in HBM (one context = one GPU stream):
-//   field      float2 uv[nt][ny][nx]      (u,v interleaved so one 8-byte load gives both)
-//   state      float  xo[N], yo[N]        (lon/lat offsets from a float32 origin, id order)
-//              int8   species[N]          (ROCK=1, PAPER=2, SCISSORS=3, id order)
-//              uint8  status[N]           (bit0 out of domain, bit1 non-finite)
-//   per step   float  plon[N], plat[N]    (absolute float32 lon/lat after advection, id order)
-//              uint32 key[2][N], id[2][N] (radix-sort ping-pong of (cell key, particle id))
-//              float2 spos[N]             (pos gathered into cell order)
-//              uint32 cell_start[ncells]  (first sorted index of each occupied cell; never cleared,
-//                                          an entry is trusted only if key[start] == cell)
-//              uint32 deg[N], off[N]      (neighbour counts / CSR offsets, cell order)
-//              uint32 adj[cap]            (neighbour lists in cell-order indices, each list sorted by
-//                                          descending pair priority)
-//              uint64 prio[cap]           (pair priorities while the lists are sorted)
-//              uint32 want[N], head[N], level[N], act[N]  (interaction dataflow)
+// One context holds E >= 1 independent ensembles. Particle arrays use a padded slot layout:
+// ensemble e owns slots [base_e, base_e + n_e) and, when E > 1, base_e is a multiple of
+// SLOT_BLOCK so that every 256-slot block belongs to one ensemble (block_ens[block]). Pad slots
+// carry status PAD and never take part in anything.
+//
+// Data layout in HBM:
+//   field      float2 uv[F][nt][ny][nx]   (u,v interleaved; ensemble e reads field_off_e)
+//   state      float  xo[S], yo[S]        (lon/lat offsets from a float32 origin, slot order)
+//              int8   species[S], uint8 status[S]
+//   per step   float  plon[S], plat[S]    (absolute float32 lon/lat after advection, pre-kick)
+//              uint32 key[S], rank[S]     (cell key, rank inside the cell from the counting pass)
+//              uint32 ccount[C+1], cstart[C+1]  (cell counts / exclusive starts, C = cell capacity)
+//              uint32 sid[S], skey[S], sens[S]; float2 spos[S]  (particles in cell order)
+//              uint32 deg[S], slab[S][SLAB]     (neighbour lists up to SLAB, sorted by priority)
+//              uint32 off[S], ovf[cap]; uint64 oprio[cap]  (longer lists, allocated per step)
+//              uint32 want[S], head[S], level[S], act[S]   (interaction dataflow)
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -22,42 +23,64 @@
 namespace lm {
 
 constexpr uint32_t NONE = 0xffffffffu;
+constexpr uint32_t SLOT_BLOCK = 256;   // threads per block of every per-slot kernel
+constexpr uint32_t SLAB = 8;           // neighbour-list entries kept in the per-vertex slab
+constexpr uint8_t STATUS_OK = 0, STATUS_OOB = 1, STATUS_NAN = 2, STATUS_PAD = 3;
 
 // Sticky error bits in Ctrl::err (mirrored by the LM_ERR_* status codes of lm_api.h).
 enum : uint32_t {
   ERRB_OOB = 1u << 0,        // a particle left the field domain (frozen, excluded from pairing)
   ERRB_NAN = 1u << 1,        // a non-finite position or velocity
-  ERRB_OVERFLOW = 1u << 2,   // neighbour-list capacity exceeded (step halted)
-  ERRB_ROUNDCAP = 1u << 3,   // interaction round cap reached
+  ERRB_OVERFLOW = 1u << 2,   // long-list capacity exceeded (step halted)
+  ERRB_ROUNDCAP = 1u << 3,   // reserved
   ERRB_TIMEOUT = 1u << 4,    // a bounded device wait gave up
   ERRB_TIME = 1u << 5,       // a stage time fell outside the field's time axis
 };
 
 // Device control block: one per context, lives in device memory.
 struct Ctrl {
-  unsigned long long n_dir;   // directed neighbour entries of the current step (2 x pairs)
-  unsigned long long cap;     // capacity of adj/prio
-  uint32_t err;               // sticky error bits
-  uint32_t halt;              // nonzero: every later kernel of the step sequence returns at once
-  uint32_t halt_step;         // step index at which halt was raised
-  uint32_t step;              // device-side step counter (used by captured graphs)
-  uint32_t oob;               // particles flagged out of domain (sticky count)
-  uint32_t n_valid;           // particles with a valid cell key this step
-  uint32_t rounds;            // interaction rounds used by the current step
-  uint32_t max_rounds;        // max over steps since the last reset
-  uint32_t applied;           // pairs whose species differed (draws taken) this step
-  uint32_t plog_n;            // pair-log entries written this step
-  uint32_t bar_count;         // grid barrier arrival counter
-  uint32_t bar_gen;           // grid barrier generation
-  uint32_t act_n[3];          // active-vertex list sizes (rotating)
-  uint32_t census[4];         // species counts after the current step (index = species)
-  unsigned long long pairs_total;  // unordered pairs summed over steps since the last stats reset
-  unsigned long long steps_total;  // interaction steps since the last stats reset
+  unsigned long long n_dir;     // directed neighbour entries of the current step (2 x pairs)
+  unsigned long long ovf_cap;   // capacity of ovf/oprio
+  unsigned long long ovf_used;  // long-list entries requested this step
+  unsigned long long pairs_total;  // unordered pairs summed over completed steps since the last reset
+  unsigned long long steps_total;  // interaction steps since the last reset
+  uint32_t err;                 // sticky error bits
+  uint32_t halt;                // nonzero: every later kernel of the step sequence returns at once
+  uint32_t halt_step;           // step index at which halt was raised
+  uint32_t step;                // device-side step counter (used by captured graphs)
+  uint32_t oob;                 // particles flagged out of domain or non-finite (sticky count)
+  uint32_t n_valid;             // particles binned this step
+  uint32_t ncells;              // cells of this step's grids (sum over ensembles)
+  uint32_t n_long;              // vertices whose list exceeds SLAB
+  uint32_t rounds;              // longest dependency chain (levels) of the current step
+  uint32_t max_rounds;          // max over steps since the last reset
+  uint32_t plog_n;              // pair-log entries written this step
+  uint32_t act_n;               // active vertices (with at least one pair)
+  uint32_t census[4];           // species counts after the step, all ensembles ([0] = other values)
+  uint32_t pad[2];
 };
 
-// Velocity field as the advection kernel sees it.
+// Per-ensemble constants (device array, one entry per ensemble).
+struct EnsInfo {
+  unsigned long long t_rs, t_pr, t_sp;  // u53 < t  <=>  r < p (exact)
+  unsigned long long field_off;         // element offset of this ensemble's frames in uv
+  uint32_t seed_lo, seed_hi;            // Philox key of pair draws and diffusion kicks
+  uint32_t base;                        // first slot
+  uint32_t n;                           // microbes
+};
+
+// Per-step uniform cell grid of one ensemble: cell (cx, cy) covers
+// [x0 + cx*c, x0 + (cx+1)*c) x [y0 + cy*c, ...), c >= radius; global key = cell_base + cy*ncx + cx.
+struct EnsGrid {
+  float x0, y0, inv_c, c;
+  int ncx, ncy;
+  uint32_t cell_base;
+  uint32_t pad;
+};
+
+// Velocity field geometry shared by all ensembles.
 struct FieldView {
-  const float2* uv;   // [nt][ny][nx]
+  const float2* uv;   // [F][nt][ny][nx]
   int nx, ny, nt;
   float gx0, gy0;     // grid origin minus the state origin (degrees, small)
   float inv_dx, inv_dy;
@@ -66,92 +89,110 @@ struct FieldView {
   double t0, dT;      // frame 0 time and frame spacing (seconds)
 };
 
-// Uniform cell grid for binning: cell (cx, cy) covers
-// [x0 + cx*c, x0 + (cx+1)*c) x [y0 + cy*c, y0 + (cy+1)*c) with c >= radius.
-struct CellGrid {
-  float x0, y0;       // absolute degrees
-  float inv_c;
-  int ncx, ncy;
-  uint32_t ncells;    // ncx*ncy; key value ncells marks an invalid (excluded) particle
-};
-
 struct PairParams {
   double r;           // radius (degrees)
   double r2;          // fl(r*r)
   float r2f_lo, r2f_hi;  // float32 accept / reject thresholds around r^2 (p = 2)
   float rf_lo, rf_hi;    // float32 accept / reject thresholds around r   (p = 1, inf)
+  float inv2r;        // 0.5 / r: scale of the colour grid of the pair order (0 when r == 0)
+  float cell_factor;  // binning cell size = cell_factor * r (>= 1.004)
   int norm;           // 1, 2 or 0 (= infinity)
 };
 
-struct RpsParams {
-  unsigned long long t_rs, t_pr, t_sp;  // u53 < t  <=>  u53 * 2^-53 < p
-  uint32_t seed_lo, seed_hi;
-};
-
 struct StepArgs {
-  double t_start;     // time of step 0 of this launch sequence (seconds, field clock)
+  double t_start;     // time of step step0 (seconds, field clock)
   double dt;          // step length (seconds)
   uint32_t step0;     // global step index of t_start
   int use_ctrl_step;  // 1: step index = ctrl->step (graph mode); 0: step index = step0
   float kick;         // sqrt(6 |dt| Kh) in degrees, 0 disables the diffusion kick
-  uint32_t seed_lo, seed_hi;
+};
+
+// Everything the per-step kernels need besides the field.
+struct Bufs {
+  const EnsInfo* ens;
+  const uint32_t* block_ens;
+  uint32_t n_ens;
+  uint32_t nslots;
+  uint32_t cells_cap;
+  float* xo;
+  float* yo;
+  int8_t* species;
+  uint8_t* status;
+  float* plon;
+  float* plat;
+  uint32_t* ebox;     // [E][4] ordered-int encoded min x, min y, max x, max y
+  EnsGrid* grids;     // [E]
+  uint32_t* key;
+  uint32_t* rank;
+  uint32_t* ccount;   // [cells_cap + 1]
+  uint32_t* cstart;   // [cells_cap + 1]
+  uint32_t* csum;     // [SCAN_BLOCKS]
+  uint32_t* sid;
+  uint32_t* skey;
+  uint32_t* sens;
+  float2* spos;
+  uint32_t* deg;
+  uint32_t* slab;     // [S][SLAB]
+  uint32_t* off;
+  uint32_t* ovf;
+  unsigned long long* oprio;
+  uint32_t* longv;    // vertices with lists longer than SLAB
+  uint32_t* want;
+  uint32_t* head;
+  uint32_t* level;
+  uint32_t* act;
+  uint32_t* census;   // [E][4]
+  uint32_t* plog;     // 3 x uint32 per logged pair (slot i, slot j, level) or nullptr
+  uint32_t plog_cap;
 };
 
 // ---- launchers (each enqueues on `st`) ----
 void launch_interleave(const float* u, const float* v, float2* uv, size_t n, cudaStream_t st);
-void launch_advect(const FieldView& f, const CellGrid& g, const StepArgs& a, Ctrl* ctrl, float* xo, float* yo,
-                   uint8_t* status, float* plon, float* plat, uint32_t* key, uint32_t* id, uint32_t n,
-                   cudaStream_t st);
-void launch_keys_from_pos(const CellGrid& g, Ctrl* ctrl, const float* lon, const float* lat, uint32_t* key,
-                          uint32_t* id, uint32_t n, cudaStream_t st);
+void launch_step_begin(const Bufs& b, Ctrl* ctrl, cudaStream_t st);
+void launch_step_end(Ctrl* ctrl, bool interact, cudaStream_t st);
+void launch_advect(const FieldView& f, const StepArgs& a, const Bufs& b, Ctrl* ctrl, cudaStream_t st);
+void launch_bbox(const Bufs& b, Ctrl* ctrl, bool use_status, cudaStream_t st);
 
-// LSD radix sort of (key, id), 8-bit digits: per pass hist -> scan -> scatter (ping-pong buffers).
-struct SortScratch {
-  uint32_t* counts;      // [256 * ntiles]
-  uint32_t* digit_total; // [256]
-  uint32_t ntiles_cap;
-};
-int sort_tiles(uint32_t n);
-int radix_passes(int bits);
-void launch_radix_hist(const uint32_t* key, uint32_t n, int shift, SortScratch& s, uint32_t* digit_total, Ctrl* ctrl,
+// K2 binning: per-ensemble grids, counting pass, cell scan, scatter into cell order.
+constexpr int SCAN_BLOCKS = 304;
+void launch_grid(const Bufs& b, const PairParams& pp, Ctrl* ctrl, cudaStream_t st);
+void launch_keys(const Bufs& b, Ctrl* ctrl, bool use_status, cudaStream_t st);
+void launch_cell_scan(const Bufs& b, Ctrl* ctrl, cudaStream_t st);
+void launch_scatter(const Bufs& b, Ctrl* ctrl, cudaStream_t st);
+
+// K3 neighbour lists.
+void launch_sweep(const Bufs& b, const PairParams& pp, const StepArgs& a, Ctrl* ctrl, cudaStream_t st);
+void launch_sweep_long(const Bufs& b, const PairParams& pp, const StepArgs& a, Ctrl* ctrl, int sms,
                        cudaStream_t st);
-void launch_radix_scan(uint32_t n, SortScratch& s, const uint32_t* digit_total, Ctrl* ctrl, cudaStream_t st);
-void launch_radix_scatter(const uint32_t* kin, const uint32_t* vin, uint32_t* kout, uint32_t* vout, uint32_t n,
-                          int shift, SortScratch& s, Ctrl* ctrl, cudaStream_t st);
-void launch_cells(const uint32_t* key, const uint32_t* id, const float* plon, const float* plat, float2* spos,
-                  uint32_t* cell_start, Ctrl* ctrl, uint32_t n, uint32_t invalid_key, cudaStream_t st);
 
-// Pair sweep and neighbour lists.
-int sweep_blocks(uint32_t n);
-void launch_sweep_count(const CellGrid& g, const PairParams& pp, const uint32_t* key, const float2* spos,
-                        const uint32_t* cell_start, Ctrl* ctrl, uint32_t* deg, uint32_t* block_sum, uint32_t n,
-                        cudaStream_t st);
-void launch_scan_blocks(uint32_t* block_sum, uint32_t nblocks, Ctrl* ctrl, cudaStream_t st);
-void launch_sweep_fill(const CellGrid& g, const PairParams& pp, const RpsParams& rp, const StepArgs& a,
-                       const uint32_t* key, const uint32_t* id, const float2* spos, const uint32_t* cell_start,
-                       const uint32_t* block_sum, Ctrl* ctrl, const uint32_t* deg, uint32_t* off, uint32_t* adj,
-                       unsigned long long* prio, uint32_t* want0, uint32_t* head, uint32_t* act0, uint32_t* level,
-                       uint32_t n, cudaStream_t st);
-
-// Interaction rounds (cooperative persistent kernel).
-struct RoundBufs {
-  const uint32_t* off;
-  const uint32_t* deg;
-  const uint32_t* adj;
-  const uint32_t* id;
-  int8_t* species;
-  uint32_t* want[2];
-  uint32_t* head;
-  uint32_t* act[2];
-  uint32_t* level;    // per vertex: level of its last applied pair
-  uint32_t* plog;     // 3 x uint32 per logged pair (i, j, level) or nullptr
-  uint32_t plog_cap;  // entries
-};
+// K4/K5 interaction dataflow (cooperative persistent kernel).
 int rounds_grid(int device, int* block);
-cudaError_t launch_rounds(const RoundBufs& b, const RpsParams& rp, const StepArgs& a, Ctrl* ctrl, uint32_t n,
-                          int grid, int block, uint32_t round_cap, cudaStream_t st);
-void launch_census(const int8_t* species, Ctrl* ctrl, uint32_t n, cudaStream_t st);
-void launch_step_end(Ctrl* ctrl, cudaStream_t st);
-void launch_step_begin(Ctrl* ctrl, cudaStream_t st);
+cudaError_t launch_rounds(const Bufs& b, const StepArgs& a, Ctrl* ctrl, int grid, int block, cudaStream_t st);
+void launch_census(const Bufs& b, Ctrl* ctrl, cudaStream_t st);
+void launch_unpad(const float* src, float* dst, const int32_t* map, uint32_t nslots, cudaStream_t st);
+void launch_unpad8(const int8_t* src, int8_t* dst, const int32_t* map, uint32_t nslots, cudaStream_t st);
+
+// Ordered-int encoding of floats for atomicMin/atomicMax.
+__host__ __device__ inline uint32_t enc_f(float f) {
+  uint32_t u;
+#ifdef __CUDA_ARCH__
+  u = __float_as_uint(f);
+#else
+  union { float f; uint32_t u; } x;
+  x.f = f;
+  u = x.u;
+#endif
+  return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__host__ __device__ inline float dec_f(uint32_t e) {
+  uint32_t u = (e & 0x80000000u) ? (e & 0x7fffffffu) : ~e;
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(u);
+#else
+  union { float f; uint32_t u; } x;
+  x.u = u;
+  return x.f;
+#endif
+}
 
 }  // namespace lm

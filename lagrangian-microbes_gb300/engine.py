@@ -81,6 +81,10 @@ class Simulation:
         sp = np.ascontiguousarray(species, dtype=np.int8).ravel()
         self.ctx.call("lm_species_upload", sp.size, _lib.ptr(sp))
 
+    def set_cell_factor(self, factor: float) -> None:
+        """Binning cell size in units of the radius (>= 1.004; the pair set does not change)."""
+        self.ctx.call("lm_set_cell_factor", float(factor))
+
     def set_stream(self, stream_handle: int) -> None:
         """Run on an external CUDA stream (e.g. torch.cuda.current_stream().cuda_stream)."""
         self.ctx.call("lm_ctx_set_stream", int(stream_handle))
@@ -163,8 +167,69 @@ class Simulation:
     def stats(self) -> dict:
         return self.ctx.stats()
 
+    def census(self) -> np.ndarray:
+        """[n_ensembles, 4] species counts after the last step run with census=True."""
+        n_ens = max(1, int(self.ctx.stats()["n_ensembles"]))
+        out = np.zeros((n_ens, 4), np.int64)
+        self.ctx.call("lm_census_get", _lib.ptr(out), out.size)
+        return out
+
     def close(self) -> None:
         self.ctx.close()
+
+
+class EnsembleSimulation(Simulation):
+    """Many independent ensembles in one context: every step is one launch sequence for all of them.
+
+    ``fields`` is one VelocityField shared by all ensembles or one per ensemble (same grid);
+    ``ensembles`` a list of (lons, lats, species); ``p_rs``/``p_pr``/``p_sp``/``seeds`` scalars or
+    one value per ensemble. Microbes of different ensembles never pair, and each ensemble draws
+    from its own Philox stream, so every ensemble evolves exactly as it would alone.
+    """
+
+    def __init__(self, fields, ensembles, radius: float = 0.01, norm=2, p_rs=0.5, p_pr=0.5, p_sp=0.5, seeds=0,
+                 kh: float = 0.0, device: int = 0, ctx: _lib.Context | None = None):
+        self.ctx = ctx or _lib.Context(device)
+        self.kh = float(kh)
+        self.radius = float(radius)
+        self.norm = norm
+        flds = fields if isinstance(fields, (list, tuple)) else [fields]
+        self.field = flds[0]
+        self.upload_fields(flds)
+        e = len(ensembles)
+        self.counts = np.array([np.asarray(x[0]).size for x in ensembles], dtype=np.int64)
+        lons = np.concatenate([np.asarray(x[0], np.float64).ravel() for x in ensembles]) if e else np.zeros(0)
+        lats = np.concatenate([np.asarray(x[1], np.float64).ravel() for x in ensembles]) if e else np.zeros(0)
+        sp = np.concatenate([np.asarray(x[2], np.int8).ravel() for x in ensembles]) if e else np.zeros(0, np.int8)
+        self.ctx.call("lm_ensembles_upload", e, _lib.ptr(self.counts), _lib.ptr(lons), _lib.ptr(lats),
+                      _lib.ptr(sp))
+        self.n = int(self.counts.sum())
+        self.n_ensembles = e
+        as_arr = lambda v, dt: np.ascontiguousarray(np.broadcast_to(np.asarray(v, dtype=dt), (e,)))
+        seeds_u = np.array([int(x) & 0xFFFFFFFFFFFFFFFF for x in np.broadcast_to(np.asarray(seeds, dtype=object), (e,))],
+                           dtype=np.uint64)
+        self.ctx.call("lm_set_interaction", float(radius), norm_code(norm), 0.5, 0.5, 0.5, 0)
+        self.ctx.call("lm_set_ensemble_params", e, _lib.ptr(as_arr(p_rs, np.float64)), _lib.ptr(as_arr(p_pr, np.float64)),
+                      _lib.ptr(as_arr(p_sp, np.float64)), _lib.ptr(seeds_u))
+        self.step_index = 0
+        self._graph = None
+
+    def upload_fields(self, flds) -> None:
+        f0 = flds[0]
+        nt, ny, nx = f0.u.shape
+        for f in flds[1:]:
+            if f.u.shape != f0.u.shape or not (np.array_equal(f.lon, f0.lon) and np.array_equal(f.lat, f0.lat)
+                                               and np.array_equal(f.times, f0.times)):
+                raise ValueError("ensemble fields must share one grid and time axis")
+        u = np.ascontiguousarray(np.stack([f.u for f in flds])) if len(flds) > 1 else f0.u
+        v = np.ascontiguousarray(np.stack([f.v for f in flds])) if len(flds) > 1 else f0.v
+        self.ctx.call("lm_field_upload_batch", len(flds), _lib.ptr(u), _lib.ptr(v), nt, ny, nx, _lib.ptr(f0.lon),
+                      _lib.ptr(f0.lat), _lib.ptr(f0.times))
+
+    def split(self, flat):
+        """Split a per-microbe array (last axis) into a list per ensemble."""
+        edges = np.cumsum(self.counts)[:-1]
+        return np.split(np.asarray(flat), edges, axis=-1)
 
 
 def get_pair_log(ctx: _lib.Context):

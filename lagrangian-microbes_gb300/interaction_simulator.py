@@ -74,8 +74,8 @@ class InteractionSimulator:
         t = start_time
         while t < end_time:
             i = self.iteration
-            lon = np.ascontiguousarray(plon[:, i])
-            lat = np.ascontiguousarray(plat[:, i])
+            lon = np.ascontiguousarray(plon[:, i], dtype=np.float32)
+            lat = np.ascontiguousarray(plat[:, i], dtype=np.float32)
             ctx.call("lm_interact", N_particles, _lib.ptr(lon), _lib.ptr(lat), i, 0)
             ctx.call("lm_particles_download", None, None, _lib.ptr(sp), None)
             species[...] = sp  # in place, as the reference's pair function mutates it

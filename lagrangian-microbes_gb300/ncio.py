@@ -37,9 +37,10 @@ def write_particle_file(path: str, variables: dict, start: datetime, times_s: np
 
 
 def read_particle_file(path: str) -> dict:
-    """name -> numpy array (copied out of the memory map) for every variable of the file."""
+    """name -> numpy array in native byte order (NetCDF stores big-endian) for every variable."""
     out = {}
     with netcdf_file(path, "r", mmap=False) as f:
         for name, var in f.variables.items():
-            out[name] = np.array(var[:])
+            a = np.array(var[:])
+            out[name] = a.astype(a.dtype.newbyteorder("="), copy=False)
     return out

@@ -291,3 +291,70 @@ def test_gpu_490k_lattice_first_step_pairs(engine, lm, orc):
     assert sim.stats()["pairs"] == m
     np.testing.assert_array_equal(rec["species"][0], want)
     sim.close()
+
+
+# ---------------- batched ensembles ----------------
+
+def _batched_setup(lm, orc, E=5, seed=12):
+    rng = np.random.default_rng(seed)
+    fields = [lm.synthetic_psi_field(195, 215, 20, 35, 1 / 12, n_frames=14, seed=100 + e) for e in range(E)]
+    ens = []
+    for e in range(E):
+        n = int(np.exp(rng.uniform(np.log(1000), np.log(20000))))
+        side = rng.uniform(0.5, 1.5)
+        x0, y0 = rng.uniform(198, 210), rng.uniform(23, 31)
+        lons, lats = orc.lattice(n, y0, y0 + side, x0, x0 + side)
+        ens.append((lons, lats, rng.integers(1, 4, lons.size).astype(np.int8)))
+    p = rng.uniform(0.5, 0.9, E)
+    seeds = rng.integers(1, 2**62, E)
+    return fields, ens, p, seeds
+
+
+def test_gpu_batched_ensembles_equal_single_runs(engine, lm, orc):
+    fields, ens, p, seeds = _batched_setup(lm, orc)
+    bat = engine.EnsembleSimulation(fields, ens, radius=0.01, p_rs=p, p_pr=p, p_sp=p, seeds=seeds)
+    rec = bat.step(0.0, 3600.0, 10, record=True, census=True)
+    lon_e = bat.split(rec["lon"])
+    sp_e = bat.split(rec["species"])
+    cen = bat.census()
+    for e, (lons, lats, sp0) in enumerate(ens):
+        one = engine.Simulation(fields[e], lons, lats, sp0, radius=0.01, p_rs=p[e], p_pr=p[e], p_sp=p[e],
+                                seed=int(seeds[e]))
+        r1 = one.step(0.0, 3600.0, 10, record=True)
+        np.testing.assert_array_equal(lon_e[e], r1["lon"], err_msg=f"ensemble {e}")
+        np.testing.assert_array_equal(sp_e[e], r1["species"], err_msg=f"ensemble {e}")
+        np.testing.assert_array_equal(cen[e], np.bincount(r1["species"][-1], minlength=4)[:4])
+        one.close()
+    # and the oracle on one ensemble, step by step
+    lons, lats, sp = ens[1]
+    for s in range(10):
+        sp, _ = orc.interact_step(lon_e[1][s], bat.split(rec["lat"])[1][s], sp, 0.01, 2, p[1], p[1], p[1],
+                                  int(seeds[1]), s)
+        np.testing.assert_array_equal(sp_e[1][s], sp)
+    bat.close()
+
+
+def test_gpu_batched_graph_equals_plain(engine, lm, orc):
+    fields, ens, p, seeds = _batched_setup(lm, orc, E=7, seed=4)
+    a = engine.EnsembleSimulation(fields, ens, radius=0.01, p_rs=p, p_pr=p, p_sp=p, seeds=seeds)
+    a.step(0.0, 3600.0, 12)
+    b = engine.EnsembleSimulation(fields, ens, radius=0.01, p_rs=p, p_pr=p, p_sp=p, seeds=seeds)
+    b.capture(0.0, 3600.0, steps_per_graph=4)
+    b.run_graph(3)
+    for x, y in zip(a.state(), b.state()):
+        np.testing.assert_array_equal(x, y)
+    a.close()
+    b.close()
+
+
+def test_gpu_cell_factor_does_not_change_results(engine, lm, orc):
+    fld, lons, lats, sp0 = _fused_setup(lm, orc, n=20000, seed=6)
+    out = []
+    for f in (1.004, 2.0, 3.5):
+        sim = engine.Simulation(fld, lons, lats, sp0, radius=0.01, p_rs=0.7, p_pr=0.7, p_sp=0.7, seed=3)
+        sim.set_cell_factor(f)
+        rec = sim.step(0.0, 3600.0, 5, record=True)
+        out.append(rec["species"])
+        sim.close()
+    np.testing.assert_array_equal(out[0], out[1])
+    np.testing.assert_array_equal(out[0], out[2])

@@ -131,6 +131,7 @@ def test_netcdf_roundtrip(tmp_path):
     np.testing.assert_array_equal(d["species"], sp)
     np.testing.assert_array_equal(d["particle number"], np.arange(1, 8))
     np.testing.assert_array_equal(d["time"], np.arange(4) * 3600.0)
+    assert all(a.dtype.isnative for a in d.values())  # NetCDF is big-endian on disk
 
 
 def test_shard_partitions(lm):
