@@ -183,6 +183,22 @@ int lm_profile_enable(lm_ctx* ctx, int on);
 int lm_profile_get(lm_ctx* ctx, int kernel, char* name, size_t name_len, double* total_ms, int64_t* launches);
 int lm_profile_count(void);
 
+/* Pair counting for callers that cannot allocate device memory (no counterpart in the reference;
+ * it has no GPU path). Some callers may not call cudaMalloc/cudaFree at all: code running inside
+ * another library's stream capture, hosts that give all device memory to their own pool, plugins
+ * whose process forbids allocation after start-up. They pass device pointers: d_lon, d_lat
+ * (float32[n]) in, d_degree (int32[n], neighbours of each point) and d_pairs (one uint64, the
+ * number of unordered pairs, the size of cKDTree.query_pairs) out, all written on `stream` (a
+ * cudaStream_t as an integer, 0 = default stream). Pair semantics are lm_query_pairs'.
+ * Nothing is allocated: the scratch is a fixed ~1.8 MB array inside the library that every GPU
+ * loading it keeps until the process exits, so n is limited to 65536 (larger n: LM_ERR_ARG).
+ * The first call on a device looks up that array's device address; make that first call before
+ * any stream capture. All calls share the array and it keeps the last call's contents, so calls
+ * whose work overlaps on the GPU (other streams, other threads) race: serialise them.
+ * Errors: lm_last_error(NULL, ...). */
+int lm_count_pairs_noalloc(const float* d_lon, const float* d_lat, int64_t n, double radius, int norm,
+                           int32_t* d_degree, unsigned long long* d_pairs, uintptr_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -120,6 +120,7 @@ SIGNATURES = {
     "lm_profile_enable": [P, I32],
     "lm_profile_get": [P, I32, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(F64), ctypes.POINTER(I64)],
     "lm_profile_count": [],
+    "lm_count_pairs_noalloc": [P, P, I64, F64, I32, P, P, ctypes.c_size_t],
 }
 
 

@@ -1184,3 +1184,7 @@ int lm_profile_get(lm_ctx* c, int kernel, char* name, size_t name_len, double* t
 int lm_profile_count(void) { return P_COUNT; }
 
 }  // extern "C"
+
+namespace lm {
+void set_thread_error(const char* msg) { g_create_error = msg ? msg : ""; }
+}  // namespace lm

@@ -172,6 +172,9 @@ void launch_census(const Bufs& b, Ctrl* ctrl, cudaStream_t st);
 void launch_unpad(const float* src, float* dst, const int32_t* map, uint32_t nslots, cudaStream_t st);
 void launch_unpad8(const int8_t* src, int8_t* dst, const int32_t* map, uint32_t nslots, cudaStream_t st);
 
+// Message for lm_last_error(NULL, ...) from entry points that have no context.
+void set_thread_error(const char* msg);
+
 // Ordered-int encoding of floats for atomicMin/atomicMax.
 __host__ __device__ inline uint32_t enc_f(float f) {
   uint32_t u;
