@@ -274,6 +274,7 @@ def run_gb300(args):
             "e2e": e2e, "cpu_baseline": cpu, "clocks": clk,
             "gpu_launches": int(round(launches_per_step * K)),
             "max_rounds": stats["max_rounds"],
+            "mean_rounds": stats["rounds_total"] / max(stats["steps_total"], 1),
         }
         print(json.dumps(line), flush=True)
     sim.close()

@@ -36,7 +36,7 @@ extern "C" {
 #define LM_ERR_STATE 4          /* call out of order (no field / no particles / no parameters) */
 #define LM_ERR_OUT_OF_BOUNDS 5  /* particles left the field domain (they are frozen and excluded) */
 #define LM_ERR_NAN 6            /* non-finite positions */
-#define LM_ERR_ROUND_CAP 7      /* interaction round cap reached */
+#define LM_ERR_ROUND_CAP 7      /* a microbe has more than 2^24 - 1 neighbours in one step */
 #define LM_ERR_TIMEOUT 8        /* a bounded device wait gave up; the context stays usable */
 #define LM_ERR_TIME 9           /* a stage time fell outside the field's time axis */
 #define LM_ERR_GRID 10          /* field axes are not uniformly spaced / ascending */
@@ -70,6 +70,7 @@ typedef struct lm_stats {
   int64_t cells;          /* binning cells of the last step (all ensembles) */
   int64_t long_lists;     /* microbes of the last step with more than 8 neighbours */
   int64_t n_ensembles;
+  int64_t rounds_total;   /* levels summed over interaction steps since lm_stats_reset */
 } lm_stats;
 
 int lm_version(void);

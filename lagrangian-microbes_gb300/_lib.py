@@ -72,6 +72,7 @@ class Stats(ctypes.Structure):
         ("cells", ctypes.c_int64),
         ("long_lists", ctypes.c_int64),
         ("n_ensembles", ctypes.c_int64),
+        ("rounds_total", ctypes.c_int64),
     ]
 
     def as_dict(self) -> dict:

@@ -125,16 +125,14 @@ __global__ void __launch_bounds__(SLOT_BLOCK) k_advect(FieldView f, StepArgs a, 
   __shared__ int sh_skip;
   __shared__ EnsInfo sh_ens;
   __shared__ uint32_t sh_e;
-  if (threadIdx.x == 0) {
-    uint32_t step = a.use_ctrl_step ? ctrl->step : a.step0;
-    double t = a.t_start + (double)(int)(step - a.step0) * a.dt;
-    sh[0] = stage_at(f, t);
-    sh[1] = stage_at(f, t + 0.5 * a.dt);
-    sh[2] = stage_at(f, t + a.dt);
-    sh_step = step;
-    int ok = sh[0].ok && sh[1].ok && sh[2].ok;
-    sh_skip = ctrl->halt != 0 || !ok;
-    if (!ok && blockIdx.x == 0) atomicOr(&ctrl->err, ERRB_TIME);
+  if (threadIdx.x == 0) {  // the step's stage brackets were computed once by k_step_begin
+    for (int k = 0; k < 3; ++k) {
+      sh[k].k = ctrl->stage_k[k];
+      sh[k].w = ctrl->stage_w[k];
+      sh[k].ok = 1;
+    }
+    sh_step = a.use_ctrl_step ? ctrl->step : a.step0;
+    sh_skip = ctrl->halt != 0 || !ctrl->stage_ok;
     sh_e = b.block_ens[blockIdx.x];
     sh_ens = b.ens[sh_e];
   }
@@ -221,7 +219,7 @@ void launch_bbox(const Bufs& b, Ctrl* ctrl, bool use_status, cudaStream_t st) {
 
 // Per-step bookkeeping: reset the per-step counters and the ensemble boxes (start), advance the
 // device step counter (end).
-__global__ void k_step_begin(Bufs b, Ctrl* ctrl) {
+__global__ void k_step_begin(Bufs b, FieldView f, StepArgs a, int bracket, Ctrl* ctrl) {
   if (ctrl->halt) return;
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   for (uint32_t e = t; e < b.n_ens; e += gridDim.x * blockDim.x) {
@@ -240,6 +238,20 @@ __global__ void k_step_begin(Bufs b, Ctrl* ctrl) {
     ctrl->n_long = 0;
     ctrl->ovf_used = 0;
     ctrl->census[0] = ctrl->census[1] = ctrl->census[2] = ctrl->census[3] = 0;
+    if (bracket) {  // float64 time arithmetic once per step, not once per advection block
+      const uint32_t step = a.use_ctrl_step ? ctrl->step : a.step0;
+      const double t0 = a.t_start + (double)(int)(step - a.step0) * a.dt;
+      const double ts[3] = {t0, t0 + 0.5 * a.dt, t0 + a.dt};
+      int ok = 1;
+      for (int k = 0; k < 3; ++k) {
+        const Stage sg = stage_at(f, ts[k]);
+        ctrl->stage_k[k] = sg.k;
+        ctrl->stage_w[k] = sg.w;
+        ok = ok && sg.ok;
+      }
+      ctrl->stage_ok = ok;
+      if (!ok) atomicOr(&ctrl->err, (uint32_t)ERRB_TIME);
+    }
   }
 }
 
@@ -248,15 +260,18 @@ __global__ void k_step_end(Ctrl* ctrl, int interact) {
   if (interact) {
     ctrl->pairs_total += ctrl->n_dir / 2;
     ctrl->steps_total += 1;
+    ctrl->rounds_total += ctrl->rounds;
   }
   ctrl->step += 1;
 }
 
-void launch_step_begin(const Bufs& b, Ctrl* ctrl, cudaStream_t st) {
+void launch_step_begin(const Bufs& b, const FieldView* f, const StepArgs& a, Ctrl* ctrl, cudaStream_t st) {
   int grid = (int)((b.n_ens + 255) / 256);
   if (grid < 1) grid = 1;
   if (grid > 64) grid = 64;
-  k_step_begin<<<grid, 256, 0, st>>>(b, ctrl);
+  FieldView fv{};
+  if (f) fv = *f;
+  k_step_begin<<<grid, 256, 0, st>>>(b, fv, a, f ? 1 : 0, ctrl);
 }
 void launch_step_end(Ctrl* ctrl, bool interact, cudaStream_t st) { k_step_end<<<1, 1, 0, st>>>(ctrl, interact ? 1 : 0); }
 

@@ -21,15 +21,17 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
   return m;
 }
 
-// Cells of one ensemble's grid at cell size c (1 for an empty ensemble).
-__device__ __forceinline__ double grid_dims(const uint32_t* box, double c, double* ncx, double* ncy) {
+// Cells of one ensemble's grid at cell size c (1 for an empty ensemble). Float32 throughout: the
+// grid only has to be consistent within the step (any c >= r gives the same pairs), and float64 is
+// slow on this GPU.
+__device__ __forceinline__ float grid_dims(const uint32_t* box, float c, float* ncx, float* ncy) {
   const float mnx = dec_f(box[0]), mny = dec_f(box[1]), mxx = dec_f(box[2]), mxy = dec_f(box[3]);
   if (!(mnx <= mxx && mny <= mxy)) {
-    *ncx = *ncy = 1.0;
-    return 1.0;
+    *ncx = *ncy = 1.f;
+    return 1.f;
   }
-  *ncx = floor(((double)mxx - (double)mnx) / c) + 3.0;
-  *ncy = floor(((double)mxy - (double)mny) / c) + 3.0;
+  *ncx = floorf((mxx - mnx) / c) + 3.f;
+  *ncy = floorf((mxy - mny) / c) + 3.f;
   return *ncx * *ncy;
 }
 
@@ -37,74 +39,80 @@ __device__ __forceinline__ double grid_dims(const uint32_t* box, double c, doubl
 // exceed the capacity, the cell size grows (pairs stay exact because only c >= r matters).
 __global__ void __launch_bounds__(GRID_THREADS) k_grid(Bufs b, PairParams pp, Ctrl* ctrl) {
   if (ctrl->halt) return;
-  __shared__ double ws[GRID_THREADS / 32];
-  __shared__ double total_sh;
+  __shared__ float ws[GRID_THREADS / 32];
+  __shared__ float total_sh;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  double c = (double)pp.cell_factor * pp.r;
-  if (!(c > 0.0)) c = 1e-3;
+  float c = pp.cell_factor * (float)pp.r;
+  if (!(c > 0.f)) c = 1e-3f;
+  const float cap = (float)b.cells_cap;
   // 1. cell size: total cells over all ensembles must fit the capacity
   for (int attempt = 0; attempt < 16; ++attempt) {
-    double t = 0;
+    float t = 0.f;
     for (uint32_t e = threadIdx.x; e < b.n_ens; e += GRID_THREADS) {
-      double nx, ny;
+      float nx, ny;
       t += grid_dims(b.ebox + 4 * e, c, &nx, &ny);
     }
     for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
     if (lane == 0) ws[wid] = t;
     __syncthreads();
     if (threadIdx.x == 0) {
-      double s = 0;
-      for (int w = 0; w < GRID_THREADS / 32; ++w) s += ws[w];
-      total_sh = s;
+      float sum = 0.f;
+      for (int w = 0; w < GRID_THREADS / 32; ++w) sum += ws[w];
+      total_sh = sum;
     }
     __syncthreads();
-    const double total = total_sh;
+    const float total = total_sh;
     __syncthreads();
-    if (total <= (double)b.cells_cap) break;
-    c = c * sqrt(total / (double)b.cells_cap) * 1.02;
+    if (total <= cap * 0.999f) break;  // margin for float rounding of the sum
+    c = c * sqrtf(total / cap) * 1.02f;
   }
-  // 2. per-ensemble geometry and exclusive cell offsets
-  __shared__ double carry_sh;
-  if (threadIdx.x == 0) carry_sh = 0;
+  // 2. per-ensemble geometry and exclusive cell offsets (integers, exact)
+  __shared__ uint32_t wsi[GRID_THREADS / 32];
+  __shared__ unsigned long long carry;
+  if (threadIdx.x == 0) carry = 0;
   __syncthreads();
   for (uint32_t e0 = 0; e0 < b.n_ens; e0 += GRID_THREADS) {
     const uint32_t e = e0 + threadIdx.x;
-    double nx = 0, ny = 0, cells = 0;
-    if (e < b.n_ens) cells = grid_dims(b.ebox + 4 * e, c, &nx, &ny);
-    double y = cells;
+    float nx = 0.f, ny = 0.f;
+    uint32_t cells = 0;
+    if (e < b.n_ens) {
+      grid_dims(b.ebox + 4 * e, c, &nx, &ny);
+      cells = (uint32_t)fminf(nx * ny, 4.0e9f);
+    }
+    uint32_t y = cells;
     for (int o = 1; o < 32; o <<= 1) {
-      const double t = __shfl_up_sync(0xffffffffu, y, o);
+      const uint32_t t = __shfl_up_sync(0xffffffffu, y, o);
       if (lane >= o) y += t;
     }
-    if (lane == 31) ws[wid] = y;
+    if (lane == 31) wsi[wid] = y;
     __syncthreads();
-    double wp = 0, tot = 0;
+    unsigned long long wp = 0, tot = 0;
     for (int w = 0; w < GRID_THREADS / 32; ++w) {
-      if (w < wid) wp += ws[w];
-      tot += ws[w];
+      if (w < wid) wp += wsi[w];
+      tot += wsi[w];
     }
-    const double base = carry_sh + wp + y - cells;
+    const unsigned long long base = carry + wp + y - cells;
     if (e < b.n_ens) {
       EnsGrid g;
       const uint32_t* box = b.ebox + 4 * e;
       const bool empty = !(dec_f(box[0]) <= dec_f(box[2]));
-      g.c = (float)c;
-      g.inv_c = (float)(1.0 / c);
-      g.x0 = empty ? 0.f : (float)((double)dec_f(box[0]) - c);
-      g.y0 = empty ? 0.f : (float)((double)dec_f(box[1]) - c);
-      g.ncx = (int)fmin(nx, 2147483647.0);
-      g.ncy = (int)fmin(ny, 2147483647.0);
-      g.cell_base = (uint32_t)fmin(base, 4294967295.0);
+      g.c = c;
+      g.inv_c = 1.f / c;
+      g.x0 = empty ? 0.f : dec_f(box[0]) - c;
+      g.y0 = empty ? 0.f : dec_f(box[1]) - c;
+      g.ncx = (int)nx;
+      g.ncy = (int)ny;
+      g.cell_base = (uint32_t)(base > 0xffffffffull ? 0xffffffffull : base);
       g.pad = 0;
       b.grids[e] = g;
     }
     __syncthreads();
-    if (threadIdx.x == 0) carry_sh += tot;
+    if (threadIdx.x == 0) carry += tot;
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    const double total = carry_sh;
-    if (total > (double)b.cells_cap) {  // cannot happen unless ensembles vastly outnumber cells
+    const unsigned long long total = carry;
+    if (total > b.cells_cap) {  // only when ensembles vastly outnumber the capacity
       ctrl->ncells = b.cells_cap;
       ctrl->halt = 1;
       ctrl->halt_step = ctrl->step;

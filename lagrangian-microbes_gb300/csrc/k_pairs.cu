@@ -11,12 +11,12 @@
 // One thread per particle (cell order) scans the three rows of its 3x3 cell neighbourhood; the
 // three cells of a row are consecutive keys, hence one contiguous run of the sorted array. Each
 // neighbour list is kept sorted by descending pair priority, the order in which the interaction
-// applies pairs: lists of up to SLAB entries are built by insertion in registers and stored in
+// applies pairs: lists of up to SLAB entries are gathered in registers, sorted by a sorting network and stored in
 // the per-vertex slab; longer lists are rebuilt by a second kernel into a per-step overflow
 // area (allocated with an atomic cursor, regrown by the host on overflow) and sorted there.
 //
 // Pair priority: the pair's colour (a 2x2 checkerboard of cells of size r, taken at the pair's
-// midpoint) first, then a 64-bit Philox hash of (seed, step, i, j). Two pairs sharing a microbe
+// midpoint) first, then a 62-bit order hash of (seed, step, i, j). Two pairs sharing a microbe
 // have midpoints at most r apart per coordinate, so they sit in the same or in adjacent cells,
 // and same-colour pairs of different cells never conflict: the longest chain of conflicting
 // pairs is bounded by 4 x the longest chain inside one cell. Any fixed order is a valid choice
@@ -57,10 +57,10 @@ __device__ __forceinline__ uint32_t floor_parity(float v) {
 
 __device__ __forceinline__ unsigned long long pair_prio(uint32_t i, uint32_t j, uint32_t step, uint32_t k0,
                                                         uint32_t k1, float2 a, float2 b, float inv2r) {
-  const PairDraw d = pair_draw(i, j, step, k0, k1);
+  const unsigned long long h = order_hash(i, j, step, ((unsigned long long)k1 << 32) | k0);
   const float mx = __fadd_rn(a.x, b.x), my = __fadd_rn(a.y, b.y);  // twice the midpoint (commutative)
   const uint32_t color = floor_parity(__fmul_rn(mx, inv2r)) | (floor_parity(__fmul_rn(my, inv2r)) << 1);
-  return ((unsigned long long)(3u - color) << 62) | (d.prio >> 2);
+  return ((unsigned long long)(3u - color) << 62) | (h >> 2);
 }
 
 // a before b: higher priority first, ties by lower partner id (one global order on pairs).
@@ -141,23 +141,12 @@ __global__ void __launch_bounds__(SLOT_BLOCK) k_sweep(Bufs b, PairParams pp, Ste
       pl[k] = NONE;
     }
     for_neighbours(b, pp, v, [&](uint32_t t) {
-      if (m < SLAB) {
+      if (m < SLAB) {  // append in registers (compile-time slots, predicated)
         const uint32_t lb = b.sid[t] - v.base;
         const unsigned long long p = pair_prio(min(la, lb), max(la, lb), step, k0, k1, v.ps, b.spos[t], pp.inv2r);
-        uint32_t pos = 0;
-#pragma unroll
-        for (int k = 0; k < (int)SLAB; ++k) pos += ((uint32_t)k < m && before(pr[k], pl[k], p, lb)) ? 1u : 0u;
-#pragma unroll
-        for (int k = (int)SLAB - 1; k >= 1; --k) {
-          if ((uint32_t)k <= m && (uint32_t)k > pos) {
-            pr[k] = pr[k - 1];
-            nb[k] = nb[k - 1];
-            pl[k] = pl[k - 1];
-          }
-        }
 #pragma unroll
         for (int k = 0; k < (int)SLAB; ++k) {
-          if ((uint32_t)k == pos) {
+          if ((uint32_t)k == m) {
             pr[k] = p;
             nb[k] = t;
             pl[k] = lb;
@@ -166,18 +155,32 @@ __global__ void __launch_bounds__(SLOT_BLOCK) k_sweep(Bufs b, PairParams pp, Ste
       }
       ++m;
     });
+    if (m > 1 && m <= SLAB) {
+      // 19-comparator sorting network for 8 entries; empty slots (priority 0, partner NONE) sort last
+#define LM_CX(x, y)                                         \
+  if (before(pr[y], pl[y], pr[x], pl[x])) {                  \
+    const unsigned long long tp = pr[x]; pr[x] = pr[y]; pr[y] = tp; \
+    const uint32_t tn = nb[x]; nb[x] = nb[y]; nb[y] = tn;    \
+    const uint32_t tl = pl[x]; pl[x] = pl[y]; pl[y] = tl;    \
+  }
+      LM_CX(0, 2) LM_CX(1, 3) LM_CX(4, 6) LM_CX(5, 7)
+      LM_CX(0, 4) LM_CX(1, 5) LM_CX(2, 6) LM_CX(3, 7)
+      LM_CX(0, 1) LM_CX(2, 3) LM_CX(4, 5) LM_CX(6, 7)
+      LM_CX(2, 4) LM_CX(3, 5) LM_CX(1, 4) LM_CX(3, 6)
+      LM_CX(1, 2) LM_CX(3, 4) LM_CX(5, 6)
+#undef LM_CX
+    }
     b.deg[s] = m;
-    b.head[s] = 0;
     b.level[s] = 0;
     if (m <= SLAB) {
 #pragma unroll
       for (int k = 0; k < (int)SLAB; ++k)
         if ((uint32_t)k < m) b.slab[(size_t)s * SLAB + k] = nb[k];
-      b.want[s] = m ? nb[0] : NONE;
+      b.wstate[s] = pack_state(m ? nb[0] : NONE, 0u, b.species[b.sid[s]]);  // entry 0 of the list
       active = m > 0;
     } else {
       is_long = true;
-      b.want[s] = NONE;  // set by k_sweep_long
+      b.wstate[s] = pack_state(NONE, 0u, b.species[b.sid[s]]);  // set by k_sweep_long
     }
   }
   append_active(b, ctrl, active, s);
@@ -271,7 +274,11 @@ __global__ void __launch_bounds__(SLOT_BLOCK) k_sweep_long(Bufs b, PairParams pp
       s = b.longv[x];
       const uint32_t d = b.deg[s];
       const unsigned long long o = atomicAdd(&ctrl->ovf_used, (unsigned long long)d);
-      if (o + d > ctrl->ovf_cap) {  // the host regrows the overflow area and re-runs the step
+      if (d > MAX_DEGREE) {  // list positions no longer fit the state word
+        ctrl->halt = 1;
+        ctrl->halt_step = ctrl->step;
+        atomicOr(&ctrl->err, (uint32_t)ERRB_ROUNDCAP);
+      } else if (o + d > ctrl->ovf_cap) {  // the host regrows the overflow area and re-runs the step
         ctrl->halt = 1;
         ctrl->halt_step = ctrl->step;
         atomicOr(&ctrl->err, (uint32_t)ERRB_OVERFLOW);
@@ -291,7 +298,7 @@ __global__ void __launch_bounds__(SLOT_BLOCK) k_sweep_long(Bufs b, PairParams pp
         });
         sort_segment(b.oprio + o, b.ovf + o, b.sid, d);
         b.off[s] = (uint32_t)o;
-        b.want[s] = b.ovf[o];
+        b.wstate[s] = pack_state(b.ovf[o], 0u, b.species[b.sid[s]]);  // entry 0 of the list
         active = true;
       }
     }

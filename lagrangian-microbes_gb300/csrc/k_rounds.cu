@@ -15,17 +15,18 @@
 // r < p is evaluated exactly as the integer test u53 < ceil(p * 2^53).
 //
 // All pairs are applied by one persistent cooperative launch without grid barriers. Each vertex v
-// publishes want[v], the partner of its highest-priority unprocessed pair (NONE when it has none).
-// A pair (v, u) is ready exactly when want[v] == u and want[u] == v; the thread that polls the
-// lower endpoint applies it and advances both heads. Only the applier of a vertex's current head
-// pair ever writes that vertex's head/want, so every write has a single owner. Species and head
-// writes are released before the want words that hand the vertices on; pollers read want with
-// acquire loads. The globally highest-priority pending pair is always ready, so the loop always
-// progresses; every wait is still bounded (error flag + return after a timeout).
+// publishes the partner of its highest-priority unprocessed pair (NONE when it has none). A pair
+// (v, u) is ready exactly when each names the other; the thread that polls the
+// lower endpoint applies it and advances both. The current species, the list position and the
+// partner of a vertex share one 64-bit state word, so one load tells a poller everything and the
+// handoff needs no memory fence. Only the applier of a vertex's current pair ever writes that
+// vertex's word, so every write has a single owner. The globally highest-priority pending pair is
+// always ready, so the loop always progresses; every wait is still bounded (error flag + return
+// after a timeout).
 //
-// Each applied pair gets a level = 1 + max(level of the previous pair at either endpoint): pairs of
-// one level share no microbe, and (level, i, j) is a deterministic sequential order equal in
-// effect to the priority order. The pair log records it; the step's "rounds" is the max level.
+// In pair-log runs each applied pair also gets a level = 1 + max(level of the previous pair at
+// either endpoint): pairs of one level share no microbe, and (level, i, j) is a deterministic
+// sequential order equal in effect to the priority order. The step's "rounds" is the max level.
 #include "lm_internal.h"
 #include "lm_philox.cuh"
 
@@ -40,14 +41,17 @@ __device__ __forceinline__ unsigned long long globaltimer() {
   return t;
 }
 
-__device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
-  uint32_t v;
-  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+// Vertex state words are read and written with relaxed .gpu operations: each word is the only
+// shared state a pair needs, and a word changes only through the applier of its vertex's current
+// pair, so coherence of the single word is all the ordering required.
+__device__ __forceinline__ unsigned long long ld_relaxed(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
   return v;
 }
 
-__device__ __forceinline__ void st_release(uint32_t* p, uint32_t v) {
-  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+__device__ __forceinline__ void st_relaxed(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
 __device__ __forceinline__ bool beats(int x, int y) {
@@ -55,20 +59,28 @@ __device__ __forceinline__ bool beats(int x, int y) {
   return (x == 1 && y == 3) || (x == 2 && y == 1) || (x == 3 && y == 2);
 }
 
-// Partner of vertex s at list position h (NONE past the end).
+// Partner of vertex s at list position h (NONE past the end); lists are read-only here.
 __device__ __forceinline__ uint32_t next_partner(const Bufs& b, uint32_t s, uint32_t h) {
   const uint32_t d = b.deg[s];
   if (h >= d) return NONE;
   return d <= SLAB ? b.slab[(size_t)s * SLAB + h] : b.ovf[(size_t)b.off[s] + h];
 }
 
-// Apply pair (s, u), s < u in cell order, both heads pointing at it; returns its level.
-__device__ __forceinline__ uint32_t apply_pair(const Bufs& b, uint32_t step, uint32_t s, uint32_t u, Ctrl* ctrl) {
-  const EnsInfo& info = b.ens[b.sens[s]];
+// Apply pair (s, u), s < u in cell order, whose state words ws, wu name each other. Everything
+// the pair needs that other threads write (both species, both list positions) is inside the two
+// words, so no fence is needed: the next applier of either vertex reads the words this one
+// stores. Returns the pair's level when levels are tracked (pair-log runs), else 0.
+__device__ __forceinline__ uint32_t apply_pair(const Bufs& b, uint32_t step, uint32_t s, uint32_t u,
+                                               unsigned long long ws, unsigned long long wu, Ctrl* ctrl) {
+  const uint32_t hs = state_pos(ws), hu = state_pos(wu);
+  const uint32_t ns = next_partner(b, s, hs + 1u), nu = next_partner(b, u, hu + 1u);
   const uint32_t pa = b.sid[s], pb = b.sid[u];
-  const uint32_t pi = min(pa, pb), pj = max(pa, pb);  // slots; local ids are slot - base
-  const int si = __ldcg(b.species + pi), sj = __ldcg(b.species + pj);
+  const bool s_is_i = pa < pb;  // i < j are the pair's slots (local ids are slot - base)
+  const uint32_t pi = s_is_i ? pa : pb, pj = s_is_i ? pb : pa;
+  const int si = state_species(s_is_i ? ws : wu), sj = state_species(s_is_i ? wu : ws);
+  int ni = si, nj = sj;
   if (si != sj) {
+    const EnsInfo& info = b.ens[b.sens[s]];
     unsigned long long t = 0;
     bool valid = true;
     if ((si == 1 && sj == 3) || (si == 3 && sj == 1)) t = info.t_rs;
@@ -78,33 +90,34 @@ __device__ __forceinline__ uint32_t apply_pair(const Bufs& b, uint32_t step, uin
     if (valid) {
       const PairDraw d = pair_draw(pi - info.base, pj - info.base, step, info.seed_lo, info.seed_hi);
       const bool fwd_wins = d.u53 < t;
-      const bool i_wins = (beats(si, sj) == fwd_wins);  // i is the cyclic winner and won, or lost and won anyway
-      if (i_wins) __stcg(b.species + pj, (int8_t)si);
-      else __stcg(b.species + pi, (int8_t)sj);
+      if (beats(si, sj) == fwd_wins) nj = si;  // i wins: j takes i's species
+      else ni = sj;                            // j wins
     }
   }
-  const uint32_t level = max(__ldcg(b.level + s), __ldcg(b.level + u)) + 1u;
-  __stcg(b.level + s, level);
-  __stcg(b.level + u, level);
-  if (b.plog) {
+  const int new_s = s_is_i ? ni : nj, new_u = s_is_i ? nj : ni;
+  uint32_t level = 0;
+  if (b.plog) {  // pair-log runs: levels live outside the state words, so order them with fences
+    __threadfence();
+    level = max(__ldcg(b.level + s), __ldcg(b.level + u)) + 1u;
+    __stcg(b.level + s, level);
+    __stcg(b.level + u, level);
     const uint32_t k = atomicAdd(&ctrl->plog_n, 1u);
     if (k < b.plog_cap) {
       b.plog[3 * k + 0] = pi;
       b.plog[3 * k + 1] = pj;
       b.plog[3 * k + 2] = level - 1u;
     }
+    __threadfence();
   }
-  // hand both vertices on to their next pair
-  const uint32_t hu = __ldcg(b.head + u) + 1u, hs = __ldcg(b.head + s) + 1u;
-  __stcg(b.head + u, hu);
-  __stcg(b.head + s, hs);
-  const uint32_t nu = next_partner(b, u, hu);
-  const uint32_t ns = next_partner(b, s, hs);
-  __threadfence();
-  st_release(b.want + u, nu);
-  st_release(b.want + s, ns);
+  // a vertex whose list is done keeps its final species in the species array
+  if (nu == NONE) b.species[pb] = (int8_t)new_u;
+  if (ns == NONE) b.species[pa] = (int8_t)new_s;
+  st_relaxed(b.wstate + u, pack_state(nu, hu + 1u, new_u));
+  st_relaxed(b.wstate + s, pack_state(ns, hs + 1u, new_s));
   return level;
 }
+
+constexpr int POLL_BATCH = 4;  // vertices whose state words one thread loads before testing them
 
 __global__ void __launch_bounds__(RD_THREADS) k_rounds(Bufs b, StepArgs a, Ctrl* ctrl) {
   if (((volatile uint32_t*)&ctrl->halt)[0]) return;
@@ -118,12 +131,30 @@ __global__ void __launch_bounds__(RD_THREADS) k_rounds(Bufs b, StepArgs a, Ctrl*
   uint32_t polls = 0;
   while (pending) {
     pending = false;
-    for (uint32_t x = first; x < cnt; x += stride) {
-      const uint32_t s = b.act[x];
-      const uint32_t u = ld_acquire(b.want + s);
-      if (u == NONE) continue;
-      pending = true;
-      if (s < u && ld_acquire(b.want + u) == s) max_level = max(max_level, apply_pair(b, step, s, u, ctrl));
+    for (uint32_t x0 = first; x0 < cnt; x0 += POLL_BATCH * stride) {
+      uint32_t sv[POLL_BATCH];
+      unsigned long long ws[POLL_BATCH], wu[POLL_BATCH];
+#pragma unroll
+      for (int k = 0; k < POLL_BATCH; ++k) {
+        const uint32_t x = x0 + (uint32_t)k * stride;
+        sv[k] = x < cnt ? b.act[x] : NONE;
+        ws[k] = sv[k] != NONE ? ld_relaxed(b.wstate + sv[k]) : (unsigned long long)NONE;
+      }
+#pragma unroll
+      for (int k = 0; k < POLL_BATCH; ++k) {
+        const uint32_t u = state_partner(ws[k]);
+        wu[k] = NONE;
+        if (u != NONE) {
+          pending = true;
+          if (sv[k] < u) wu[k] = ld_relaxed(b.wstate + u);
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < POLL_BATCH; ++k) {
+        const uint32_t u = state_partner(ws[k]);
+        if (u != NONE && sv[k] < u && state_partner(wu[k]) == sv[k])
+          max_level = max(max_level, apply_pair(b, step, sv[k], u, ws[k], wu[k], ctrl));
+      }
     }
     if (pending && ((++polls & 63u) == 0u) && globaltimer() - t0 > ROUNDS_TIMEOUT_NS) {
       atomicOr(&ctrl->err, (uint32_t)ERRB_TIMEOUT);

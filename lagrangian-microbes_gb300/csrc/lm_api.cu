@@ -62,7 +62,8 @@ struct lm_ctx {
   int8_t* species = nullptr;
   uint8_t* status = nullptr;
   uint32_t *key = nullptr, *rank = nullptr, *sid = nullptr, *skey = nullptr, *sens = nullptr, *deg = nullptr;
-  uint32_t *slab = nullptr, *off = nullptr, *longv = nullptr, *want = nullptr, *head = nullptr, *level = nullptr;
+  uint32_t *slab = nullptr, *off = nullptr, *longv = nullptr, *level = nullptr;
+  unsigned long long* wstate = nullptr;
   uint32_t* act = nullptr;
   float2* spos = nullptr;
   float *rlon = nullptr, *rlat = nullptr;  // caller-order staging (E > 1)
@@ -247,7 +248,7 @@ int ensure_slots(lm_ctx* c, uint32_t slots, uint32_t n_ens) {
         (r = dalloc(c, &c->key, cap)) || (r = dalloc(c, &c->rank, cap)) || (r = dalloc(c, &c->sid, cap)) ||
         (r = dalloc(c, &c->skey, cap)) || (r = dalloc(c, &c->sens, cap)) || (r = dalloc(c, &c->deg, cap)) ||
         (r = dalloc(c, &c->slab, (size_t)cap * SLAB)) || (r = dalloc(c, &c->off, cap)) ||
-        (r = dalloc(c, &c->longv, cap)) || (r = dalloc(c, &c->want, cap)) || (r = dalloc(c, &c->head, cap)) ||
+        (r = dalloc(c, &c->longv, cap)) || (r = dalloc(c, &c->wstate, cap)) ||
         (r = dalloc(c, &c->level, cap)) || (r = dalloc(c, &c->act, cap)) || (r = dalloc(c, &c->spos, cap)) ||
         (r = dalloc(c, &c->rlon, cap)) || (r = dalloc(c, &c->rlat, cap)) || (r = dalloc(c, &c->rsp, cap)) ||
         (r = dalloc(c, &c->map_d, cap)) || (r = dalloc(c, &c->block_ens, nblk)))
@@ -364,8 +365,7 @@ Bufs bufs(const lm_ctx* c, bool log) {
   b.ovf = c->ovf;
   b.oprio = c->oprio;
   b.longv = c->longv;
-  b.want = c->want;
-  b.head = c->head;
+  b.wstate = c->wstate;
   b.level = c->level;
   b.act = c->act;
   b.census = c->census;
@@ -419,6 +419,10 @@ int consume_errors(lm_ctx* c) {
 int regrow(lm_ctx* c) {
   int r;
   const Ctrl& h = *c->hctrl;
+  if (h.err & ERRB_ROUNDCAP) {
+    write_err(c, 0u, 0u);
+    return fail(c, LM_ERR_ROUND_CAP, "a microbe has more than %u neighbours", MAX_DEGREE);
+  }
   if (h.ovf_used > c->ovf_cap) {
     size_t need = (size_t)h.ovf_used;
     if ((r = set_ovf_capacity(c, std::max(need + need / 4 + 4096, c->ovf_cap * 2)))) return r;
@@ -463,7 +467,7 @@ cudaError_t enqueue_interaction(lm_ctx* c, const StepArgs& a, uint32_t flags, bo
 // One fused step; `advect` false re-runs only the interaction part of an advected step.
 cudaError_t enqueue_step(lm_ctx* c, const StepArgs& a, uint32_t flags, bool advect) {
   const Bufs b = bufs(c, false);
-  PROF(c, P_BOOKKEEPING, launch_step_begin(b, c->ctrl, c->st));
+  PROF(c, P_BOOKKEEPING, launch_step_begin(b, advect ? &c->fv : nullptr, a, c->ctrl, c->st));
   if (advect) PROF(c, P_ADVECT, launch_advect(c->fv, a, b, c->ctrl, c->st));
   if (flags & LM_STEP_INTERACT) {
     cudaError_t e = enqueue_interaction(c, a, flags, !advect, true);
@@ -676,7 +680,7 @@ int lm_ctx_destroy(lm_ctx* c) {
   if (c->graph) cudaGraphDestroy(c->graph);
   void* bufs_[] = {c->uv,     c->xo,    c->yo,     c->plon,   c->plat,   c->species, c->status, c->key,
                    c->rank,   c->sid,   c->skey,   c->sens,   c->deg,    c->slab,    c->off,    c->longv,
-                   c->want,   c->head,  c->level,  c->act,    c->spos,   c->rlon,    c->rlat,   c->rsp,
+                   c->wstate, c->level,  c->act,    c->spos,   c->rlon,    c->rlat,   c->rsp,
                    c->map_d,  c->block_ens, c->ens_d, c->grids, c->ebox, c->census,  c->ccount, c->cstart,
                    c->csum,   c->ovf,   c->oprio,  c->ctrl,   c->plog};
   for (void* p : bufs_)
@@ -943,7 +947,7 @@ int lm_query_pairs(lm_ctx* c, int64_t n, const float* lon, const float* lat, int
   c->has_particles = false;  // positions now hold query points, not an advected state
   const StepArgs a = step_args(0.0, 1.0, 0, 0.0, false);
   for (;;) {
-    PROF(c, P_BOOKKEEPING, launch_step_begin(bufs(c, false), c->ctrl, c->st));
+    PROF(c, P_BOOKKEEPING, launch_step_begin(bufs(c, false), nullptr, a, c->ctrl, c->st));
     CK(enqueue_interaction(c, a, 0u, true, false));
     if ((r = read_ctrl(c))) return r;
     if (c->hctrl->halt) {
@@ -1002,7 +1006,7 @@ int lm_interact(lm_ctx* c, int64_t n, const float* lon, const float* lat, int64_
   const StepArgs a = step_args(0.0, 1.0, step_index, 0.0, false);
   const Bufs b = bufs(c, false);
   for (;;) {
-    PROF(c, P_BOOKKEEPING, launch_step_begin(b, c->ctrl, c->st));
+    PROF(c, P_BOOKKEEPING, launch_step_begin(b, nullptr, a, c->ctrl, c->st));
     CK(enqueue_interaction(c, a, flags | LM_STEP_INTERACT, true, false));
     if (flags & LM_STEP_CENSUS) PROF(c, P_CENSUS, launch_census(b, c->ctrl, c->st));
     PROF(c, P_BOOKKEEPING, launch_step_end(c->ctrl, true, c->st));
@@ -1130,6 +1134,7 @@ int lm_stats_get(lm_ctx* c, lm_stats* out) {
   out->cells = h.ncells;
   out->long_lists = h.n_long;
   out->n_ensembles = c->n_ens;
+  out->rounds_total = (int64_t)h.rounds_total;
   return LM_OK;
 }
 
@@ -1141,6 +1146,7 @@ int lm_stats_reset(lm_ctx* c) {
   CK(cudaMemcpyAsync(&c->ctrl->max_rounds, &zero, sizeof(zero), cudaMemcpyHostToDevice, c->st));
   CK(cudaMemcpyAsync(&c->ctrl->pairs_total, &z64, sizeof(z64), cudaMemcpyHostToDevice, c->st));
   CK(cudaMemcpyAsync(&c->ctrl->steps_total, &z64, sizeof(z64), cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(&c->ctrl->rounds_total, &z64, sizeof(z64), cudaMemcpyHostToDevice, c->st));
   CK(cudaStreamSynchronize(c->st));
   return LM_OK;
 }

@@ -15,7 +15,8 @@
 //              uint32 sid[S], skey[S], sens[S]; float2 spos[S]  (particles in cell order)
 //              uint32 deg[S], slab[S][SLAB]     (neighbour lists up to SLAB, sorted by priority)
 //              uint32 off[S], ovf[cap]; uint64 oprio[cap]  (longer lists, allocated per step)
-//              uint32 want[S], head[S], level[S], act[S]   (interaction dataflow)
+//              uint64 wstate[S] = species << 56 | list position << 32 | partner;
+//              uint32 level[S] (pair-log runs only), act[S]   (interaction dataflow)
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -26,13 +27,23 @@ constexpr uint32_t NONE = 0xffffffffu;
 constexpr uint32_t SLOT_BLOCK = 256;   // threads per block of every per-slot kernel
 constexpr uint32_t SLAB = 8;           // neighbour-list entries kept in the per-vertex slab
 constexpr uint8_t STATUS_OK = 0, STATUS_OOB = 1, STATUS_NAN = 2, STATUS_PAD = 3;
+constexpr uint32_t MAX_DEGREE = (1u << 24) - 1;  // list positions take 24 bits of the state word
+
+// Interaction state word of a vertex: its current species, the position of its current pair in
+// its list, and that pair's partner (NONE once the list is done).
+__host__ __device__ inline unsigned long long pack_state(uint32_t partner, uint32_t pos, int species) {
+  return ((unsigned long long)(uint8_t)species << 56) | ((unsigned long long)(pos & MAX_DEGREE) << 32) | partner;
+}
+__host__ __device__ inline uint32_t state_partner(unsigned long long w) { return (uint32_t)w; }
+__host__ __device__ inline uint32_t state_pos(unsigned long long w) { return (uint32_t)(w >> 32) & MAX_DEGREE; }
+__host__ __device__ inline int state_species(unsigned long long w) { return (int)(int8_t)(uint8_t)(w >> 56); }
 
 // Sticky error bits in Ctrl::err (mirrored by the LM_ERR_* status codes of lm_api.h).
 enum : uint32_t {
   ERRB_OOB = 1u << 0,        // a particle left the field domain (frozen, excluded from pairing)
   ERRB_NAN = 1u << 1,        // a non-finite position or velocity
   ERRB_OVERFLOW = 1u << 2,   // long-list capacity exceeded (step halted)
-  ERRB_ROUNDCAP = 1u << 3,   // reserved
+  ERRB_ROUNDCAP = 1u << 3,   // a microbe has more than MAX_DEGREE neighbours (step halted)
   ERRB_TIMEOUT = 1u << 4,    // a bounded device wait gave up
   ERRB_TIME = 1u << 5,       // a stage time fell outside the field's time axis
 };
@@ -57,7 +68,11 @@ struct Ctrl {
   uint32_t plog_n;              // pair-log entries written this step
   uint32_t act_n;               // active vertices (with at least one pair)
   uint32_t census[4];           // species counts after the step, all ensembles ([0] = other values)
-  uint32_t pad[2];
+  unsigned long long rounds_total;  // sum of per-step levels since the last reset
+  int stage_k[3];               // frame brackets of this step's stage times t, t+dt/2, t+dt
+  float stage_w[3];
+  int stage_ok;                 // 0 when a stage time left the field's time axis
+  uint32_t pad2;
 };
 
 // Per-ensemble constants (device array, one entry per ensemble).
@@ -137,8 +152,7 @@ struct Bufs {
   uint32_t* ovf;
   unsigned long long* oprio;
   uint32_t* longv;    // vertices with lists longer than SLAB
-  uint32_t* want;
-  uint32_t* head;
+  unsigned long long* wstate;  // per vertex: species << 56 | current list position << 32 | partner
   uint32_t* level;
   uint32_t* act;
   uint32_t* census;   // [E][4]
@@ -148,7 +162,8 @@ struct Bufs {
 
 // ---- launchers (each enqueues on `st`) ----
 void launch_interleave(const float* u, const float* v, float2* uv, size_t n, cudaStream_t st);
-void launch_step_begin(const Bufs& b, Ctrl* ctrl, cudaStream_t st);
+// step_begin also brackets the stage times of the step in the field's frames when `f` is given.
+void launch_step_begin(const Bufs& b, const FieldView* f, const StepArgs& a, Ctrl* ctrl, cudaStream_t st);
 void launch_step_end(Ctrl* ctrl, bool interact, cudaStream_t st);
 void launch_advect(const FieldView& f, const StepArgs& a, const Bufs& b, Ctrl* ctrl, cudaStream_t st);
 void launch_bbox(const Bufs& b, Ctrl* ctrl, bool use_status, cudaStream_t st);

@@ -38,17 +38,28 @@ __host__ __device__ __forceinline__ U4 philox4x32_10(U4 c, uint32_t k0, uint32_t
 }
 
 // One Philox block per unordered pair (i < j) at step `step`:
-//   u53  = 53-bit uniform integer; the reference's r = np.random.rand() becomes u53 * 2^-53
-//   prio = 64-bit priority that fixes the pair's place in the sequential application order
-struct PairDraw { unsigned long long u53, prio; };
+//   u53 = 53-bit uniform integer; the reference's r = np.random.rand() becomes u53 * 2^-53
+struct PairDraw { unsigned long long u53; };
 
 __host__ __device__ __forceinline__ PairDraw pair_draw(uint32_t i, uint32_t j, uint32_t step, uint32_t k0,
                                                        uint32_t k1) {
   U4 o = philox4x32_10(U4{i, j, step, TAG_PAIR}, k0, k1);
   PairDraw d;
   d.u53 = ((unsigned long long)o.x << 21) | (o.y >> 11);
-  d.prio = ((unsigned long long)o.z << 32) | o.w;
   return d;
+}
+
+// 64-bit order hash of pair (i < j) at step `step`: the output function of SplitMix64 (Steele, Lea,
+// Flood, "Fast splittable pseudorandom number generators", OOPSLA 2014) applied to the pair index
+// offset by Weyl multiples of seed and step. A bijection of its 64-bit input, so pairs of one step
+// never collide; cheap enough to evaluate for every neighbour-list entry.
+__host__ __device__ __forceinline__ unsigned long long order_hash(uint32_t i, uint32_t j, uint32_t step,
+                                                                  unsigned long long seed) {
+  unsigned long long z = (((unsigned long long)i << 32) | j) + seed * 0x9E3779B97F4A7C15ull +
+                         (unsigned long long)step * 0xD1B54A32D192ED03ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
 }
 
 // Two uniforms in (-1, 1) for the diffusion kick of particle `p` at step `step`

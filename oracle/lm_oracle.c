@@ -20,8 +20,8 @@
  *       Philox4x32-10 (Salmon et al., SC'11) keyed by (seed, step, i, j) instead of MT19937.
  *   orc_priority_order / orc_interact_step : the pair order used by the GPU, then the sequential
  *       replay. The order key is the pair's colour (2x2 checkerboard of cells of size r at the
- *       pair's midpoint, computed in float32 exactly as the GPU does) followed by a 62-bit Philox
- *       hash of (seed, step, i, j); ties by (i, j).
+ *       pair's midpoint, computed in float32 exactly as the GPU does) followed by a 62-bit order
+ *       hash of (seed, step, i, j) (SplitMix64's output function); ties by (i, j).
  */
 #include "lm_oracle.h"
 
@@ -80,10 +80,18 @@ static uint32_t floor_parity(float v) {
   return (uint32_t)(f - 2.0f * floorf(f * 0.5f));
 }
 
+/* 64-bit order hash: the output function of SplitMix64 (Steele, Lea, Flood, OOPSLA 2014) applied to
+ * (i << 32 | j) offset by Weyl multiples of seed and step. */
+uint64_t orc_order_hash(uint32_t i, uint32_t j, uint32_t step, uint64_t seed) {
+  uint64_t z = (((uint64_t)i << 32) | j) + seed * 0x9E3779B97F4A7C15ull + (uint64_t)step * 0xD1B54A32D192ED03ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
 uint64_t orc_pair_prio(uint32_t i, uint32_t j, uint32_t step, uint64_t seed, float xa, float ya, float xb, float yb,
                        float inv2r) {
-  uint64_t h;
-  orc_pair_draw(i, j, step, seed, NULL, &h);
+  const uint64_t h = orc_order_hash(i, j, step, seed);
   const float mx = xa + xb, my = ya + yb;
   const uint32_t color = floor_parity(mx * inv2r) | (floor_parity(my * inv2r) << 1);
   return ((uint64_t)(3u - color) << 62) | (h >> 2);

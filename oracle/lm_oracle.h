@@ -32,6 +32,7 @@ int64_t orc_pairs(int64_t n, const float* lon, const float* lat, double r, int n
 void orc_rps_apply(int8_t* species, int32_t p1, int32_t p2, uint64_t u53, uint64_t t_rs, uint64_t t_pr, uint64_t t_sp);
 void orc_rps_replay(int8_t* species, int64_t m, const int32_t* pi, const int32_t* pj, uint32_t step, uint64_t seed,
                     uint64_t t_rs, uint64_t t_pr, uint64_t t_sp);
+uint64_t orc_order_hash(uint32_t i, uint32_t j, uint32_t step, uint64_t seed);
 uint64_t orc_pair_prio(uint32_t i, uint32_t j, uint32_t step, uint64_t seed, float xa, float ya, float xb, float yb,
                        float inv2r);
 float orc_inv2r(double r);
