@@ -87,7 +87,8 @@ int lm_ctx_set_stream(lm_ctx* ctx, uintptr_t stream);
 int lm_sync(lm_ctx* ctx);
 
 /* Velocity field: u, v float32 [nt][ny][nx] in m/s on a rectilinear lon/lat grid whose axes are
- * uniformly spaced and ascending (lon[nx], lat[ny] degrees, t_sec[nt] seconds, nt >= 2).
+ * uniformly spaced and ascending (lon[nx], lat[ny] degrees, t_sec[nt] seconds, nt >= 2). u and v
+ * may be host or device pointers (both are copied).
  * Replaces parcels RectilinearZGrid + Field(interp_method="linear") + FieldSet
  * (particle_advecter.py:177-184). */
 int lm_field_upload(lm_ctx* ctx, const float* u, const float* v, int nt, int ny, int nx, const double* lon,
@@ -199,6 +200,35 @@ int lm_profile_count(void);
  * Errors: lm_last_error(NULL, ...). */
 int lm_count_pairs_noalloc(const float* d_lon, const float* d_lat, int64_t n, double radius, int norm,
                            int32_t* d_degree, unsigned long long* d_pairs, uintptr_t stream);
+
+/* ---- Adjoint of the advection (no reference counterpart: the reference does not differentiate) ----
+ * A tape records a forward RK4 run, with the arithmetic and freezing rules of lm_step's advection
+ * (particle_advecter.py:220-223; no diffusion kick), and returns gradients of a loss on the final
+ * positions w.r.t. the initial positions and the gridded u, v. The tape keeps its own copy of the
+ * field and the state every `checkpoint_every` steps; the backward sweep recomputes each segment
+ * from its checkpoint. The velocity gradient is a deterministic segmented reduction (bit-identical
+ * from run to run, no float atomics). All arrays are DEVICE pointers (float32), on ctx's stream
+ * (lm_ctx_set_stream); errors through lm_last_error(ctx). Destroy tapes before their context. */
+typedef struct lm_adjoint lm_adjoint;
+int lm_adjoint_create(lm_ctx* ctx, lm_adjoint** out);
+int lm_adjoint_destroy(lm_adjoint* adj);
+/* u, v [nt][ny][nx] m/s and the axes as lm_field_upload (axes are host arrays); n microbes from
+ * lon0/lat0 (absolute degrees) for n_steps steps of dt_sec from t_sec0; final positions into
+ * lon_out/lat_out. Microbes leaving the domain are frozen (LM_ERR_OUT_OF_BOUNDS is returned, the tape is
+ * still valid and their gradient passes through the frozen steps unchanged). */
+int lm_adjoint_forward(lm_adjoint* adj, const float* u, const float* v, int nt, int ny, int nx, const double* lon,
+                       const double* lat, const double* t_sec, int64_t n, const float* lon0, const float* lat0,
+                       double t_sec0, double dt_sec, int n_steps, int checkpoint_every, float* lon_out,
+                       float* lat_out);
+/* dL/d(final lon, lat) [n] -> dL/d(initial lon, lat) [n] and dL/du, dL/dv [nt][ny][nx] (overwritten).
+ * May be called several times after one forward. */
+int lm_adjoint_backward(lm_adjoint* adj, const float* g_lon, const float* g_lat, float* g_lon0, float* g_lat0,
+                        float* g_u, float* g_v);
+/* Cell path of every microbe of the recorded run (device uint64 [n]): the grid cell j * nx + i of
+ * every stage evaluation, folded in order as sig = (sig ^ cell) * 0x100000001B3. The forward map
+ * is piecewise smooth (bilinear pieces meet at cell edges); two runs whose signatures agree
+ * sampled the same pieces. Used to compare gradients with an FP64 run cell path by cell path. */
+int lm_adjoint_cell_signature(lm_adjoint* adj, unsigned long long* sig);
 
 #ifdef __cplusplus
 }

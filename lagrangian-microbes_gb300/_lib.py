@@ -122,6 +122,11 @@ SIGNATURES = {
     "lm_profile_get": [P, I32, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(F64), ctypes.POINTER(I64)],
     "lm_profile_count": [],
     "lm_count_pairs_noalloc": [P, P, I64, F64, I32, P, P, ctypes.c_size_t],
+    "lm_adjoint_create": [P, ctypes.POINTER(P)],
+    "lm_adjoint_destroy": [P],
+    "lm_adjoint_forward": [P, P, P, I32, I32, I32, P, P, P, I64, P, P, F64, F64, I32, I32, P, P],
+    "lm_adjoint_backward": [P, P, P, P, P, P, P],
+    "lm_adjoint_cell_signature": [P, P],
 }
 
 

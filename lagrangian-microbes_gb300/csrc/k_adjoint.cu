@@ -1,0 +1,596 @@
+// K6 + K7: adjoint of the RK4 advection. The reference has no differentiation; the forward scheme
+// is the one of K1 (particle_advecter.py:177-187, 220-223), shared through lm_field.cuh so that
+// recomputed trajectories are bit-identical to lm_step's.
+//
+// K6 k_adj_step: one thread per microbe takes x_m (recomputed from a checkpoint) and the adjoint
+// lambda_{m+1} = dL/dx_{m+1}, and returns lambda_m by running the four RK4 stages forward and
+// their Jacobians backward:
+//   x' = x + dt/6 (k1 + 2 k2 + 2 k3 + k4),  k_s = f(t_s, x_s),  f = (U / (M cos lat), V / M),
+//   with U, V bilinear in (lon, lat), linear in time, M = 1852 * 60 m per degree.
+// For every stage it emits a record (a, b, dL/dU_s, dL/dV_s) keyed by (field cell, stage time):
+// the stage's bilinear fractions inside its cell and its adjoint in field units.
+//
+// K7, the deterministic segmented reduction: the 4 N records of a step are put in (cell, stage
+// time, record id) order by a stable LSD radix sort (block-local ranks from warp match masks, no
+// atomics on positions); one warp per cell then sums each (cell, stage time) segment into the four
+// corner weights (fixed lane order, Neumaier-compensated float32 lane sums, fixed-shape warp tree);
+// a node pass adds, for every grid node, the four cells around it in a fixed order and spreads the
+// three stage times onto the field's frames with the linear-in-time weights. No float atomics: the
+// gradient is bit-identical from run to run.
+#include "lm_field.cuh"
+#include "lm_internal.h"
+
+namespace lm {
+
+// ---------------------------------------------------------------- stage table, recompute
+
+// Stage brackets of step m at t_m = t_start + m * dt (the arithmetic of k_step_begin).
+__global__ void k_adj_stages(FieldView f, double t_start, double dt, int n_steps, AdjStep* table, uint32_t* err) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= n_steps) return;
+  const double t0 = t_start + (double)m * dt;
+  const double ts[3] = {t0, t0 + 0.5 * dt, t0 + dt};
+  AdjStep s;
+  int ok = 1;
+  for (int k = 0; k < 3; ++k) {
+    const Stage sg = stage_at(f, ts[k]);
+    s.k[k] = sg.k;
+    s.w[k] = sg.w;
+    ok = ok && sg.ok;
+  }
+  table[m] = s;
+  if (!ok) atomicOr(err, (uint32_t)ERRB_TIME);
+}
+
+// Absolute float32 positions -> offsets from the field origin (exact in float64), status.
+__global__ void k_adj_init(FieldView f, uint32_t n, const float* __restrict__ lon, const float* __restrict__ lat,
+                           float* __restrict__ x, float* __restrict__ y, uint8_t* __restrict__ st) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const float a = lon[p], b = lat[p];
+  x[p] = (float)((double)a - (double)f.org_lon);
+  y[p] = (float)((double)b - (double)f.org_lat);
+  st[p] = (isfinite(a) && isfinite(b)) ? STATUS_OK : STATUS_NAN;
+}
+
+__global__ void k_adj_final(FieldView f, uint32_t n, const float* __restrict__ x, const float* __restrict__ y,
+                            float* __restrict__ lon, float* __restrict__ lat) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  lon[p] = __fadd_rn(f.org_lon, x[p]);
+  lat[p] = __fadd_rn(f.org_lat, y[p]);
+}
+
+// Steps [m0, m1) of every microbe in registers, the forward's arithmetic and freezing rules. With
+// rec_* set, the state before every step is stored ([m - m0][n]) for the backward sweep.
+__global__ void __launch_bounds__(256) k_adj_forward(FieldView f, const AdjStep* __restrict__ table, int m0, int m1,
+                                                     float dt, uint32_t n, float* __restrict__ xs,
+                                                     float* __restrict__ ys, uint8_t* __restrict__ sts,
+                                                     float* __restrict__ rec_x, float* __restrict__ rec_y,
+                                                     uint8_t* __restrict__ rec_st, uint32_t* err) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  float x = xs[p], y = ys[p];
+  uint8_t st = sts[p];
+  uint32_t bits = 0;
+  for (int m = m0; m < m1; ++m) {
+    if (rec_x) {
+      const size_t o = (size_t)(m - m0) * n + p;
+      rec_x[o] = x;
+      rec_y[o] = y;
+      rec_st[o] = st;
+    }
+    if (st != STATUS_OK) continue;
+    const AdjStep s = table[m];
+    const Stage sh[3] = {{s.k[0], s.w[0], 1}, {s.k[1], s.w[1], 1}, {s.k[2], s.w[2], 1}};
+    float nx, ny;
+    if (rk4_step(f, f.uv, sh, dt, x, y, nx, ny)) {
+      if (isfinite(nx) && isfinite(ny)) {
+        x = nx;
+        y = ny;
+      } else {
+        st = STATUS_NAN;
+        bits |= ERRB_NAN;
+      }
+    } else {
+      st = (isfinite(x) && isfinite(y)) ? STATUS_OOB : STATUS_NAN;
+      bits |= st == STATUS_OOB ? (uint32_t)ERRB_OOB : (uint32_t)ERRB_NAN;
+    }
+  }
+  xs[p] = x;
+  ys[p] = y;
+  sts[p] = st;
+  if (bits) atomicOr(err, bits);
+}
+
+// ---------------------------------------------------------------- K6: one backward step
+
+// Velocity and its Jacobian w.r.t. the offset position; the value is computed with exactly the
+// arithmetic of velocity() so that the recomputed stage positions are the forward's.
+struct VelJac {
+  float flon, flat;                          // deg/s
+  float dlon_dx, dlon_dy, dlat_dx, dlat_dy;  // 1/s
+  uint32_t cell;                             // j * (nx - 1) + i
+  float a, b;                                // bilinear fractions
+  float inv_mc;                              // d flon / d U = 1 / (M cos lat)
+};
+
+__device__ __forceinline__ bool vel_jac(const FieldView& f, const Stage& s, float xo, float yo, VelJac& r) {
+  const float fx = (xo - f.gx0) * f.inv_dx;
+  const float fy = (yo - f.gy0) * f.inv_dy;
+  if (!(fx >= 0.f && fx <= f.max_fx && fy >= 0.f && fy <= f.max_fy)) return false;
+  const int i = min((int)fx, f.nx - 2);
+  const int j = min((int)fy, f.ny - 2);
+  const float a = fx - (float)i, b = fy - (float)j;
+  const float2* p = f.uv + ((size_t)s.k * f.ny + j) * f.nx + i;
+  float2 c00 = __ldg(p), c01 = __ldg(p + 1), c10 = __ldg(p + f.nx), c11 = __ldg(p + f.nx + 1);
+  const float w00 = (1.f - a) * (1.f - b), w01 = a * (1.f - b), w10 = (1.f - a) * b, w11 = a * b;
+  float u = w00 * c00.x + w01 * c01.x + w10 * c10.x + w11 * c11.x;
+  float v = w00 * c00.y + w01 * c01.y + w10 * c10.y + w11 * c11.y;
+  float ua = (1.f - b) * (c01.x - c00.x) + b * (c11.x - c10.x);
+  float ub = (1.f - a) * (c10.x - c00.x) + a * (c11.x - c01.x);
+  float va = (1.f - b) * (c01.y - c00.y) + b * (c11.y - c10.y);
+  float vb = (1.f - a) * (c10.y - c00.y) + a * (c11.y - c01.y);
+  if (s.w != 0.f) {
+    p += (size_t)f.nx * f.ny;
+    c00 = __ldg(p); c01 = __ldg(p + 1); c10 = __ldg(p + f.nx); c11 = __ldg(p + f.nx + 1);
+    const float u1 = w00 * c00.x + w01 * c01.x + w10 * c10.x + w11 * c11.x;
+    const float v1 = w00 * c00.y + w01 * c01.y + w10 * c10.y + w11 * c11.y;
+    u = u + s.w * (u1 - u);
+    v = v + s.w * (v1 - v);
+    ua = ua + s.w * (((1.f - b) * (c01.x - c00.x) + b * (c11.x - c10.x)) - ua);
+    ub = ub + s.w * (((1.f - a) * (c10.x - c00.x) + a * (c11.x - c01.x)) - ub);
+    va = va + s.w * (((1.f - b) * (c01.y - c00.y) + b * (c11.y - c10.y)) - va);
+    vb = vb + s.w * (((1.f - a) * (c10.y - c00.y) + a * (c11.y - c01.y)) - vb);
+  }
+  const float lat = f.org_lat + yo;
+  const float c = cospif(lat * (1.0f / 180.0f));
+  const float sn = sinpif(lat * (1.0f / 180.0f));
+  r.flon = u / (M_PER_DEG * c);
+  r.flat = v * (1.0f / M_PER_DEG);
+  r.inv_mc = 1.0f / (M_PER_DEG * c);
+  // d/dlat (1 / cos(lat)) = tan(lat) / cos(lat) * pi / 180 per degree
+  r.dlon_dx = ua * f.inv_dx * r.inv_mc;
+  r.dlon_dy = ub * f.inv_dy * r.inv_mc + r.flon * (sn / c) * 0.017453292519943295f;
+  r.dlat_dx = va * f.inv_dx * (1.0f / M_PER_DEG);
+  r.dlat_dy = vb * f.inv_dy * (1.0f / M_PER_DEG);
+  r.cell = (uint32_t)j * (uint32_t)(f.nx - 1) + (uint32_t)i;
+  r.a = a;
+  r.b = b;
+  return true;
+}
+
+// lambda_{m+1} -> lambda_m, plus 4 records per microbe (key = cell * 4 + stage time, or `sent`).
+__global__ void __launch_bounds__(256) k_adj_step(FieldView f, AdjStep s, float dt, uint32_t n,
+                                                  const float* __restrict__ xs, const float* __restrict__ ys,
+                                                  const uint8_t* __restrict__ sts, float* __restrict__ lx,
+                                                  float* __restrict__ ly, float4* __restrict__ rec,
+                                                  uint32_t* __restrict__ key, uint32_t sent) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const float x = xs[p], y = ys[p];
+  const Stage sh0 = {s.k[0], s.w[0], 1}, sh1 = {s.k[1], s.w[1], 1}, sh2 = {s.k[2], s.w[2], 1};
+  VelJac J1, J2, J3, J4;
+  bool ok = sts[p] == STATUS_OK;
+  ok = ok && vel_jac(f, sh0, x, y, J1);
+  ok = ok && vel_jac(f, sh1, x + 0.5f * dt * J1.flon, y + 0.5f * dt * J1.flat, J2);
+  ok = ok && vel_jac(f, sh1, x + 0.5f * dt * J2.flon, y + 0.5f * dt * J2.flat, J3);
+  ok = ok && vel_jac(f, sh2, x + dt * J3.flon, y + dt * J3.flat, J4);
+  if (ok) {  // a non-finite step was frozen by the forward: identity, like a stage off the grid
+    const float nx = x + (J1.flon + 2.f * J2.flon + 2.f * J3.flon + J4.flon) * (dt * (1.0f / 6.0f));
+    const float ny = y + (J1.flat + 2.f * J2.flat + 2.f * J3.flat + J4.flat) * (dt * (1.0f / 6.0f));
+    ok = isfinite(nx) && isfinite(ny);
+  }
+  uint4* kq = reinterpret_cast<uint4*>(key) + p;
+  if (!ok) {  // frozen this step: x_{m+1} = x_m, the adjoint passes through
+    *kq = make_uint4(sent, sent, sent, sent);
+    return;
+  }
+  const float gx = lx[p], gy = ly[p];
+  const float h6 = dt * (1.0f / 6.0f), h3 = dt * (1.0f / 3.0f), h2 = 0.5f * dt;
+  // dL/dk4, then back through x3 = x + dt k3, x2 = x + dt/2 k2, x1 = x + dt/2 k1
+  const float g4x = h6 * gx, g4y = h6 * gy;
+  const float x3x = J4.dlon_dx * g4x + J4.dlat_dx * g4y, x3y = J4.dlon_dy * g4x + J4.dlat_dy * g4y;
+  const float g3x = h3 * gx + dt * x3x, g3y = h3 * gy + dt * x3y;
+  const float x2x = J3.dlon_dx * g3x + J3.dlat_dx * g3y, x2y = J3.dlon_dy * g3x + J3.dlat_dy * g3y;
+  const float g2x = h3 * gx + h2 * x2x, g2y = h3 * gy + h2 * x2y;
+  const float x1x = J2.dlon_dx * g2x + J2.dlat_dx * g2y, x1y = J2.dlon_dy * g2x + J2.dlat_dy * g2y;
+  const float g1x = h6 * gx + h2 * x1x, g1y = h6 * gy + h2 * x1y;
+  const float x0x = J1.dlon_dx * g1x + J1.dlat_dx * g1y, x0y = J1.dlon_dy * g1x + J1.dlat_dy * g1y;
+  lx[p] = gx + ((x0x + x1x) + (x2x + x3x));
+  ly[p] = gy + ((x0y + x1y) + (x2y + x3y));
+  // records: dL/dU_s = dL/dk_s,lon / (M cos lat_s), dL/dV_s = dL/dk_s,lat / M
+  float4* rq = rec + 4 * (size_t)p;
+  rq[0] = make_float4(J1.a, J1.b, g1x * J1.inv_mc, g1y * (1.0f / M_PER_DEG));
+  rq[1] = make_float4(J2.a, J2.b, g2x * J2.inv_mc, g2y * (1.0f / M_PER_DEG));
+  rq[2] = make_float4(J3.a, J3.b, g3x * J3.inv_mc, g3y * (1.0f / M_PER_DEG));
+  rq[3] = make_float4(J4.a, J4.b, g4x * J4.inv_mc, g4y * (1.0f / M_PER_DEG));
+  *kq = make_uint4(4u * J1.cell + 0u, 4u * J2.cell + 1u, 4u * J3.cell + 1u, 4u * J4.cell + 2u);
+}
+
+// Cell path of every microbe over steps [0, n_steps): the grid cell (j * nx + i) of each stage that
+// the forward evaluated, folded in order as sig = (sig ^ cell) * 0x100000001B3. The stage
+// positions come from vel_jac, whose values are the forward's; two runs of one microbe with equal
+// signatures sampled the same bilinear pieces, so the map between them is smooth.
+__global__ void __launch_bounds__(256) k_adj_signature(FieldView f, const AdjStep* __restrict__ table, int n_steps,
+                                                       float dt, uint32_t n, const float* __restrict__ xs,
+                                                       const float* __restrict__ ys, const uint8_t* __restrict__ sts,
+                                                       unsigned long long* __restrict__ sig) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  float x = xs[p], y = ys[p];
+  bool live = sts[p] == STATUS_OK;
+  unsigned long long h = 0;
+  const unsigned long long nx = (unsigned long long)f.nx, cw = (unsigned long long)(f.nx - 1);
+  for (int m = 0; m < n_steps && live; ++m) {
+    const AdjStep s = table[m];
+    const Stage sh0 = {s.k[0], s.w[0], 1}, sh1 = {s.k[1], s.w[1], 1}, sh2 = {s.k[2], s.w[2], 1};
+    VelJac J;
+    float kx[4], ky[4];
+    bool ok = vel_jac(f, sh0, x, y, J);
+    if (ok) {
+      h = (h ^ ((J.cell / cw) * nx + J.cell % cw)) * 0x100000001B3ull;
+      kx[0] = J.flon, ky[0] = J.flat;
+      ok = vel_jac(f, sh1, x + 0.5f * dt * kx[0], y + 0.5f * dt * ky[0], J);
+    }
+    if (ok) {
+      h = (h ^ ((J.cell / cw) * nx + J.cell % cw)) * 0x100000001B3ull;
+      kx[1] = J.flon, ky[1] = J.flat;
+      ok = vel_jac(f, sh1, x + 0.5f * dt * kx[1], y + 0.5f * dt * ky[1], J);
+    }
+    if (ok) {
+      h = (h ^ ((J.cell / cw) * nx + J.cell % cw)) * 0x100000001B3ull;
+      kx[2] = J.flon, ky[2] = J.flat;
+      ok = vel_jac(f, sh2, x + dt * kx[2], y + dt * ky[2], J);
+    }
+    if (!ok) break;
+    h = (h ^ ((J.cell / cw) * nx + J.cell % cw)) * 0x100000001B3ull;
+    kx[3] = J.flon, ky[3] = J.flat;
+    const float nx_ = x + (kx[0] + 2.f * kx[1] + 2.f * kx[2] + kx[3]) * (dt * (1.0f / 6.0f));
+    const float ny_ = y + (ky[0] + 2.f * ky[1] + 2.f * ky[2] + ky[3]) * (dt * (1.0f / 6.0f));
+    if (!(isfinite(nx_) && isfinite(ny_))) break;
+    x = nx_;
+    y = ny_;
+  }
+  sig[p] = h;
+}
+
+// ---------------------------------------------------------------- K7a: stable LSD radix sort
+
+constexpr int RS_THREADS = 256;
+constexpr int RS_ITEMS = 16;
+constexpr uint32_t RS_TILE = RS_THREADS * RS_ITEMS;
+constexpr int RS_WARPS = RS_THREADS / 32;
+
+// Digit histogram of one tile, written digit-major: hist[d * tiles + tile].
+__global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const uint32_t* __restrict__ keys, uint32_t m, int shift,
+                                                        int bits, uint32_t* __restrict__ hist, uint32_t tiles) {
+  __shared__ uint32_t h[RS_RADIX_MAX];
+  const uint32_t R = 1u << bits, mask = R - 1u;
+  for (uint32_t d = threadIdx.x; d < R; d += RS_THREADS) h[d] = 0;
+  __syncthreads();
+  const uint32_t base = blockIdx.x * RS_TILE;
+  const uint32_t lane = threadIdx.x & 31u;
+  for (int r = 0; r < RS_ITEMS; ++r) {
+    const uint32_t i = base + (uint32_t)r * RS_THREADS + threadIdx.x;
+    const bool valid = i < m;
+    const uint32_t d = valid ? (keys[i] >> shift) & mask : R;
+    const uint32_t peers = __match_any_sync(0xffffffffu, d);
+    if (valid && (peers & ((1u << lane) - 1u)) == 0) atomicAdd(&h[d], (uint32_t)__popc(peers));
+  }
+  __syncthreads();
+  for (uint32_t d = threadIdx.x; d < R; d += RS_THREADS) hist[(size_t)d * tiles + blockIdx.x] = h[d];
+}
+
+// Stable scatter of one tile. Items are taken in index order (round r, warp w, lane l), so the rank
+// of an item among equal digits is (tile offset of the digit) + (earlier rounds) + (earlier warps
+// of this round) + (earlier lanes of its warp): the order of equal keys is preserved.
+__global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint32_t* __restrict__ kin,
+                                                           const uint32_t* __restrict__ vin,
+                                                           uint32_t* __restrict__ kout, uint32_t* __restrict__ vout,
+                                                           uint32_t m, int shift, int bits,
+                                                           const uint32_t* __restrict__ hscan, uint32_t tiles) {
+  __shared__ uint32_t run[RS_RADIX_MAX];
+  __shared__ uint32_t wcnt[RS_WARPS][RS_RADIX_MAX];
+  const uint32_t R = 1u << bits, mask = R - 1u;
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  for (uint32_t d = threadIdx.x; d < R; d += RS_THREADS) {
+    run[d] = hscan[(size_t)d * tiles + blockIdx.x];
+    for (int w = 0; w < RS_WARPS; ++w) wcnt[w][d] = 0;
+  }
+  __syncthreads();
+  const uint32_t base = blockIdx.x * RS_TILE;
+  for (int r = 0; r < RS_ITEMS; ++r) {
+    const uint32_t i = base + (uint32_t)r * RS_THREADS + threadIdx.x;
+    const bool valid = i < m;
+    const uint32_t k = valid ? kin[i] : 0u;
+    const uint32_t v = valid ? (vin ? vin[i] : i) : 0u;
+    const uint32_t d = valid ? (k >> shift) & mask : R;
+    const uint32_t peers = __match_any_sync(0xffffffffu, d);
+    const uint32_t below = peers & ((1u << lane) - 1u);
+    const bool leader = valid && below == 0;
+    if (leader) wcnt[warp][d] = (uint32_t)__popc(peers);
+    __syncthreads();
+    if (valid) {
+      uint32_t o = run[d] + (uint32_t)__popc(below);
+      for (uint32_t w = 0; w < warp; ++w) o += wcnt[w][d];
+      kout[o] = k;
+      vout[o] = v;
+    }
+    __syncthreads();
+    if (leader) {
+      atomicAdd(&run[d], (uint32_t)__popc(peers));
+      wcnt[warp][d] = 0;
+    }
+    __syncwarp();
+  }
+}
+
+// Exclusive scan of n uint32 values (in -> out), in SCAN_BLOCKS contiguous chunks: block sums, then
+// each block adds the sums of the blocks before it while scanning its chunk.
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* sh, uint32_t* total) {
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  uint32_t x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= (uint32_t)o) x += y;
+  }
+  if (lane == 31) sh[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t s = lane < blockDim.x / 32 ? sh[lane] : 0u;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+      if (lane >= (uint32_t)o) s += y;
+    }
+    sh[lane] = s;  // inclusive warp totals
+  }
+  __syncthreads();
+  const uint32_t before = warp ? sh[warp - 1] : 0u;
+  *total = sh[blockDim.x / 32 - 1];
+  __syncthreads();
+  return before + x - v;
+}
+
+__global__ void __launch_bounds__(256) k_scan_sums(const uint32_t* __restrict__ in, size_t n, size_t chunk,
+                                                   uint32_t* __restrict__ bsum) {
+  __shared__ uint32_t red[8];
+  const size_t lo = (size_t)blockIdx.x * chunk, hi = min(n, lo + chunk);
+  uint32_t s = 0;
+  for (size_t i = lo + threadIdx.x; i < hi; i += blockDim.x) s += in[i];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t t = 0;
+    for (int w = 0; w < 8; ++w) t += red[w];
+    bsum[blockIdx.x] = t;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_scan_chunks(const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
+                                                     size_t n, size_t chunk, const uint32_t* __restrict__ bsum) {
+  __shared__ uint32_t sh[32];
+  __shared__ uint32_t carry;
+  if (threadIdx.x < 32) {
+    uint32_t s = 0;
+    for (uint32_t b = threadIdx.x; b < blockIdx.x; b += 32) s += bsum[b];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (threadIdx.x == 0) carry = s;
+  }
+  __syncthreads();
+  const size_t lo = (size_t)blockIdx.x * chunk, hi = min(n, lo + chunk);
+  for (size_t t = lo; t < hi; t += blockDim.x) {
+    const size_t i = t + threadIdx.x;
+    const uint32_t v = i < hi ? in[i] : 0u;
+    uint32_t total;
+    const uint32_t ex = block_exclusive_scan(v, sh, &total);
+    if (i < hi) out[i] = carry + ex;
+    __syncthreads();
+    if (threadIdx.x == 0) carry += total;
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------- K7b: segmented reduction
+
+// Segment bounds of the sorted keys: cst[k] = first index, cen[k] = one past the last (both left at
+// 0 for absent keys; the reduction resets the entries it read).
+__global__ void k_adj_bounds(const uint32_t* __restrict__ skey, uint32_t m, uint32_t sent, uint32_t* __restrict__ cst,
+                             uint32_t* __restrict__ cen) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const uint32_t k = skey[i];
+  if (k >= sent) return;
+  if (i == 0 || skey[i - 1] != k) cst[k] = i;
+  if (i + 1 == m || skey[i + 1] != k) cen[k] = i + 1;
+}
+
+__device__ __forceinline__ void neumaier(float& s, float& c, float v) {
+  const float t = s + v;
+  c += (fabsf(s) >= fabsf(v)) ? ((s - t) + v) : ((v - t) + s);
+  s = t;
+}
+
+// One warp per field cell: for each stage time g, the records of segment (cell, g) in sorted order,
+// lane l taking entries l, l+32, ...; out csum[(cell * 3 + g) * 8 + q], q = corner (00, 01, 10, 11)
+// of dL/dU, then of dL/dV.
+__global__ void __launch_bounds__(256) k_adj_reduce(uint32_t ncells, uint32_t* __restrict__ cst,
+                                                    uint32_t* __restrict__ cen, const uint32_t* __restrict__ sval,
+                                                    const float4* __restrict__ rec, float* __restrict__ csum) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t c = wid; c < ncells; c += nw) {
+    for (uint32_t g = 0; g < 3; ++g) {
+      const uint32_t k = 4u * c + g;
+      const uint32_t lo = cst[k], hi = cen[k];
+      float* out = csum + ((size_t)c * 3 + g) * 8;
+      if (lo == hi) {  // warp-uniform: an empty segment
+        if (lane < 8) out[lane] = 0.f;
+        continue;
+      }
+      float s[8], e[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) s[q] = e[q] = 0.f;
+      for (uint32_t i = lo + lane; i < hi; i += 32) {
+        const float4 r = rec[sval[i]];
+        const float a = r.x, b = r.y;
+        const float w[4] = {(1.f - a) * (1.f - b), a * (1.f - b), (1.f - a) * b, a * b};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          neumaier(s[q], e[q], w[q] * r.z);
+          neumaier(s[4 + q], e[4 + q], w[q] * r.w);
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        float t = s[q] + e[q];
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        s[q] = t;
+      }
+      if (lane == 0) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) out[q] = s[q];
+        cst[k] = 0;
+        cen[k] = 0;
+      }
+    }
+  }
+}
+
+// One thread per grid node: the four cells around it in a fixed order, then the three stage times
+// spread onto frames k_g (weight 1 - w_g) and k_g + 1 (weight w_g), added to the gradient.
+__global__ void __launch_bounds__(256) k_adj_nodes(int nx, int ny, AdjStep s, const float* __restrict__ csum,
+                                                   float* __restrict__ gu, float* __restrict__ gv) {
+  const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= (uint32_t)nx * (uint32_t)ny) return;
+  const int ni = (int)(q % (uint32_t)nx), nj = (int)(q / (uint32_t)nx);
+  const int cw = nx - 1;
+  float U[3] = {0.f, 0.f, 0.f}, V[3] = {0.f, 0.f, 0.f};
+  // cell (ci, cj) sees this node as corner (nj - cj) * 2 + (ni - ci)
+  const int ci_[4] = {ni - 1, ni, ni - 1, ni}, cj_[4] = {nj - 1, nj - 1, nj, nj}, corner[4] = {3, 2, 1, 0};
+#pragma unroll
+  for (int t = 0; t < 4; ++t) {
+    const int ci = ci_[t], cj = cj_[t];
+    if (ci < 0 || cj < 0 || ci > nx - 2 || cj > ny - 2) continue;
+    const float* cs = csum + ((size_t)cj * cw + ci) * 24;
+#pragma unroll
+    for (int g = 0; g < 3; ++g) {
+      U[g] += cs[g * 8 + corner[t]];
+      V[g] += cs[g * 8 + 4 + corner[t]];
+    }
+  }
+  if (U[0] == 0.f && U[1] == 0.f && U[2] == 0.f && V[0] == 0.f && V[1] == 0.f && V[2] == 0.f) return;
+  int kmin = s.k[0], kmax = s.k[0];
+#pragma unroll
+  for (int g = 0; g < 3; ++g) {
+    kmin = min(kmin, s.k[g]);
+    kmax = max(kmax, s.k[g] + (s.w[g] != 0.f ? 1 : 0));
+  }
+  const size_t plane = (size_t)nx * ny;
+  for (int fr = kmin; fr <= kmax; ++fr) {
+    float du = 0.f, dv = 0.f;
+    bool any = false;
+#pragma unroll
+    for (int g = 0; g < 3; ++g) {
+      if (s.k[g] == fr) {
+        du += (1.f - s.w[g]) * U[g];
+        dv += (1.f - s.w[g]) * V[g];
+        any = true;
+      }
+      if (s.w[g] != 0.f && s.k[g] + 1 == fr) {
+        du += s.w[g] * U[g];
+        dv += s.w[g] * V[g];
+        any = true;
+      }
+    }
+    if (any) {
+      gu[(size_t)fr * plane + q] += du;
+      gv[(size_t)fr * plane + q] += dv;
+    }
+  }
+}
+
+// ---------------------------------------------------------------- launchers
+
+static inline unsigned grid_for(size_t n, unsigned block) { return (unsigned)((n + block - 1) / block); }
+
+void launch_adj_stages(const FieldView& f, double t_start, double dt, int n_steps, AdjStep* table, uint32_t* err,
+                       cudaStream_t st) {
+  if (n_steps > 0) k_adj_stages<<<grid_for(n_steps, 128), 128, 0, st>>>(f, t_start, dt, n_steps, table, err);
+}
+
+void launch_adj_init(const FieldView& f, uint32_t n, const float* lon, const float* lat, float* x, float* y,
+                     uint8_t* status, cudaStream_t st) {
+  if (n) k_adj_init<<<grid_for(n, 256), 256, 0, st>>>(f, n, lon, lat, x, y, status);
+}
+
+void launch_adj_final(const FieldView& f, uint32_t n, const float* x, const float* y, float* lon, float* lat,
+                      cudaStream_t st) {
+  if (n) k_adj_final<<<grid_for(n, 256), 256, 0, st>>>(f, n, x, y, lon, lat);
+}
+
+void launch_adj_forward(const FieldView& f, const AdjStep* table, int m0, int m1, float dt, uint32_t n, float* x,
+                        float* y, uint8_t* status, float* rec_x, float* rec_y, uint8_t* rec_st, uint32_t* err,
+                        cudaStream_t st) {
+  if (n && m1 > m0)
+    k_adj_forward<<<grid_for(n, 256), 256, 0, st>>>(f, table, m0, m1, dt, n, x, y, status, rec_x, rec_y, rec_st, err);
+}
+
+void launch_adj_step(const FieldView& f, const AdjStep& s, float dt, uint32_t n, const float* x, const float* y,
+                     const uint8_t* status, float* lx, float* ly, float4* rec, uint32_t* key, uint32_t sent,
+                     cudaStream_t st) {
+  if (n) k_adj_step<<<grid_for(n, 256), 256, 0, st>>>(f, s, dt, n, x, y, status, lx, ly, rec, key, sent);
+}
+
+void launch_adj_signature(const FieldView& f, const AdjStep* table, int n_steps, float dt, uint32_t n, const float* x,
+                          const float* y, const uint8_t* status, unsigned long long* sig, cudaStream_t st) {
+  if (n) k_adj_signature<<<grid_for(n, 256), 256, 0, st>>>(f, table, n_steps, dt, n, x, y, status, sig);
+}
+
+size_t adj_sort_hist_len(uint32_t m) { return (size_t)RS_RADIX_MAX * grid_for(m, RS_TILE); }
+
+void adj_sort(const AdjSortBufs& sb, uint32_t m, int key_bits, cudaStream_t st, const uint32_t** skey,
+              const uint32_t** sval) {
+  const uint32_t tiles = grid_for(m, RS_TILE);
+  const int passes = key_bits <= RS_BITS_MAX ? 1 : (key_bits + RS_BITS_MAX - 1) / RS_BITS_MAX;
+  const int width = (key_bits + passes - 1) / passes;
+  const uint32_t* kin = sb.key;
+  const uint32_t* vin = nullptr;
+  for (int p = 0; p < passes; ++p) {
+    uint32_t* kout = (p & 1) ? sb.k2 : sb.k1;
+    uint32_t* vout = (p & 1) ? sb.v2 : sb.v1;
+    const int shift = p * width;
+    const int bits = key_bits - shift < width ? key_bits - shift : width;
+    k_rs_hist<<<tiles, RS_THREADS, 0, st>>>(kin, m, shift, bits, sb.hist, tiles);
+    const size_t len = ((size_t)1 << bits) * tiles;
+    const size_t chunk = (len + SCAN_BLOCKS - 1) / SCAN_BLOCKS;
+    const unsigned nb = grid_for(len, chunk);
+    k_scan_sums<<<nb, 256, 0, st>>>(sb.hist, len, chunk, sb.bsum);
+    k_scan_chunks<<<nb, 256, 0, st>>>(sb.hist, sb.hscan, len, chunk, sb.bsum);
+    k_rs_scatter<<<tiles, RS_THREADS, 0, st>>>(kin, vin, kout, vout, m, shift, bits, sb.hscan, tiles);
+    kin = kout;
+    vin = vout;
+  }
+  *skey = kin;
+  *sval = vin;
+}
+
+void launch_adj_bounds(const uint32_t* skey, uint32_t m, uint32_t sent, uint32_t* cst, uint32_t* cen,
+                       cudaStream_t st) {
+  if (m) k_adj_bounds<<<grid_for(m, 256), 256, 0, st>>>(skey, m, sent, cst, cen);
+}
+
+void launch_adj_reduce(uint32_t ncells, uint32_t* cst, uint32_t* cen, const uint32_t* sval, const float4* rec,
+                       float* csum, int sms, cudaStream_t st) {
+  unsigned blocks = grid_for((size_t)ncells * 32, 256);
+  const unsigned cap = (unsigned)(sms > 0 ? sms : 152) * 16u;
+  if (blocks > cap) blocks = cap;
+  if (ncells) k_adj_reduce<<<blocks, 256, 0, st>>>(ncells, cst, cen, sval, rec, csum);
+}
+
+void launch_adj_nodes(int nx, int ny, const AdjStep& s, const float* csum, float* gu, float* gv, cudaStream_t st) {
+  k_adj_nodes<<<grid_for((size_t)nx * ny, 256), 256, 0, st>>>(nx, ny, s, csum, gu, gv);
+}
+
+}  // namespace lm

@@ -13,6 +13,7 @@
 // seed and slot base are loaded once per block. The block also reduces the bounding box of its
 // advected positions into its ensemble's box (ordered-int atomics), from which the binning grid
 // of this step is built.
+#include "lm_field.cuh"
 #include "lm_internal.h"
 #include "lm_philox.cuh"
 
@@ -29,59 +30,6 @@ void launch_interleave(const float* u, const float* v, float2* uv, size_t n, cud
   if (grid > 152 * 32) grid = 152 * 32;
   if (grid < 1) grid = 1;
   k_interleave<<<grid, 256, 0, st>>>(u, v, uv, n);
-}
-
-struct Stage {
-  int k;    // frame index
-  float w;  // weight of frame k+1 (0 means frame k only)
-  int ok;
-};
-
-// Frame bracket of time t on a uniform time axis t0 + k*dT, k in [0, nt).
-__device__ __forceinline__ Stage stage_at(const FieldView& f, double t) {
-  Stage s;
-  double fk = (t - f.t0) / f.dT;
-  s.ok = (fk >= -1e-9 && fk <= (double)(f.nt - 1) + 1e-9);
-  double kf = floor(fk);
-  int k = (int)fmin(fmax(kf, 0.0), (double)(f.nt - 2));
-  double w = fmin(fmax(fk - (double)k, 0.0), 1.0);
-  if (w >= 1.0) {  // exactly on frame k+1: read that frame alone
-    k += 1;
-    w = 0.0;
-  }
-  s.k = k;
-  s.w = (float)w;
-  return s;
-}
-
-// Velocity in deg/s at offset position (xo, yo). Returns false outside the grid or on NaN.
-__device__ __forceinline__ bool velocity(const FieldView& f, const float2* __restrict__ uv, const Stage& s, float xo,
-                                         float yo, float& dlon, float& dlat) {
-  float fx = (xo - f.gx0) * f.inv_dx;
-  float fy = (yo - f.gy0) * f.inv_dy;
-  if (!(fx >= 0.f && fx <= f.max_fx && fy >= 0.f && fy <= f.max_fy)) return false;
-  int i = min((int)fx, f.nx - 2);
-  int j = min((int)fy, f.ny - 2);
-  float a = fx - (float)i, b = fy - (float)j;
-  const float2* p = uv + ((size_t)s.k * f.ny + j) * f.nx + i;
-  float2 c00 = __ldg(p), c01 = __ldg(p + 1), c10 = __ldg(p + f.nx), c11 = __ldg(p + f.nx + 1);
-  float w00 = (1.f - a) * (1.f - b), w01 = a * (1.f - b), w10 = (1.f - a) * b, w11 = a * b;
-  float u = w00 * c00.x + w01 * c01.x + w10 * c10.x + w11 * c11.x;
-  float v = w00 * c00.y + w01 * c01.y + w10 * c10.y + w11 * c11.y;
-  if (s.w != 0.f) {
-    p += (size_t)f.nx * f.ny;
-    c00 = __ldg(p); c01 = __ldg(p + 1); c10 = __ldg(p + f.nx); c11 = __ldg(p + f.nx + 1);
-    float u1 = w00 * c00.x + w01 * c01.x + w10 * c10.x + w11 * c11.x;
-    float v1 = w00 * c00.y + w01 * c01.y + w10 * c10.y + w11 * c11.y;
-    u = u + s.w * (u1 - u);
-    v = v + s.w * (v1 - v);
-  }
-  // 1 degree of latitude = 1852 m * 60 (the nautical-mile convention of a spherical mesh).
-  float lat = f.org_lat + yo;
-  float c = cospif(lat * (1.0f / 180.0f));
-  dlon = u / (111120.0f * c);
-  dlat = v * (1.0f / 111120.0f);
-  return true;
 }
 
 // Block-level bounding box of valid positions, merged into the ensemble's box.
@@ -149,14 +97,8 @@ __global__ void __launch_bounds__(SLOT_BLOCK) k_advect(FieldView f, StepArgs a, 
   }
   const float dt = (float)a.dt;
   if (st == STATUS_OK) {
-    float k1x, k1y, k2x, k2y, k3x, k3y, k4x, k4y;
-    bool ok = velocity(f, uv, sh[0], x, y, k1x, k1y);
-    ok = ok && velocity(f, uv, sh[1], x + 0.5f * dt * k1x, y + 0.5f * dt * k1y, k2x, k2y);
-    ok = ok && velocity(f, uv, sh[1], x + 0.5f * dt * k2x, y + 0.5f * dt * k2y, k3x, k3y);
-    ok = ok && velocity(f, uv, sh[2], x + dt * k3x, y + dt * k3y, k4x, k4y);
-    if (ok) {
-      float nx = x + (k1x + 2.f * k2x + 2.f * k3x + k4x) * (dt * (1.0f / 6.0f));
-      float ny = y + (k1y + 2.f * k2y + 2.f * k3y + k4y) * (dt * (1.0f / 6.0f));
+    float nx, ny;
+    if (rk4_step(f, uv, sh, dt, x, y, nx, ny)) {
       if (isfinite(nx) && isfinite(ny)) {
         x = nx;
         y = ny;

@@ -515,16 +515,6 @@ void set_pair_params(lm_ctx* c, double r, int norm) {
   pp.cell_factor = (float)c->cell_factor;
 }
 
-bool uniform_axis(const double* a, int n, double* d) {
-  if (n < 2) return false;
-  const double step = (a[n - 1] - a[0]) / (n - 1);
-  if (!(step > 0) || !std::isfinite(step)) return false;
-  for (int k = 0; k < n; ++k)
-    if (std::fabs(a[k] - (a[0] + step * k)) > 1e-6 * step) return false;
-  *d = step;
-  return true;
-}
-
 // Copies of one step's records into caller-order host arrays.
 int record_step(lm_ctx* c, int64_t k, float* rec_lon, float* rec_lat, int8_t* rec_species) {
   const uint32_t n = c->ntotal;
@@ -742,8 +732,8 @@ int lm_field_upload_batch(lm_ctx* c, int n_fields, const float* u, const float* 
   if ((r = dalloc(c, &tmp, 2 * chunk))) return r;
   for (size_t o = 0; o < n; o += chunk) {
     const size_t m = std::min(chunk, n - o);
-    CK(cudaMemcpyAsync(tmp, u + o, m * sizeof(float), cudaMemcpyHostToDevice, c->st));
-    CK(cudaMemcpyAsync(tmp + chunk, v + o, m * sizeof(float), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(tmp, u + o, m * sizeof(float), cudaMemcpyDefault, c->st));
+    CK(cudaMemcpyAsync(tmp + chunk, v + o, m * sizeof(float), cudaMemcpyDefault, c->st));
     launch_interleave(tmp, tmp + chunk, c->uv + o, m, c->st);
   }
   CK(cudaGetLastError());
@@ -764,21 +754,7 @@ int lm_field_upload_batch(lm_ctx* c, int n_fields, const float* u, const float* 
   }
   c->org_lon = new_org_lon;
   c->org_lat = new_org_lat;
-  FieldView& f = c->fv;
-  f.uv = c->uv;
-  f.nx = nx;
-  f.ny = ny;
-  f.nt = nt;
-  f.gx0 = (float)(lon[0] - c->org_lon);
-  f.gy0 = (float)(lat[0] - c->org_lat);
-  f.inv_dx = (float)(1.0 / dx);
-  f.inv_dy = (float)(1.0 / dy);
-  f.max_fx = (float)(nx - 1);
-  f.max_fy = (float)(ny - 1);
-  f.org_lon = (float)c->org_lon;
-  f.org_lat = (float)c->org_lat;
-  f.t0 = t_sec[0];
-  f.dT = dT;
+  fill_field_view(c->fv, c->uv, nt, ny, nx, lon, lat, t_sec, dx, dy, dT);
   c->has_field = true;
   if (c->n_ens) return upload_ens(c);
   return LM_OK;
@@ -1193,4 +1169,38 @@ int lm_profile_count(void) { return P_COUNT; }
 
 namespace lm {
 void set_thread_error(const char* msg) { g_create_error = msg ? msg : ""; }
+int ctx_device(const lm_ctx* c) { return c->device; }
+int ctx_sms(const lm_ctx* c) { return c->sms; }
+cudaStream_t ctx_stream(const lm_ctx* c) { return c->st; }
+void ctx_set_error(lm_ctx* c, const char* msg) { c->err = msg ? msg : ""; }
+
+bool uniform_axis(const double* a, int n, double* d) {
+  if (n < 2) return false;
+  const double step = (a[n - 1] - a[0]) / (n - 1);
+  if (!(step > 0) || !std::isfinite(step)) return false;
+  for (int k = 0; k < n; ++k)
+    if (std::fabs(a[k] - (a[0] + step * k)) > 1e-6 * step) return false;
+  *d = step;
+  return true;
+}
+
+// Offsets are taken from the float32 origin (lon[0], lat[0]) of the grid.
+void fill_field_view(FieldView& f, float2* uv, int nt, int ny, int nx, const double* lon, const double* lat,
+                     const double* t_sec, double dx, double dy, double dT) {
+  const double org_lon = (double)(float)lon[0], org_lat = (double)(float)lat[0];
+  f.uv = uv;
+  f.nx = nx;
+  f.ny = ny;
+  f.nt = nt;
+  f.gx0 = (float)(lon[0] - org_lon);
+  f.gy0 = (float)(lat[0] - org_lat);
+  f.inv_dx = (float)(1.0 / dx);
+  f.inv_dy = (float)(1.0 / dy);
+  f.max_fx = (float)(nx - 1);
+  f.max_fy = (float)(ny - 1);
+  f.org_lon = (float)org_lon;
+  f.org_lat = (float)org_lat;
+  f.t0 = t_sec[0];
+  f.dT = dT;
+}
 }  // namespace lm

@@ -21,6 +21,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+struct lm_ctx;
+
 namespace lm {
 
 constexpr uint32_t NONE = 0xffffffffu;
@@ -187,8 +189,59 @@ void launch_census(const Bufs& b, Ctrl* ctrl, cudaStream_t st);
 void launch_unpad(const float* src, float* dst, const int32_t* map, uint32_t nslots, cudaStream_t st);
 void launch_unpad8(const int8_t* src, int8_t* dst, const int32_t* map, uint32_t nslots, cudaStream_t st);
 
+// ---- K6/K7 adjoint of the advection (k_adjoint.cu) ----
+// Stage brackets of one step: frames k[g] and weights w[g] of the stage times t, t + dt/2, t + dt.
+struct AdjStep {
+  int k[3];
+  float w[3];
+};
+constexpr int RS_BITS_MAX = 10;                      // digit width of one radix pass
+constexpr uint32_t RS_RADIX_MAX = 1u << RS_BITS_MAX;
+
+struct AdjSortBufs {
+  const uint32_t* key;      // input keys (m)
+  uint32_t *k1, *k2;        // ping-pong keys (m)
+  uint32_t *v1, *v2;        // ping-pong record ids (m)
+  uint32_t *hist, *hscan;   // adj_sort_hist_len(m)
+  uint32_t* bsum;           // SCAN_BLOCKS
+};
+
+void launch_adj_stages(const FieldView& f, double t_start, double dt, int n_steps, AdjStep* table, uint32_t* err,
+                       cudaStream_t st);
+void launch_adj_init(const FieldView& f, uint32_t n, const float* lon, const float* lat, float* x, float* y,
+                     uint8_t* status, cudaStream_t st);
+void launch_adj_final(const FieldView& f, uint32_t n, const float* x, const float* y, float* lon, float* lat,
+                      cudaStream_t st);
+void launch_adj_forward(const FieldView& f, const AdjStep* table, int m0, int m1, float dt, uint32_t n, float* x,
+                        float* y, uint8_t* status, float* rec_x, float* rec_y, uint8_t* rec_st, uint32_t* err,
+                        cudaStream_t st);
+void launch_adj_step(const FieldView& f, const AdjStep& s, float dt, uint32_t n, const float* x, const float* y,
+                     const uint8_t* status, float* lx, float* ly, float4* rec, uint32_t* key, uint32_t sent,
+                     cudaStream_t st);
+void launch_adj_signature(const FieldView& f, const AdjStep* table, int n_steps, float dt, uint32_t n, const float* x,
+                          const float* y, const uint8_t* status, unsigned long long* sig, cudaStream_t st);
+size_t adj_sort_hist_len(uint32_t m);
+// Stable sort of m keys of key_bits bits; returns the sorted keys and the record ids (input index).
+void adj_sort(const AdjSortBufs& sb, uint32_t m, int key_bits, cudaStream_t st, const uint32_t** skey,
+              const uint32_t** sval);
+void launch_adj_bounds(const uint32_t* skey, uint32_t m, uint32_t sent, uint32_t* cst, uint32_t* cen,
+                       cudaStream_t st);
+void launch_adj_reduce(uint32_t ncells, uint32_t* cst, uint32_t* cen, const uint32_t* sval, const float4* rec,
+                       float* csum, int sms, cudaStream_t st);
+void launch_adj_nodes(int nx, int ny, const AdjStep& s, const float* csum, float* gu, float* gv, cudaStream_t st);
+
+// Field geometry from uniform axes (shared by lm_field_upload_batch and the adjoint tape).
+bool uniform_axis(const double* a, int n, double* d);
+void fill_field_view(FieldView& f, float2* uv, int nt, int ny, int nx, const double* lon, const double* lat,
+                     const double* t_sec, double dx, double dy, double dT);
+
 // Message for lm_last_error(NULL, ...) from entry points that have no context.
 void set_thread_error(const char* msg);
+// Context accessors for translation units other than lm_api.cu.
+int ctx_device(const lm_ctx* c);
+int ctx_sms(const lm_ctx* c);
+cudaStream_t ctx_stream(const lm_ctx* c);
+void ctx_set_error(lm_ctx* c, const char* msg);
 
 // Ordered-int encoding of floats for atomicMin/atomicMax.
 __host__ __device__ inline uint32_t enc_f(float f) {

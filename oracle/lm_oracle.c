@@ -10,7 +10,12 @@
  *       converted with u / (1852*60*cos(lat)), v / (1852*60). Parcels itself (2.0.0beta2) is not
  *       vendored; the scheme is restated from its documented kernel and interpolation.
  *       f64 = accuracy oracle; f32 = the Parcels-JIT-like float32 loop used as the CPU baseline,
- *       split into contiguous tiles over threads like particle_advecter.py:38-66,146.
+ *       split into contiguous tiles over threads like particle_advecter.py:38-66,146;
+ *       orc_advect_f64d = the f64 scheme on a float64 field, the forward of the adjoint's central
+ *       finite differences (no reference counterpart: the reference does not differentiate); it
+ *       can fold the grid cells of every stage evaluation into a per-particle signature, so that a
+ *       difference quotient whose two runs sample different cells (straddling an edge of the
+ *       piecewise-bilinear field, where the derivative jumps) is recognised and left out.
  *   orc_pairs        : cKDTree(X).query_pairs(r, p) (interaction_simulator.py:93-98): all i < j with
  *       Minkowski-p distance <= r on float32 positions promoted to float64; for p = 2 the test is
  *       fl(fl(dx*dx) + fl(dy*dy)) <= fl(r*r) (no FMA; this file must be compiled with
@@ -174,6 +179,72 @@ int64_t orc_advect_f64(const orc_field* f, int64_t n, double* lon, double* lat, 
       }
       if (rec_lon) rec_lon[(size_t)s * n + p] = lon[p];
       if (rec_lat) rec_lat[(size_t)s * n + p] = lat[p];
+    }
+  }
+  return bad;
+}
+
+/* The same FP64 scheme on an FP64 field (finite differences along u, v directions need
+ * perturbations far below float32 resolution). Stage brackets as bracket(); one thread per particle. */
+static int vel64d(const orc_field64* f, int k, double w, double x, double y, double* dlon, double* dlat,
+                  uint64_t* sig) {
+  double fx = (x - f->lon0) / f->dlon, fy = (y - f->lat0) / f->dlat;
+  if (!(fx >= 0 && fx <= f->nx - 1 && fy >= 0 && fy <= f->ny - 1)) return 0;
+  int i = (int)fx, j = (int)fy;
+  if (i > f->nx - 2) i = f->nx - 2;
+  if (j > f->ny - 2) j = f->ny - 2;
+  *sig = (*sig ^ (uint64_t)((int64_t)j * f->nx + i)) * 0x100000001B3ull; /* FNV-style fold of the cell path */
+  double a = fx - i, b = fy - j;
+  double w00 = (1 - a) * (1 - b), w01 = a * (1 - b), w10 = (1 - a) * b, w11 = a * b;
+  size_t base = ((size_t)k * f->ny + j) * f->nx + i;
+  size_t nxny = (size_t)f->nx * f->ny;
+  double u = 0, v = 0;
+  for (int fr = 0; fr < 2; ++fr) {
+    double wt = fr == 0 ? 1.0 - w : w;
+    if (wt == 0.0) continue;
+    size_t q = base + fr * nxny;
+    u += wt * (w00 * f->u[q] + w01 * f->u[q + 1] + w10 * f->u[q + f->nx] + w11 * f->u[q + f->nx + 1]);
+    v += wt * (w00 * f->v[q] + w01 * f->v[q + 1] + w10 * f->v[q + f->nx] + w11 * f->v[q + f->nx + 1]);
+  }
+  *dlon = u / (1852.0 * 60.0 * cos(y * M_PI / 180.0));
+  *dlat = v / (1852.0 * 60.0);
+  return 1;
+}
+
+int64_t orc_advect_f64d(const orc_field64* f, int64_t n, double* lon, double* lat, uint8_t* status, double t0,
+                        double dt, int n_steps, int n_threads, uint64_t* cell_sig) {
+  const orc_field fk = {NULL, NULL, f->nx, f->ny, f->nt, f->lon0, f->dlon, f->lat0, f->dlat, f->t0, f->dT};
+  int64_t bad = 0;
+#ifdef _OPENMP
+  if (n_threads > 0) omp_set_num_threads(n_threads);
+#else
+  (void)n_threads;
+#endif
+  for (int s = 0; s < n_steps; ++s) {
+    double t = t0 + dt * s;
+    int k[3];
+    double w[3];
+    if (!bracket(&fk, t, &k[0], &w[0]) || !bracket(&fk, t + 0.5 * dt, &k[1], &w[1]) ||
+        !bracket(&fk, t + dt, &k[2], &w[2]))
+      return -1;
+#pragma omp parallel for schedule(static) reduction(+ : bad)
+    for (int64_t p = 0; p < n; ++p) {
+      if (status[p]) continue;
+      double x = lon[p], y = lat[p];
+      double k1x, k1y, k2x, k2y, k3x, k3y, k4x, k4y;
+      uint64_t sg = cell_sig ? cell_sig[p] : 0;
+      int ok = vel64d(f, k[0], w[0], x, y, &k1x, &k1y, &sg) &&
+               vel64d(f, k[1], w[1], x + 0.5 * dt * k1x, y + 0.5 * dt * k1y, &k2x, &k2y, &sg) &&
+               vel64d(f, k[1], w[1], x + 0.5 * dt * k2x, y + 0.5 * dt * k2y, &k3x, &k3y, &sg) &&
+               vel64d(f, k[2], w[2], x + dt * k3x, y + dt * k3y, &k4x, &k4y, &sg);
+      if (cell_sig) cell_sig[p] = sg;
+      if (ok) {
+        lon[p] = x + (k1x + 2 * k2x + 2 * k3x + k4x) * dt / 6.0;
+        lat[p] = y + (k1y + 2 * k2y + 2 * k3y + k4y) * dt / 6.0;
+      } else {
+        status[p] = 1;
+        bad += 1;
+      }
     }
   }
   return bad;

@@ -16,6 +16,14 @@ typedef struct orc_field {
   double lon0, dlon, lat0, dlat, t0, dT;
 } orc_field;
 
+/* The same field with float64 u, v (finite differences of the adjoint). */
+typedef struct orc_field64 {
+  const double* u;
+  const double* v;
+  int nx, ny, nt;
+  double lon0, dlon, lat0, dlat, t0, dT;
+} orc_field64;
+
 void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 void orc_pair_draw(uint32_t i, uint32_t j, uint32_t step, uint64_t seed, uint64_t* u53, uint64_t* prio);
 void orc_diffusion_draw(uint32_t p, uint32_t step, uint64_t seed, float* ulat, float* ulon);
@@ -23,6 +31,8 @@ uint64_t orc_prob_threshold(double p);
 
 int64_t orc_advect_f64(const orc_field* f, int64_t n, double* lon, double* lat, uint8_t* status, double t0,
                        double dt, int n_steps, double* rec_lon, double* rec_lat);
+int64_t orc_advect_f64d(const orc_field64* f, int64_t n, double* lon, double* lat, uint8_t* status, double t0,
+                        double dt, int n_steps, int n_threads, uint64_t* cell_sig);
 int64_t orc_advect_f32(const orc_field* f, int64_t n, float* lon, float* lat, uint8_t* status, double t0, double dt,
                        int n_steps, int n_threads);
 
