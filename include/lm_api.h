@@ -212,6 +212,13 @@ int lm_count_pairs_noalloc(const float* d_lon, const float* d_lat, int64_t n, do
 typedef struct lm_adjoint lm_adjoint;
 int lm_adjoint_create(lm_ctx* ctx, lm_adjoint** out);
 int lm_adjoint_destroy(lm_adjoint* adj);
+/* Working precision of the next lm_adjoint_forward. LM_ADJ_F32 (default): float32 state with the
+ * engine's arithmetic, final positions bit-identical to lm_step's. LM_ADJ_F64: float64 state and
+ * arithmetic (the field stays float32); on long chaotic runs its trajectories, and so its
+ * gradients, stay close to an FP64 reference where float32 rounding has been amplified. */
+#define LM_ADJ_F32 0
+#define LM_ADJ_F64 1
+int lm_adjoint_set_precision(lm_adjoint* adj, int precision);
 /* u, v [nt][ny][nx] m/s and the axes as lm_field_upload (axes are host arrays); n microbes from
  * lon0/lat0 (absolute degrees) for n_steps steps of dt_sec from t_sec0; final positions into
  * lon_out/lat_out. Microbes leaving the domain are frozen (LM_ERR_OUT_OF_BOUNDS is returned, the tape is
@@ -224,6 +231,9 @@ int lm_adjoint_forward(lm_adjoint* adj, const float* u, const float* v, int nt, 
  * May be called several times after one forward. */
 int lm_adjoint_backward(lm_adjoint* adj, const float* g_lon, const float* g_lat, float* g_lon0, float* g_lat0,
                         float* g_u, float* g_v);
+/* Final positions of the recorded run in float64 (device double [n] each, absolute degrees): the
+ * working state rounded only once, for losses that need more than float32 positions. */
+int lm_adjoint_final_positions(lm_adjoint* adj, double* lon, double* lat);
 /* Cell path of every microbe of the recorded run (device uint64 [n]): the grid cell j * nx + i of
  * every stage evaluation, folded in order as sig = (sig ^ cell) * 0x100000001B3. The forward map
  * is piecewise smooth (bilinear pieces meet at cell edges); two runs whose signatures agree

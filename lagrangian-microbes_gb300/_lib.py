@@ -124,9 +124,11 @@ SIGNATURES = {
     "lm_count_pairs_noalloc": [P, P, I64, F64, I32, P, P, ctypes.c_size_t],
     "lm_adjoint_create": [P, ctypes.POINTER(P)],
     "lm_adjoint_destroy": [P],
+    "lm_adjoint_set_precision": [P, I32],
     "lm_adjoint_forward": [P, P, P, I32, I32, I32, P, P, P, I64, P, P, F64, F64, I32, I32, P, P],
     "lm_adjoint_backward": [P, P, P, P, P, P, P],
     "lm_adjoint_cell_signature": [P, P],
+    "lm_adjoint_final_positions": [P, P, P],
 }
 
 

@@ -26,15 +26,29 @@ from . import _lib
 EARTH_RADIUS_M = 6371.228e3
 
 
-class AdjointTape:
-    """One lm_adjoint tape: the recorded forward run and its backward sweep."""
+PRECISIONS = {"f32": 0, "f64": 1}
 
-    def __init__(self, ctx: _lib.Context | None = None, device: int = 0):
+
+class AdjointTape:
+    """One lm_adjoint tape: the recorded forward run and its backward sweep.
+
+    ``precision="f32"`` keeps float32 state with the engine's arithmetic (final positions
+    bit-identical to the fused engine's advection); ``"f64"`` carries float64 state and arithmetic
+    over the float32 field, for long runs where float32 rounding, amplified by the flow, moves
+    trajectories across cell edges of the piecewise-bilinear field. In "f64" mode the final
+    positions come back as float64 tensors.
+    """
+
+    def __init__(self, ctx: _lib.Context | None = None, device: int = 0, precision: str = "f32"):
+        if precision not in PRECISIONS:
+            raise ValueError(f"precision must be one of {sorted(PRECISIONS)}; got {precision!r}")
         self.ctx = ctx or _lib.Context(device)
         self._lib = self.ctx._lib
         h = ctypes.c_void_p()
         self.ctx.check(self._lib.lm_adjoint_create(self.ctx.handle, ctypes.byref(h)))
         self._h = h
+        self.precision = precision
+        self.ctx.check(self._lib.lm_adjoint_set_precision(self._h, PRECISIONS[precision]))
         self.n = 0
         self.field_shape = None
 
@@ -67,6 +81,10 @@ class AdjointTape:
             self.ctx.check(rc)
         self.n = n
         self.field_shape = (nt, ny, nx)
+        if self.precision == "f64":  # hand back the float64 state, rounded once
+            lon = torch.empty(n, dtype=torch.float64, device=lon0.device)
+            lat = torch.empty_like(lon)
+            self.ctx.check(self._lib.lm_adjoint_final_positions(self._h, lon.data_ptr(), lat.data_ptr()))
         return lon, lat
 
     def backward(self, g_lon, g_lat):
@@ -121,9 +139,10 @@ class _AdvectRK4(torch.autograd.Function):
 
 
 def advect_rk4(lon0, lat0, u, v, lon_axis, lat_axis, t_axis, t0: float, dt: float, n_steps: int,
-               checkpoint_every: int = 32, tape: AdjointTape | None = None, allow_out_of_bounds: bool = False):
+               checkpoint_every: int = 32, tape: AdjointTape | None = None, allow_out_of_bounds: bool = False,
+               precision: str = "f32"):
     """Differentiable RK4 advection (float32 CUDA tensors in and out); see the module docstring."""
-    tape = tape or AdjointTape(device=lon0.device.index or 0)
+    tape = tape or AdjointTape(device=lon0.device.index or 0, precision=precision)
     return _AdvectRK4.apply(lon0, lat0, u, v, tape, (lon_axis, lat_axis, t_axis), float(t0), float(dt),
                             int(n_steps), int(checkpoint_every), bool(allow_out_of_bounds))
 

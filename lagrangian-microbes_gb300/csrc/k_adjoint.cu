@@ -36,41 +36,194 @@ __global__ void k_adj_stages(FieldView f, double t_start, double dt, int n_steps
     const Stage sg = stage_at(f, ts[k]);
     s.k[k] = sg.k;
     s.w[k] = sg.w;
+    // the float64 weight of the same bracket (stage_at rounds it to float32)
+    const double fk = (ts[k] - f.t0) / f.dT;
+    s.wd[k] = sg.w == 0.f ? 0.0 : fmin(fmax(fk - (double)sg.k, 0.0), 1.0);
     ok = ok && sg.ok;
   }
   table[m] = s;
   if (!ok) atomicOr(err, (uint32_t)ERRB_TIME);
 }
 
-// Absolute float32 positions -> offsets from the field origin (exact in float64), status.
+// Geometry of the offset frame in the working precision T. The float32 instance is the forward
+// engine's (FieldView's float fields); the float64 one is the same grid in float64.
+template <class T>
+struct Geo;
+template <>
+struct Geo<float> {
+  float gx0, gy0, inv_dx, inv_dy, max_fx, max_fy, org_lat;
+  __device__ explicit Geo(const FieldView& f)
+      : gx0(f.gx0), gy0(f.gy0), inv_dx(f.inv_dx), inv_dy(f.inv_dy), max_fx(f.max_fx), max_fy(f.max_fy),
+        org_lat(f.org_lat) {}
+};
+template <>
+struct Geo<double> {
+  double gx0, gy0, inv_dx, inv_dy, max_fx, max_fy, org_lat;
+  __device__ explicit Geo(const FieldView& f)
+      : gx0(f.gx0d), gy0(f.gy0d), inv_dx(f.inv_dxd), inv_dy(f.inv_dyd), max_fx(f.max_fx), max_fy(f.max_fy),
+        org_lat((double)f.org_lat) {}
+};
+__device__ __forceinline__ float cospi_t(float x) { return cospif(x); }
+__device__ __forceinline__ double cospi_t(double x) { return cospi(x); }
+__device__ __forceinline__ float sinpi_t(float x) { return sinpif(x); }
+__device__ __forceinline__ double sinpi_t(double x) { return sinpi(x); }
+template <class T>
+__device__ __forceinline__ T stage_w(const AdjStep& s, int g);
+template <>
+__device__ __forceinline__ float stage_w<float>(const AdjStep& s, int g) { return s.w[g]; }
+template <>
+__device__ __forceinline__ double stage_w<double>(const AdjStep& s, int g) { return s.wd[g]; }
+
+// Absolute float32 positions -> offsets from the field's float32 origin (exact in float64), status.
+template <class T>
 __global__ void k_adj_init(FieldView f, uint32_t n, const float* __restrict__ lon, const float* __restrict__ lat,
-                           float* __restrict__ x, float* __restrict__ y, uint8_t* __restrict__ st) {
+                           T* __restrict__ x, T* __restrict__ y, uint8_t* __restrict__ st) {
   const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
   const float a = lon[p], b = lat[p];
-  x[p] = (float)((double)a - (double)f.org_lon);
-  y[p] = (float)((double)b - (double)f.org_lat);
+  x[p] = (T)((double)a - (double)f.org_lon);
+  y[p] = (T)((double)b - (double)f.org_lat);
   st[p] = (isfinite(a) && isfinite(b)) ? STATUS_OK : STATUS_NAN;
 }
 
-__global__ void k_adj_final(FieldView f, uint32_t n, const float* __restrict__ x, const float* __restrict__ y,
+template <class T>
+__global__ void k_adj_final(FieldView f, uint32_t n, const T* __restrict__ x, const T* __restrict__ y,
                             float* __restrict__ lon, float* __restrict__ lat) {
   const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
-  lon[p] = __fadd_rn(f.org_lon, x[p]);
-  lat[p] = __fadd_rn(f.org_lat, y[p]);
+  if (sizeof(T) == sizeof(float)) {  // the engine's rounding of the recorded position
+    lon[p] = __fadd_rn(f.org_lon, (float)x[p]);
+    lat[p] = __fadd_rn(f.org_lat, (float)y[p]);
+  } else {
+    lon[p] = (float)((double)f.org_lon + (double)x[p]);
+    lat[p] = (float)((double)f.org_lat + (double)y[p]);
+  }
 }
 
-// Steps [m0, m1) of every microbe in registers, the forward's arithmetic and freezing rules. With
-// rec_* set, the state before every step is stored ([m - m0][n]) for the backward sweep.
-__global__ void __launch_bounds__(256) k_adj_forward(FieldView f, const AdjStep* __restrict__ table, int m0, int m1,
-                                                     float dt, uint32_t n, float* __restrict__ xs,
-                                                     float* __restrict__ ys, uint8_t* __restrict__ sts,
-                                                     float* __restrict__ rec_x, float* __restrict__ rec_y,
-                                                     uint8_t* __restrict__ rec_st, uint32_t* err) {
+// Final positions in float64 (absolute degrees) from the T-typed state.
+template <class T>
+__global__ void k_adj_final64(FieldView f, uint32_t n, const T* __restrict__ x, const T* __restrict__ y,
+                              double* __restrict__ lon, double* __restrict__ lat) {
   const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
-  float x = xs[p], y = ys[p];
+  lon[p] = (double)f.org_lon + (double)x[p];
+  lat[p] = (double)f.org_lat + (double)y[p];
+}
+
+// dL/dx of the final positions (float32) into the T-typed adjoint state, and back out at the end.
+template <class T>
+__global__ void k_adj_convert_in(uint32_t n, const float* __restrict__ gx, const float* __restrict__ gy,
+                                 T* __restrict__ lx, T* __restrict__ ly) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  lx[p] = (T)gx[p];
+  ly[p] = (T)gy[p];
+}
+template <class T>
+__global__ void k_adj_convert_out(uint32_t n, const T* __restrict__ lx, const T* __restrict__ ly,
+                                  float* __restrict__ gx, float* __restrict__ gy) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  gx[p] = (float)lx[p];
+  gy[p] = (float)ly[p];
+}
+
+// ---------------------------------------------------------------- K6: one backward step
+
+// Velocity and its Jacobian w.r.t. the offset position. For T = float the value is computed with
+// exactly the arithmetic of velocity() so that the recomputed stage positions are the forward's.
+template <class T>
+struct VelJac {
+  T flon, flat;                          // deg/s
+  T dlon_dx, dlon_dy, dlat_dx, dlat_dy;  // 1/s
+  uint32_t cell;                         // j * (nx - 1) + i
+  T a, b;                                // bilinear fractions
+  T inv_mc;                              // d flon / d U = 1 / (M cos lat)
+};
+
+template <class T>
+__device__ __forceinline__ bool vel_jac(const FieldView& f, const Geo<T>& g, int k, T w, T xo, T yo, VelJac<T>& r) {
+  const T fx = (xo - g.gx0) * g.inv_dx;
+  const T fy = (yo - g.gy0) * g.inv_dy;
+  if (!(fx >= T(0) && fx <= g.max_fx && fy >= T(0) && fy <= g.max_fy)) return false;
+  const int i = min((int)fx, f.nx - 2);
+  const int j = min((int)fy, f.ny - 2);
+  const T a = fx - (T)i, b = fy - (T)j;
+  const float2* p = f.uv + ((size_t)k * f.ny + j) * f.nx + i;
+  float2 q00 = __ldg(p), q01 = __ldg(p + 1), q10 = __ldg(p + f.nx), q11 = __ldg(p + f.nx + 1);
+  const T w00 = (T(1) - a) * (T(1) - b), w01 = a * (T(1) - b), w10 = (T(1) - a) * b, w11 = a * b;
+  T u = w00 * (T)q00.x + w01 * (T)q01.x + w10 * (T)q10.x + w11 * (T)q11.x;
+  T v = w00 * (T)q00.y + w01 * (T)q01.y + w10 * (T)q10.y + w11 * (T)q11.y;
+  T ua = (T(1) - b) * ((T)q01.x - (T)q00.x) + b * ((T)q11.x - (T)q10.x);
+  T ub = (T(1) - a) * ((T)q10.x - (T)q00.x) + a * ((T)q11.x - (T)q01.x);
+  T va = (T(1) - b) * ((T)q01.y - (T)q00.y) + b * ((T)q11.y - (T)q10.y);
+  T vb = (T(1) - a) * ((T)q10.y - (T)q00.y) + a * ((T)q11.y - (T)q01.y);
+  if (w != T(0)) {
+    p += (size_t)f.nx * f.ny;
+    q00 = __ldg(p); q01 = __ldg(p + 1); q10 = __ldg(p + f.nx); q11 = __ldg(p + f.nx + 1);
+    const T u1 = w00 * (T)q00.x + w01 * (T)q01.x + w10 * (T)q10.x + w11 * (T)q11.x;
+    const T v1 = w00 * (T)q00.y + w01 * (T)q01.y + w10 * (T)q10.y + w11 * (T)q11.y;
+    u = u + w * (u1 - u);
+    v = v + w * (v1 - v);
+    ua = ua + w * (((T(1) - b) * ((T)q01.x - (T)q00.x) + b * ((T)q11.x - (T)q10.x)) - ua);
+    ub = ub + w * (((T(1) - a) * ((T)q10.x - (T)q00.x) + a * ((T)q11.x - (T)q01.x)) - ub);
+    va = va + w * (((T(1) - b) * ((T)q01.y - (T)q00.y) + b * ((T)q11.y - (T)q10.y)) - va);
+    vb = vb + w * (((T(1) - a) * ((T)q10.y - (T)q00.y) + a * ((T)q11.y - (T)q01.y)) - vb);
+  }
+  const T lat = g.org_lat + yo;
+  const T c = cospi_t(lat * (T(1) / T(180)));
+  const T sn = sinpi_t(lat * (T(1) / T(180)));
+  const T M = (T)M_PER_DEG;
+  r.flon = u / (M * c);
+  r.flat = v * (T(1) / M);
+  r.inv_mc = T(1) / (M * c);
+  // d/dlat (1 / cos(lat)) = tan(lat) / cos(lat) * pi / 180 per degree
+  r.dlon_dx = ua * g.inv_dx * r.inv_mc;
+  r.dlon_dy = ub * g.inv_dy * r.inv_mc + r.flon * (sn / c) * (T)0.017453292519943295;
+  r.dlat_dx = va * g.inv_dx * (T(1) / M);
+  r.dlat_dy = vb * g.inv_dy * (T(1) / M);
+  r.cell = (uint32_t)j * (uint32_t)(f.nx - 1) + (uint32_t)i;
+  r.a = a;
+  r.b = b;
+  return true;
+}
+
+// One RK4 step in precision T. For T = float it is rk4_step, the engine's own arithmetic.
+template <class T>
+__device__ __forceinline__ bool rk4_t(const FieldView& f, const Geo<T>& g, const AdjStep& s, T dt, T x, T y, T& nx,
+                                      T& ny);
+template <>
+__device__ __forceinline__ bool rk4_t<float>(const FieldView& f, const Geo<float>&, const AdjStep& s, float dt, float x,
+                                             float y, float& nx, float& ny) {
+  const Stage sh[3] = {{s.k[0], s.w[0], 1}, {s.k[1], s.w[1], 1}, {s.k[2], s.w[2], 1}};
+  return rk4_step(f, f.uv, sh, dt, x, y, nx, ny);
+}
+template <>
+__device__ __forceinline__ bool rk4_t<double>(const FieldView& f, const Geo<double>& g, const AdjStep& s, double dt,
+                                              double x, double y, double& nx, double& ny) {
+  VelJac<double> J1, J2, J3, J4;
+  bool ok = vel_jac(f, g, s.k[0], s.wd[0], x, y, J1);
+  ok = ok && vel_jac(f, g, s.k[1], s.wd[1], x + 0.5 * dt * J1.flon, y + 0.5 * dt * J1.flat, J2);
+  ok = ok && vel_jac(f, g, s.k[1], s.wd[1], x + 0.5 * dt * J2.flon, y + 0.5 * dt * J2.flat, J3);
+  ok = ok && vel_jac(f, g, s.k[2], s.wd[2], x + dt * J3.flon, y + dt * J3.flat, J4);
+  if (!ok) return false;
+  nx = x + (J1.flon + 2.0 * J2.flon + 2.0 * J3.flon + J4.flon) * (dt * (1.0 / 6.0));
+  ny = y + (J1.flat + 2.0 * J2.flat + 2.0 * J3.flat + J4.flat) * (dt * (1.0 / 6.0));
+  return true;
+}
+
+// Steps [m0, m1) of every microbe in registers, the forward's freezing rules. With rec_* set, the
+// state before every step is stored ([m - m0][n]) for the backward sweep.
+template <class T>
+__global__ void __launch_bounds__(256) k_adj_forward(FieldView f, const AdjStep* __restrict__ table, int m0, int m1,
+                                                     T dt, uint32_t n, T* __restrict__ xs, T* __restrict__ ys,
+                                                     uint8_t* __restrict__ sts, T* __restrict__ rec_x,
+                                                     T* __restrict__ rec_y, uint8_t* __restrict__ rec_st,
+                                                     uint32_t* err) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const Geo<T> g(f);
+  T x = xs[p], y = ys[p];
   uint8_t st = sts[p];
   uint32_t bits = 0;
   for (int m = m0; m < m1; ++m) {
@@ -82,9 +235,8 @@ __global__ void __launch_bounds__(256) k_adj_forward(FieldView f, const AdjStep*
     }
     if (st != STATUS_OK) continue;
     const AdjStep s = table[m];
-    const Stage sh[3] = {{s.k[0], s.w[0], 1}, {s.k[1], s.w[1], 1}, {s.k[2], s.w[2], 1}};
-    float nx, ny;
-    if (rk4_step(f, f.uv, sh, dt, x, y, nx, ny)) {
+    T nx, ny;
+    if (rk4_t<T>(f, g, s, dt, x, y, nx, ny)) {
       if (isfinite(nx) && isfinite(ny)) {
         x = nx;
         y = ny;
@@ -103,82 +255,26 @@ __global__ void __launch_bounds__(256) k_adj_forward(FieldView f, const AdjStep*
   if (bits) atomicOr(err, bits);
 }
 
-// ---------------------------------------------------------------- K6: one backward step
-
-// Velocity and its Jacobian w.r.t. the offset position; the value is computed with exactly the
-// arithmetic of velocity() so that the recomputed stage positions are the forward's.
-struct VelJac {
-  float flon, flat;                          // deg/s
-  float dlon_dx, dlon_dy, dlat_dx, dlat_dy;  // 1/s
-  uint32_t cell;                             // j * (nx - 1) + i
-  float a, b;                                // bilinear fractions
-  float inv_mc;                              // d flon / d U = 1 / (M cos lat)
-};
-
-__device__ __forceinline__ bool vel_jac(const FieldView& f, const Stage& s, float xo, float yo, VelJac& r) {
-  const float fx = (xo - f.gx0) * f.inv_dx;
-  const float fy = (yo - f.gy0) * f.inv_dy;
-  if (!(fx >= 0.f && fx <= f.max_fx && fy >= 0.f && fy <= f.max_fy)) return false;
-  const int i = min((int)fx, f.nx - 2);
-  const int j = min((int)fy, f.ny - 2);
-  const float a = fx - (float)i, b = fy - (float)j;
-  const float2* p = f.uv + ((size_t)s.k * f.ny + j) * f.nx + i;
-  float2 c00 = __ldg(p), c01 = __ldg(p + 1), c10 = __ldg(p + f.nx), c11 = __ldg(p + f.nx + 1);
-  const float w00 = (1.f - a) * (1.f - b), w01 = a * (1.f - b), w10 = (1.f - a) * b, w11 = a * b;
-  float u = w00 * c00.x + w01 * c01.x + w10 * c10.x + w11 * c11.x;
-  float v = w00 * c00.y + w01 * c01.y + w10 * c10.y + w11 * c11.y;
-  float ua = (1.f - b) * (c01.x - c00.x) + b * (c11.x - c10.x);
-  float ub = (1.f - a) * (c10.x - c00.x) + a * (c11.x - c01.x);
-  float va = (1.f - b) * (c01.y - c00.y) + b * (c11.y - c10.y);
-  float vb = (1.f - a) * (c10.y - c00.y) + a * (c11.y - c01.y);
-  if (s.w != 0.f) {
-    p += (size_t)f.nx * f.ny;
-    c00 = __ldg(p); c01 = __ldg(p + 1); c10 = __ldg(p + f.nx); c11 = __ldg(p + f.nx + 1);
-    const float u1 = w00 * c00.x + w01 * c01.x + w10 * c10.x + w11 * c11.x;
-    const float v1 = w00 * c00.y + w01 * c01.y + w10 * c10.y + w11 * c11.y;
-    u = u + s.w * (u1 - u);
-    v = v + s.w * (v1 - v);
-    ua = ua + s.w * (((1.f - b) * (c01.x - c00.x) + b * (c11.x - c10.x)) - ua);
-    ub = ub + s.w * (((1.f - a) * (c10.x - c00.x) + a * (c11.x - c01.x)) - ub);
-    va = va + s.w * (((1.f - b) * (c01.y - c00.y) + b * (c11.y - c10.y)) - va);
-    vb = vb + s.w * (((1.f - a) * (c10.y - c00.y) + a * (c11.y - c01.y)) - vb);
-  }
-  const float lat = f.org_lat + yo;
-  const float c = cospif(lat * (1.0f / 180.0f));
-  const float sn = sinpif(lat * (1.0f / 180.0f));
-  r.flon = u / (M_PER_DEG * c);
-  r.flat = v * (1.0f / M_PER_DEG);
-  r.inv_mc = 1.0f / (M_PER_DEG * c);
-  // d/dlat (1 / cos(lat)) = tan(lat) / cos(lat) * pi / 180 per degree
-  r.dlon_dx = ua * f.inv_dx * r.inv_mc;
-  r.dlon_dy = ub * f.inv_dy * r.inv_mc + r.flon * (sn / c) * 0.017453292519943295f;
-  r.dlat_dx = va * f.inv_dx * (1.0f / M_PER_DEG);
-  r.dlat_dy = vb * f.inv_dy * (1.0f / M_PER_DEG);
-  r.cell = (uint32_t)j * (uint32_t)(f.nx - 1) + (uint32_t)i;
-  r.a = a;
-  r.b = b;
-  return true;
-}
-
 // lambda_{m+1} -> lambda_m, plus 4 records per microbe (key = cell * 4 + stage time, or `sent`).
-__global__ void __launch_bounds__(256) k_adj_step(FieldView f, AdjStep s, float dt, uint32_t n,
-                                                  const float* __restrict__ xs, const float* __restrict__ ys,
-                                                  const uint8_t* __restrict__ sts, float* __restrict__ lx,
-                                                  float* __restrict__ ly, float4* __restrict__ rec,
+template <class T>
+__global__ void __launch_bounds__(256) k_adj_step(FieldView f, AdjStep s, T dt, uint32_t n, const T* __restrict__ xs,
+                                                  const T* __restrict__ ys, const uint8_t* __restrict__ sts,
+                                                  T* __restrict__ lx, T* __restrict__ ly, float4* __restrict__ rec,
                                                   uint32_t* __restrict__ key, uint32_t sent) {
   const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
-  const float x = xs[p], y = ys[p];
-  const Stage sh0 = {s.k[0], s.w[0], 1}, sh1 = {s.k[1], s.w[1], 1}, sh2 = {s.k[2], s.w[2], 1};
-  VelJac J1, J2, J3, J4;
+  const Geo<T> g(f);
+  const T x = xs[p], y = ys[p];
+  const T w0 = stage_w<T>(s, 0), w1 = stage_w<T>(s, 1), w2 = stage_w<T>(s, 2);
+  VelJac<T> J1, J2, J3, J4;
   bool ok = sts[p] == STATUS_OK;
-  ok = ok && vel_jac(f, sh0, x, y, J1);
-  ok = ok && vel_jac(f, sh1, x + 0.5f * dt * J1.flon, y + 0.5f * dt * J1.flat, J2);
-  ok = ok && vel_jac(f, sh1, x + 0.5f * dt * J2.flon, y + 0.5f * dt * J2.flat, J3);
-  ok = ok && vel_jac(f, sh2, x + dt * J3.flon, y + dt * J3.flat, J4);
+  ok = ok && vel_jac(f, g, s.k[0], w0, x, y, J1);
+  ok = ok && vel_jac(f, g, s.k[1], w1, x + T(0.5) * dt * J1.flon, y + T(0.5) * dt * J1.flat, J2);
+  ok = ok && vel_jac(f, g, s.k[1], w1, x + T(0.5) * dt * J2.flon, y + T(0.5) * dt * J2.flat, J3);
+  ok = ok && vel_jac(f, g, s.k[2], w2, x + dt * J3.flon, y + dt * J3.flat, J4);
   if (ok) {  // a non-finite step was frozen by the forward: identity, like a stage off the grid
-    const float nx = x + (J1.flon + 2.f * J2.flon + 2.f * J3.flon + J4.flon) * (dt * (1.0f / 6.0f));
-    const float ny = y + (J1.flat + 2.f * J2.flat + 2.f * J3.flat + J4.flat) * (dt * (1.0f / 6.0f));
+    const T nx = x + (J1.flon + T(2) * J2.flon + T(2) * J3.flon + J4.flon) * (dt * (T(1) / T(6)));
+    const T ny = y + (J1.flat + T(2) * J2.flat + T(2) * J3.flat + J4.flat) * (dt * (T(1) / T(6)));
     ok = isfinite(nx) && isfinite(ny);
   }
   uint4* kq = reinterpret_cast<uint4*>(key) + p;
@@ -186,25 +282,26 @@ __global__ void __launch_bounds__(256) k_adj_step(FieldView f, AdjStep s, float 
     *kq = make_uint4(sent, sent, sent, sent);
     return;
   }
-  const float gx = lx[p], gy = ly[p];
-  const float h6 = dt * (1.0f / 6.0f), h3 = dt * (1.0f / 3.0f), h2 = 0.5f * dt;
+  const T gx = lx[p], gy = ly[p];
+  const T h6 = dt * (T(1) / T(6)), h3 = dt * (T(1) / T(3)), h2 = T(0.5) * dt;
   // dL/dk4, then back through x3 = x + dt k3, x2 = x + dt/2 k2, x1 = x + dt/2 k1
-  const float g4x = h6 * gx, g4y = h6 * gy;
-  const float x3x = J4.dlon_dx * g4x + J4.dlat_dx * g4y, x3y = J4.dlon_dy * g4x + J4.dlat_dy * g4y;
-  const float g3x = h3 * gx + dt * x3x, g3y = h3 * gy + dt * x3y;
-  const float x2x = J3.dlon_dx * g3x + J3.dlat_dx * g3y, x2y = J3.dlon_dy * g3x + J3.dlat_dy * g3y;
-  const float g2x = h3 * gx + h2 * x2x, g2y = h3 * gy + h2 * x2y;
-  const float x1x = J2.dlon_dx * g2x + J2.dlat_dx * g2y, x1y = J2.dlon_dy * g2x + J2.dlat_dy * g2y;
-  const float g1x = h6 * gx + h2 * x1x, g1y = h6 * gy + h2 * x1y;
-  const float x0x = J1.dlon_dx * g1x + J1.dlat_dx * g1y, x0y = J1.dlon_dy * g1x + J1.dlat_dy * g1y;
+  const T g4x = h6 * gx, g4y = h6 * gy;
+  const T x3x = J4.dlon_dx * g4x + J4.dlat_dx * g4y, x3y = J4.dlon_dy * g4x + J4.dlat_dy * g4y;
+  const T g3x = h3 * gx + dt * x3x, g3y = h3 * gy + dt * x3y;
+  const T x2x = J3.dlon_dx * g3x + J3.dlat_dx * g3y, x2y = J3.dlon_dy * g3x + J3.dlat_dy * g3y;
+  const T g2x = h3 * gx + h2 * x2x, g2y = h3 * gy + h2 * x2y;
+  const T x1x = J2.dlon_dx * g2x + J2.dlat_dx * g2y, x1y = J2.dlon_dy * g2x + J2.dlat_dy * g2y;
+  const T g1x = h6 * gx + h2 * x1x, g1y = h6 * gy + h2 * x1y;
+  const T x0x = J1.dlon_dx * g1x + J1.dlat_dx * g1y, x0y = J1.dlon_dy * g1x + J1.dlat_dy * g1y;
   lx[p] = gx + ((x0x + x1x) + (x2x + x3x));
   ly[p] = gy + ((x0y + x1y) + (x2y + x3y));
-  // records: dL/dU_s = dL/dk_s,lon / (M cos lat_s), dL/dV_s = dL/dk_s,lat / M
+  // records: dL/dU_s = dL/dk_s,lon / (M cos lat_s), dL/dV_s = dL/dk_s,lat / M (float32 for the reduction)
+  const T invM = T(1) / (T)M_PER_DEG;
   float4* rq = rec + 4 * (size_t)p;
-  rq[0] = make_float4(J1.a, J1.b, g1x * J1.inv_mc, g1y * (1.0f / M_PER_DEG));
-  rq[1] = make_float4(J2.a, J2.b, g2x * J2.inv_mc, g2y * (1.0f / M_PER_DEG));
-  rq[2] = make_float4(J3.a, J3.b, g3x * J3.inv_mc, g3y * (1.0f / M_PER_DEG));
-  rq[3] = make_float4(J4.a, J4.b, g4x * J4.inv_mc, g4y * (1.0f / M_PER_DEG));
+  rq[0] = make_float4((float)J1.a, (float)J1.b, (float)(g1x * J1.inv_mc), (float)(g1y * invM));
+  rq[1] = make_float4((float)J2.a, (float)J2.b, (float)(g2x * J2.inv_mc), (float)(g2y * invM));
+  rq[2] = make_float4((float)J3.a, (float)J3.b, (float)(g3x * J3.inv_mc), (float)(g3y * invM));
+  rq[3] = make_float4((float)J4.a, (float)J4.b, (float)(g4x * J4.inv_mc), (float)(g4y * invM));
   *kq = make_uint4(4u * J1.cell + 0u, 4u * J2.cell + 1u, 4u * J3.cell + 1u, 4u * J4.cell + 2u);
 }
 
@@ -212,42 +309,41 @@ __global__ void __launch_bounds__(256) k_adj_step(FieldView f, AdjStep s, float 
 // the forward evaluated, folded in order as sig = (sig ^ cell) * 0x100000001B3. The stage
 // positions come from vel_jac, whose values are the forward's; two runs of one microbe with equal
 // signatures sampled the same bilinear pieces, so the map between them is smooth.
+template <class T>
 __global__ void __launch_bounds__(256) k_adj_signature(FieldView f, const AdjStep* __restrict__ table, int n_steps,
-                                                       float dt, uint32_t n, const float* __restrict__ xs,
-                                                       const float* __restrict__ ys, const uint8_t* __restrict__ sts,
+                                                       T dt, uint32_t n, const T* __restrict__ xs,
+                                                       const T* __restrict__ ys, const uint8_t* __restrict__ sts,
                                                        unsigned long long* __restrict__ sig) {
   const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
-  float x = xs[p], y = ys[p];
+  const Geo<T> g(f);
+  T x = xs[p], y = ys[p];
   bool live = sts[p] == STATUS_OK;
   unsigned long long h = 0;
   const unsigned long long nx = (unsigned long long)f.nx, cw = (unsigned long long)(f.nx - 1);
   for (int m = 0; m < n_steps && live; ++m) {
     const AdjStep s = table[m];
-    const Stage sh0 = {s.k[0], s.w[0], 1}, sh1 = {s.k[1], s.w[1], 1}, sh2 = {s.k[2], s.w[2], 1};
-    VelJac J;
-    float kx[4], ky[4];
-    bool ok = vel_jac(f, sh0, x, y, J);
-    if (ok) {
-      h = (h ^ ((J.cell / cw) * nx + J.cell % cw)) * 0x100000001B3ull;
-      kx[0] = J.flon, ky[0] = J.flat;
-      ok = vel_jac(f, sh1, x + 0.5f * dt * kx[0], y + 0.5f * dt * ky[0], J);
-    }
-    if (ok) {
-      h = (h ^ ((J.cell / cw) * nx + J.cell % cw)) * 0x100000001B3ull;
-      kx[1] = J.flon, ky[1] = J.flat;
-      ok = vel_jac(f, sh1, x + 0.5f * dt * kx[1], y + 0.5f * dt * ky[1], J);
-    }
-    if (ok) {
-      h = (h ^ ((J.cell / cw) * nx + J.cell % cw)) * 0x100000001B3ull;
-      kx[2] = J.flon, ky[2] = J.flat;
-      ok = vel_jac(f, sh2, x + dt * kx[2], y + dt * ky[2], J);
+    const int ks[4] = {s.k[0], s.k[1], s.k[1], s.k[2]};
+    const T ws[4] = {stage_w<T>(s, 0), stage_w<T>(s, 1), stage_w<T>(s, 1), stage_w<T>(s, 2)};
+    const T hs[4] = {T(0), T(0.5), T(0.5), T(1)};
+    T kx[4], ky[4];
+    bool ok = true;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      if (!ok) break;
+      VelJac<T> J;
+      const T sx = q == 0 ? x : x + hs[q] * dt * kx[q - 1];
+      const T sy = q == 0 ? y : y + hs[q] * dt * ky[q - 1];
+      ok = vel_jac(f, g, ks[q], ws[q], sx, sy, J);
+      if (ok) {
+        h = (h ^ ((J.cell / cw) * nx + J.cell % cw)) * 0x100000001B3ull;
+        kx[q] = J.flon;
+        ky[q] = J.flat;
+      }
     }
     if (!ok) break;
-    h = (h ^ ((J.cell / cw) * nx + J.cell % cw)) * 0x100000001B3ull;
-    kx[3] = J.flon, ky[3] = J.flat;
-    const float nx_ = x + (kx[0] + 2.f * kx[1] + 2.f * kx[2] + kx[3]) * (dt * (1.0f / 6.0f));
-    const float ny_ = y + (ky[0] + 2.f * ky[1] + 2.f * ky[2] + ky[3]) * (dt * (1.0f / 6.0f));
+    const T nx_ = x + (kx[0] + T(2) * kx[1] + T(2) * kx[2] + kx[3]) * (dt * (T(1) / T(6)));
+    const T ny_ = y + (ky[0] + T(2) * ky[1] + T(2) * ky[2] + ky[3]) * (dt * (T(1) / T(6)));
     if (!(isfinite(nx_) && isfinite(ny_))) break;
     x = nx_;
     y = ny_;
@@ -520,32 +616,83 @@ void launch_adj_stages(const FieldView& f, double t_start, double dt, int n_step
   if (n_steps > 0) k_adj_stages<<<grid_for(n_steps, 128), 128, 0, st>>>(f, t_start, dt, n_steps, table, err);
 }
 
-void launch_adj_init(const FieldView& f, uint32_t n, const float* lon, const float* lat, float* x, float* y,
+void launch_adj_init(const FieldView& f, int prec, uint32_t n, const float* lon, const float* lat, void* x, void* y,
                      uint8_t* status, cudaStream_t st) {
-  if (n) k_adj_init<<<grid_for(n, 256), 256, 0, st>>>(f, n, lon, lat, x, y, status);
+  if (!n) return;
+  if (prec == ADJ_F64)
+    k_adj_init<double><<<grid_for(n, 256), 256, 0, st>>>(f, n, lon, lat, (double*)x, (double*)y, status);
+  else
+    k_adj_init<float><<<grid_for(n, 256), 256, 0, st>>>(f, n, lon, lat, (float*)x, (float*)y, status);
 }
 
-void launch_adj_final(const FieldView& f, uint32_t n, const float* x, const float* y, float* lon, float* lat,
+void launch_adj_final(const FieldView& f, int prec, uint32_t n, const void* x, const void* y, float* lon, float* lat,
                       cudaStream_t st) {
-  if (n) k_adj_final<<<grid_for(n, 256), 256, 0, st>>>(f, n, x, y, lon, lat);
+  if (!n) return;
+  if (prec == ADJ_F64)
+    k_adj_final<double><<<grid_for(n, 256), 256, 0, st>>>(f, n, (const double*)x, (const double*)y, lon, lat);
+  else
+    k_adj_final<float><<<grid_for(n, 256), 256, 0, st>>>(f, n, (const float*)x, (const float*)y, lon, lat);
 }
 
-void launch_adj_forward(const FieldView& f, const AdjStep* table, int m0, int m1, float dt, uint32_t n, float* x,
-                        float* y, uint8_t* status, float* rec_x, float* rec_y, uint8_t* rec_st, uint32_t* err,
+void launch_adj_final64(const FieldView& f, int prec, uint32_t n, const void* x, const void* y, double* lon,
+                        double* lat, cudaStream_t st) {
+  if (!n) return;
+  if (prec == ADJ_F64)
+    k_adj_final64<double><<<grid_for(n, 256), 256, 0, st>>>(f, n, (const double*)x, (const double*)y, lon, lat);
+  else
+    k_adj_final64<float><<<grid_for(n, 256), 256, 0, st>>>(f, n, (const float*)x, (const float*)y, lon, lat);
+}
+
+void launch_adj_seed(int prec, uint32_t n, const float* gx, const float* gy, void* lx, void* ly, cudaStream_t st) {
+  if (!n) return;
+  if (prec == ADJ_F64)
+    k_adj_convert_in<double><<<grid_for(n, 256), 256, 0, st>>>(n, gx, gy, (double*)lx, (double*)ly);
+  else
+    k_adj_convert_in<float><<<grid_for(n, 256), 256, 0, st>>>(n, gx, gy, (float*)lx, (float*)ly);
+}
+
+void launch_adj_unseed(int prec, uint32_t n, const void* lx, const void* ly, float* gx, float* gy, cudaStream_t st) {
+  if (!n) return;
+  if (prec == ADJ_F64)
+    k_adj_convert_out<double><<<grid_for(n, 256), 256, 0, st>>>(n, (const double*)lx, (const double*)ly, gx, gy);
+  else
+    k_adj_convert_out<float><<<grid_for(n, 256), 256, 0, st>>>(n, (const float*)lx, (const float*)ly, gx, gy);
+}
+
+void launch_adj_forward(const FieldView& f, int prec, const AdjStep* table, int m0, int m1, double dt, uint32_t n,
+                        void* x, void* y, uint8_t* status, void* rec_x, void* rec_y, uint8_t* rec_st, uint32_t* err,
                         cudaStream_t st) {
-  if (n && m1 > m0)
-    k_adj_forward<<<grid_for(n, 256), 256, 0, st>>>(f, table, m0, m1, dt, n, x, y, status, rec_x, rec_y, rec_st, err);
+  if (!n || m1 <= m0) return;
+  if (prec == ADJ_F64)
+    k_adj_forward<double><<<grid_for(n, 256), 256, 0, st>>>(f, table, m0, m1, dt, n, (double*)x, (double*)y, status,
+                                                            (double*)rec_x, (double*)rec_y, rec_st, err);
+  else
+    k_adj_forward<float><<<grid_for(n, 256), 256, 0, st>>>(f, table, m0, m1, (float)dt, n, (float*)x, (float*)y, status,
+                                                           (float*)rec_x, (float*)rec_y, rec_st, err);
 }
 
-void launch_adj_step(const FieldView& f, const AdjStep& s, float dt, uint32_t n, const float* x, const float* y,
-                     const uint8_t* status, float* lx, float* ly, float4* rec, uint32_t* key, uint32_t sent,
+void launch_adj_step(const FieldView& f, int prec, const AdjStep& s, double dt, uint32_t n, const void* x,
+                     const void* y, const uint8_t* status, void* lx, void* ly, float4* rec, uint32_t* key, uint32_t sent,
                      cudaStream_t st) {
-  if (n) k_adj_step<<<grid_for(n, 256), 256, 0, st>>>(f, s, dt, n, x, y, status, lx, ly, rec, key, sent);
+  if (!n) return;
+  if (prec == ADJ_F64)
+    k_adj_step<double><<<grid_for(n, 256), 256, 0, st>>>(f, s, dt, n, (const double*)x, (const double*)y, status,
+                                                         (double*)lx, (double*)ly, rec, key, sent);
+  else
+    k_adj_step<float><<<grid_for(n, 256), 256, 0, st>>>(f, s, (float)dt, n, (const float*)x, (const float*)y, status,
+                                                        (float*)lx, (float*)ly, rec, key, sent);
 }
 
-void launch_adj_signature(const FieldView& f, const AdjStep* table, int n_steps, float dt, uint32_t n, const float* x,
-                          const float* y, const uint8_t* status, unsigned long long* sig, cudaStream_t st) {
-  if (n) k_adj_signature<<<grid_for(n, 256), 256, 0, st>>>(f, table, n_steps, dt, n, x, y, status, sig);
+void launch_adj_signature(const FieldView& f, int prec, const AdjStep* table, int n_steps, double dt, uint32_t n,
+                          const void* x, const void* y, const uint8_t* status, unsigned long long* sig,
+                          cudaStream_t st) {
+  if (!n) return;
+  if (prec == ADJ_F64)
+    k_adj_signature<double><<<grid_for(n, 256), 256, 0, st>>>(f, table, n_steps, dt, n, (const double*)x,
+                                                              (const double*)y, status, sig);
+  else
+    k_adj_signature<float><<<grid_for(n, 256), 256, 0, st>>>(f, table, n_steps, (float)dt, n, (const float*)x,
+                                                             (const float*)y, status, sig);
 }
 
 size_t adj_sort_hist_len(uint32_t m) { return (size_t)RS_RADIX_MAX * grid_for(m, RS_TILE); }

@@ -5,9 +5,9 @@
 //
 // Device memory of one tape (n microbes, S steps, checkpoint interval K, C = (nx-1)(ny-1) cells):
 //   uv      float2 [nt][ny][nx]            own copy of the field the forward ran on
-//   ck_*    float, float, uint8 [ceil(S/K)][n]  state at steps 0, K, 2K, ...
-//   seg_*   float, float, uint8 [K][n]     state before every step of the segment being reversed
-//   lx, ly  float [n]                      the adjoint dL/dx_m
+//   ck_*    T, T, uint8 [ceil(S/K)][n]     state at steps 0, K, 2K, ... (T = float or double)
+//   seg_*   T, T, uint8 [K][n]             state before every step of the segment being reversed
+//   lx, ly  T [n]                          the adjoint dL/dx_m
 //   rec     float4 [4n], key/k1/k2/v1/v2 uint32 [4n]  stage records and the radix-sort ping-pong
 //   cst/cen uint32 [4C + 1], csum float [C][3][8]     segment bounds, per-cell corner sums
 #include <cuda_runtime.h>
@@ -45,10 +45,13 @@ struct lm_adjoint {
   bool done = false;
   uint32_t n = 0;
   int n_steps = 0, K = 0, n_ck = 0;
-  float dt = 0.f;
+  double dt = 0.0;
+  int prec = ADJ_F32;  // working precision of the recorded run
+  int prec_next = ADJ_F32;
   DBuf<AdjStep> table;
   std::vector<AdjStep> table_h;
-  DBuf<float> x, y, ck_x, ck_y, seg_x, seg_y, lx, ly, csum;
+  DBuf<unsigned char> x, y, ck_x, ck_y, seg_x, seg_y, lx, ly, fin_x, fin_y;  // T-typed, T chosen by `prec`
+  DBuf<float> csum;
   DBuf<uint8_t> st, ck_st, seg_st;
   DBuf<float4> rec;
   DBuf<uint32_t> key, k1, k2, v1, v2, hist, hscan, bsum, cst, cen;
@@ -153,12 +156,20 @@ int lm_adjoint_destroy(lm_adjoint* a) {
   release(a->uv);
   release(a->table);
   release(a->x), release(a->y), release(a->ck_x), release(a->ck_y), release(a->seg_x), release(a->seg_y);
-  release(a->lx), release(a->ly), release(a->csum), release(a->st), release(a->ck_st), release(a->seg_st);
+  release(a->lx), release(a->ly), release(a->fin_x), release(a->fin_y), release(a->csum), release(a->st), release(a->ck_st), release(a->seg_st);
   release(a->rec), release(a->key), release(a->k1), release(a->k2), release(a->v1), release(a->v2);
   release(a->hist), release(a->hscan), release(a->bsum), release(a->cst), release(a->cen);
   if (a->err_d) cudaFree(a->err_d);
   if (a->err_h) cudaFreeHost(a->err_h);
   delete a;
+  return LM_OK;
+}
+
+int lm_adjoint_set_precision(lm_adjoint* a, int precision) {
+  if (!a) return LM_ERR_ARG;
+  if (precision != LM_ADJ_F32 && precision != LM_ADJ_F64)
+    return afail(a, LM_ERR_ARG, "precision must be LM_ADJ_F32 or LM_ADJ_F64 (got %d)", precision);
+  a->prec_next = precision == LM_ADJ_F64 ? ADJ_F64 : ADJ_F32;
   return LM_OK;
 }
 
@@ -195,17 +206,20 @@ int lm_adjoint_forward(lm_adjoint* a, const float* u, const float* v, int nt, in
   const uint32_t N = (uint32_t)n;
   const int n_ck = (n_steps + checkpoint_every - 1) / checkpoint_every;
   const size_t M = (size_t)4 * N;
+  const int prec = a->prec_next;
+  const size_t es = prec == ADJ_F64 ? sizeof(double) : sizeof(float);
   int r;
-  if ((r = grow(a, a->uv, fe)) || (r = grow(a, a->table, (size_t)n_steps)) || (r = grow(a, a->x, N)) ||
-      (r = grow(a, a->y, N)) || (r = grow(a, a->st, N)) || (r = grow(a, a->ck_x, (size_t)n_ck * N)) ||
-      (r = grow(a, a->ck_y, (size_t)n_ck * N)) || (r = grow(a, a->ck_st, (size_t)n_ck * N)) ||
-      (r = grow(a, a->seg_x, (size_t)checkpoint_every * N)) || (r = grow(a, a->seg_y, (size_t)checkpoint_every * N)) ||
-      (r = grow(a, a->seg_st, (size_t)checkpoint_every * N)) || (r = grow(a, a->lx, N)) || (r = grow(a, a->ly, N)) ||
-      (r = grow(a, a->rec, M)) || (r = grow(a, a->key, M)) || (r = grow(a, a->k1, M)) || (r = grow(a, a->k2, M)) ||
-      (r = grow(a, a->v1, M)) || (r = grow(a, a->v2, M)) || (r = grow(a, a->hist, adj_sort_hist_len((uint32_t)M))) ||
-      (r = grow(a, a->hscan, adj_sort_hist_len((uint32_t)M))) || (r = grow(a, a->bsum, SCAN_BLOCKS)) ||
-      (r = grow(a, a->cst, 4 * cells + 1, true)) || (r = grow(a, a->cen, 4 * cells + 1, true)) ||
-      (r = grow(a, a->csum, cells * 24)))
+  if ((r = grow(a, a->uv, fe)) || (r = grow(a, a->table, (size_t)n_steps)) || (r = grow(a, a->x, es * N)) ||
+      (r = grow(a, a->y, es * N)) || (r = grow(a, a->st, N)) || (r = grow(a, a->ck_x, es * n_ck * N)) ||
+      (r = grow(a, a->ck_y, es * n_ck * N)) || (r = grow(a, a->ck_st, (size_t)n_ck * N)) ||
+      (r = grow(a, a->seg_x, es * checkpoint_every * N)) || (r = grow(a, a->seg_y, es * checkpoint_every * N)) ||
+      (r = grow(a, a->seg_st, (size_t)checkpoint_every * N)) || (r = grow(a, a->lx, es * N)) ||
+      (r = grow(a, a->ly, es * N)) || (r = grow(a, a->fin_x, es * N)) || (r = grow(a, a->fin_y, es * N)) ||
+      (r = grow(a, a->rec, M)) || (r = grow(a, a->key, M)) ||
+      (r = grow(a, a->k1, M)) || (r = grow(a, a->k2, M)) || (r = grow(a, a->v1, M)) || (r = grow(a, a->v2, M)) ||
+      (r = grow(a, a->hist, adj_sort_hist_len((uint32_t)M))) || (r = grow(a, a->hscan, adj_sort_hist_len((uint32_t)M))) ||
+      (r = grow(a, a->bsum, SCAN_BLOCKS)) || (r = grow(a, a->cst, 4 * cells + 1, true)) ||
+      (r = grow(a, a->cen, 4 * cells + 1, true)) || (r = grow(a, a->csum, cells * 24)))
     return r;
   launch_interleave(u, v, a->uv.p, fe, st);
   fill_field_view(a->fv, a->uv.p, nt, ny, nx, lon, lat, t_sec, dx, dy, dT);
@@ -216,7 +230,8 @@ int lm_adjoint_forward(lm_adjoint* a, const float* u, const float* v, int nt, in
   a->n_steps = n_steps;
   a->K = checkpoint_every;
   a->n_ck = n_ck;
-  a->dt = (float)dt_sec;
+  a->prec = prec;
+  a->dt = dt_sec;
   ACK(cudaMemsetAsync(a->err_d, 0, sizeof(uint32_t), st));
   launch_adj_stages(a->fv, t_start, dt_sec, n_steps, a->table.p, a->err_d, st);
   a->table_h.resize(n_steps);
@@ -224,18 +239,22 @@ int lm_adjoint_forward(lm_adjoint* a, const float* u, const float* v, int nt, in
   uint32_t err;
   if ((r = read_err(a, st, &err))) return r;
   if (err & ERRB_TIME) return afail(a, LM_ERR_TIME, "a stage time fell outside the field's time axis");
-  launch_adj_init(a->fv, N, lon0, lat0, a->x.p, a->y.p, a->st.p, st);
+  launch_adj_init(a->fv, prec, N, lon0, lat0, a->x.p, a->y.p, a->st.p, st);
   for (int s = 0; s < n_ck; ++s) {
     const int m0 = s * checkpoint_every, m1 = std::min(m0 + checkpoint_every, n_steps);
     if (N) {
-      ACK(cudaMemcpyAsync(a->ck_x.p + (size_t)s * N, a->x.p, N * sizeof(float), cudaMemcpyDeviceToDevice, st));
-      ACK(cudaMemcpyAsync(a->ck_y.p + (size_t)s * N, a->y.p, N * sizeof(float), cudaMemcpyDeviceToDevice, st));
+      ACK(cudaMemcpyAsync(a->ck_x.p + es * s * N, a->x.p, es * N, cudaMemcpyDeviceToDevice, st));
+      ACK(cudaMemcpyAsync(a->ck_y.p + es * s * N, a->y.p, es * N, cudaMemcpyDeviceToDevice, st));
       ACK(cudaMemcpyAsync(a->ck_st.p + (size_t)s * N, a->st.p, N, cudaMemcpyDeviceToDevice, st));
     }
-    launch_adj_forward(a->fv, a->table.p, m0, m1, a->dt, N, a->x.p, a->y.p, a->st.p, nullptr, nullptr, nullptr,
+    launch_adj_forward(a->fv, prec, a->table.p, m0, m1, a->dt, N, a->x.p, a->y.p, a->st.p, nullptr, nullptr, nullptr,
                        a->err_d, st);
   }
-  launch_adj_final(a->fv, N, a->x.p, a->y.p, lon_out, lat_out, st);
+  launch_adj_final(a->fv, prec, N, a->x.p, a->y.p, lon_out, lat_out, st);
+  if (N) {
+    ACK(cudaMemcpyAsync(a->fin_x.p, a->x.p, es * N, cudaMemcpyDeviceToDevice, st));
+    ACK(cudaMemcpyAsync(a->fin_y.p, a->y.p, es * N, cudaMemcpyDeviceToDevice, st));
+  }
   ACK(cudaGetLastError());
   if ((r = read_err(a, st, &err))) return r;
   a->done = true;
@@ -260,25 +279,25 @@ int lm_adjoint_backward(lm_adjoint* a, const float* g_lon, const float* g_lat, f
   const uint32_t sent = 4u * cells;
   const int kb = key_bits_for(sent);
   const uint32_t M = 4u * N;
+  const size_t es = a->prec == ADJ_F64 ? sizeof(double) : sizeof(float);
   ACK(cudaMemsetAsync(g_u, 0, fe * sizeof(float), st));
   ACK(cudaMemsetAsync(g_v, 0, fe * sizeof(float), st));
   if (N) {
-    ACK(cudaMemcpyAsync(a->lx.p, g_lon, N * sizeof(float), cudaMemcpyDeviceToDevice, st));
-    ACK(cudaMemcpyAsync(a->ly.p, g_lat, N * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    launch_adj_seed(a->prec, N, g_lon, g_lat, a->lx.p, a->ly.p, st);
   }
   AdjSortBufs sb{a->key.p, a->k1.p, a->k2.p, a->v1.p, a->v2.p, a->hist.p, a->hscan.p, a->bsum.p};
   for (int s = a->n_ck - 1; s >= 0 && N; --s) {
     const int m0 = s * a->K, m1 = std::min(m0 + a->K, a->n_steps);
-    ACK(cudaMemcpyAsync(a->x.p, a->ck_x.p + (size_t)s * N, N * sizeof(float), cudaMemcpyDeviceToDevice, st));
-    ACK(cudaMemcpyAsync(a->y.p, a->ck_y.p + (size_t)s * N, N * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    ACK(cudaMemcpyAsync(a->x.p, a->ck_x.p + es * s * N, es * N, cudaMemcpyDeviceToDevice, st));
+    ACK(cudaMemcpyAsync(a->y.p, a->ck_y.p + es * s * N, es * N, cudaMemcpyDeviceToDevice, st));
     ACK(cudaMemcpyAsync(a->st.p, a->ck_st.p + (size_t)s * N, N, cudaMemcpyDeviceToDevice, st));
-    launch_adj_forward(a->fv, a->table.p, m0, m1, a->dt, N, a->x.p, a->y.p, a->st.p, a->seg_x.p, a->seg_y.p,
+    launch_adj_forward(a->fv, a->prec, a->table.p, m0, m1, a->dt, N, a->x.p, a->y.p, a->st.p, a->seg_x.p, a->seg_y.p,
                        a->seg_st.p, a->err_d, st);
     for (int m = m1 - 1; m >= m0; --m) {
       const size_t o = (size_t)(m - m0) * N;
       const AdjStep& sg = a->table_h[m];
-      launch_adj_step(a->fv, sg, a->dt, N, a->seg_x.p + o, a->seg_y.p + o, a->seg_st.p + o, a->lx.p, a->ly.p,
-                      a->rec.p, a->key.p, sent, st);
+      launch_adj_step(a->fv, a->prec, sg, a->dt, N, a->seg_x.p + es * o, a->seg_y.p + es * o, a->seg_st.p + o,
+                      a->lx.p, a->ly.p, a->rec.p, a->key.p, sent, st);
       const uint32_t *skey, *sval;
       adj_sort(sb, M, kb, st, &skey, &sval);
       launch_adj_bounds(skey, M, sent, a->cst.p, a->cen.p, st);
@@ -286,10 +305,19 @@ int lm_adjoint_backward(lm_adjoint* a, const float* g_lon, const float* g_lat, f
       launch_adj_nodes(a->nx, a->ny, sg, a->csum.p, g_u, g_v, st);
     }
   }
-  if (N) {
-    ACK(cudaMemcpyAsync(g_lon0, a->lx.p, N * sizeof(float), cudaMemcpyDeviceToDevice, st));
-    ACK(cudaMemcpyAsync(g_lat0, a->ly.p, N * sizeof(float), cudaMemcpyDeviceToDevice, st));
-  }
+  if (N) launch_adj_unseed(a->prec, N, a->lx.p, a->ly.p, g_lon0, g_lat0, st);
+  ACK(cudaGetLastError());
+  ACK(cudaStreamSynchronize(st));
+  return LM_OK;
+}
+
+int lm_adjoint_final_positions(lm_adjoint* a, double* lon, double* lat) {
+  if (!a) return LM_ERR_ARG;
+  if (!a->done) return afail(a, LM_ERR_STATE, "run lm_adjoint_forward first");
+  if (a->n && (!on_device(lon) || !on_device(lat))) return afail(a, LM_ERR_ARG, "lon and lat must be device pointers");
+  ACK(cudaSetDevice(a->device));
+  cudaStream_t st = ctx_stream(a->ctx);
+  launch_adj_final64(a->fv, a->prec, a->n, a->fin_x.p, a->fin_y.p, lon, lat, st);
   ACK(cudaGetLastError());
   ACK(cudaStreamSynchronize(st));
   return LM_OK;
@@ -301,7 +329,8 @@ int lm_adjoint_cell_signature(lm_adjoint* a, unsigned long long* sig) {
   if (a->n && !on_device(sig)) return afail(a, LM_ERR_ARG, "sig must be a device pointer");
   ACK(cudaSetDevice(a->device));
   cudaStream_t st = ctx_stream(a->ctx);
-  launch_adj_signature(a->fv, a->table.p, a->n_steps, a->dt, a->n, a->ck_x.p, a->ck_y.p, a->ck_st.p, sig, st);
+  launch_adj_signature(a->fv, a->prec, a->table.p, a->n_steps, a->dt, a->n, a->ck_x.p, a->ck_y.p, a->ck_st.p, sig,
+                       st);
   ACK(cudaGetLastError());
   ACK(cudaStreamSynchronize(st));
   return LM_OK;

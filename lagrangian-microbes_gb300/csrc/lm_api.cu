@@ -1202,5 +1202,9 @@ void fill_field_view(FieldView& f, float2* uv, int nt, int ny, int nx, const dou
   f.org_lat = (float)org_lat;
   f.t0 = t_sec[0];
   f.dT = dT;
+  f.gx0d = lon[0] - org_lon;
+  f.gy0d = lat[0] - org_lat;
+  f.inv_dxd = 1.0 / dx;
+  f.inv_dyd = 1.0 / dy;
 }
 }  // namespace lm

@@ -104,6 +104,8 @@ struct FieldView {
   float max_fx, max_fy;  // nx-1, ny-1
   float org_lon, org_lat;  // float32 origin of the offsets (absolute degrees)
   double t0, dT;      // frame 0 time and frame spacing (seconds)
+  // the same geometry in float64 (the adjoint's FP64-trajectory mode)
+  double gx0d, gy0d, inv_dxd, inv_dyd;
 };
 
 struct PairParams {
@@ -194,7 +196,9 @@ void launch_unpad8(const int8_t* src, int8_t* dst, const int32_t* map, uint32_t 
 struct AdjStep {
   int k[3];
   float w[3];
+  double wd[3];  // the weights in float64 (FP64-trajectory mode)
 };
+enum AdjPrecision { ADJ_F32 = 0, ADJ_F64 = 1 };
 constexpr int RS_BITS_MAX = 10;                      // digit width of one radix pass
 constexpr uint32_t RS_RADIX_MAX = 1u << RS_BITS_MAX;
 
@@ -208,18 +212,25 @@ struct AdjSortBufs {
 
 void launch_adj_stages(const FieldView& f, double t_start, double dt, int n_steps, AdjStep* table, uint32_t* err,
                        cudaStream_t st);
-void launch_adj_init(const FieldView& f, uint32_t n, const float* lon, const float* lat, float* x, float* y,
+// Per-microbe kernels in precision `prec` (ADJ_F32: float state, the engine's arithmetic; ADJ_F64:
+// double state and arithmetic); x, y, lx, ly point to arrays of that type.
+void launch_adj_init(const FieldView& f, int prec, uint32_t n, const float* lon, const float* lat, void* x, void* y,
                      uint8_t* status, cudaStream_t st);
-void launch_adj_final(const FieldView& f, uint32_t n, const float* x, const float* y, float* lon, float* lat,
+void launch_adj_final(const FieldView& f, int prec, uint32_t n, const void* x, const void* y, float* lon, float* lat,
                       cudaStream_t st);
-void launch_adj_forward(const FieldView& f, const AdjStep* table, int m0, int m1, float dt, uint32_t n, float* x,
-                        float* y, uint8_t* status, float* rec_x, float* rec_y, uint8_t* rec_st, uint32_t* err,
+void launch_adj_final64(const FieldView& f, int prec, uint32_t n, const void* x, const void* y, double* lon,
+                        double* lat, cudaStream_t st);
+void launch_adj_seed(int prec, uint32_t n, const float* gx, const float* gy, void* lx, void* ly, cudaStream_t st);
+void launch_adj_unseed(int prec, uint32_t n, const void* lx, const void* ly, float* gx, float* gy, cudaStream_t st);
+void launch_adj_forward(const FieldView& f, int prec, const AdjStep* table, int m0, int m1, double dt, uint32_t n,
+                        void* x, void* y, uint8_t* status, void* rec_x, void* rec_y, uint8_t* rec_st, uint32_t* err,
                         cudaStream_t st);
-void launch_adj_step(const FieldView& f, const AdjStep& s, float dt, uint32_t n, const float* x, const float* y,
-                     const uint8_t* status, float* lx, float* ly, float4* rec, uint32_t* key, uint32_t sent,
+void launch_adj_step(const FieldView& f, int prec, const AdjStep& s, double dt, uint32_t n, const void* x,
+                     const void* y, const uint8_t* status, void* lx, void* ly, float4* rec, uint32_t* key, uint32_t sent,
                      cudaStream_t st);
-void launch_adj_signature(const FieldView& f, const AdjStep* table, int n_steps, float dt, uint32_t n, const float* x,
-                          const float* y, const uint8_t* status, unsigned long long* sig, cudaStream_t st);
+void launch_adj_signature(const FieldView& f, int prec, const AdjStep* table, int n_steps, double dt, uint32_t n,
+                          const void* x, const void* y, const uint8_t* status, unsigned long long* sig,
+                          cudaStream_t st);
 size_t adj_sort_hist_len(uint32_t m);
 // Stable sort of m keys of key_bits bits; returns the sorted keys and the record ids (input index).
 void adj_sort(const AdjSortBufs& sb, uint32_t m, int key_bits, cudaStream_t st, const uint32_t** skey,

@@ -30,14 +30,14 @@ def _case(field, n, seed, box=(199.0, 202.0, 24.0, 27.0)):
     return lon, lat, tlon, tlat
 
 
-def _gpu_grads(field, lon, lat, tlon, tlat, t0, dt, n_steps, k, allow_oob=False, weight=None):
+def _gpu_grads(field, lon, lat, tlon, tlat, t0, dt, n_steps, k, allow_oob=False, weight=None, precision="f32"):
     from lagrangian_microbes_gb300.adjoint import AdjointTape, advect_rk4, great_circle_m
     dev = torch.device("cuda:0")
     l0 = torch.from_numpy(lon).to(dev).requires_grad_(True)
     a0 = torch.from_numpy(lat).to(dev).requires_grad_(True)
     u = torch.from_numpy(field.u).to(dev).requires_grad_(True)
     v = torch.from_numpy(field.v).to(dev).requires_grad_(True)
-    tape = AdjointTape()
+    tape = AdjointTape(precision=precision)
     x, y = advect_rk4(l0, a0, u, v, field.lon, field.lat, field.times, t0, dt, n_steps, checkpoint_every=k,
                       tape=tape, allow_out_of_bounds=allow_oob)
     dist = great_circle_m(x.double(), y.double(), torch.from_numpy(tlon).to(dev), torch.from_numpy(tlat).to(dev))
@@ -204,3 +204,23 @@ def test_adjoint_time_window_outside_field_raises(lm, small_field):
         tape.forward(z, z - 175.0, torch.from_numpy(f.u).to(dev), torch.from_numpy(f.v).to(dev), f.lon, f.lat, f.times,
                      float(f.times[-1]), 3600.0, 5)
     tape.close()
+
+
+def test_adjoint_f64_trajectories_track_the_fp64_scheme(lm, orc, small_field):
+    """FP64 mode: positions within 1e-9 deg of the FP64 oracle and gradients within 1e-5 of the FP64
+    autograd on every microbe (no cell-path selection needed), deterministic across intervals."""
+    f = small_field
+    lon, lat, tlon, tlat = _case(f, 3000, 8)
+    t0, dt, n_steps = float(f.times[0]), 3600.0, 48
+    x, y, loss, g, sig = _gpu_grads(f, lon, lat, tlon, tlat, t0, dt, n_steps, 16, precision="f64")
+    x64, y64, _, sig64 = orc.advect_f64_field64(f.u, f.v, f.lon, f.lat, f.times, lon.astype(np.float64),
+                                                lat.astype(np.float64), t0, dt, n_steps, cell_signature=True)
+    # final positions come back as float64 in this mode
+    assert x.dtype == np.float64 and np.abs(x - x64).max() <= 1e-9 and np.abs(y - y64).max() <= 1e-9
+    assert (sig == sig64).all()
+    loss64, g64 = _fp64_grads(f, lon, lat, tlon, tlat, t0, dt, n_steps)
+    errs = [_rel(a, b) for a, b in zip(g, g64)]
+    assert max(errs) < 1e-5, errs
+    again = _gpu_grads(f, lon, lat, tlon, tlat, t0, dt, n_steps, 5, precision="f64")
+    for a, b in zip(again[3], g):
+        np.testing.assert_array_equal(a, b)
