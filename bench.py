@@ -253,6 +253,12 @@ def run_gb300(args):
     if not args.no_e2e:
         e2e = run_e2e(fld, lons, lats, species, K, spg, local, stream)
 
+    batched = adjoint = None
+    if rank == 0 and not args.no_batched:
+        batched = run_batched(local, stream)
+    if rank == 0 and not args.no_adjoint:
+        adjoint = run_adjoint(fld, local)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(fld, lons, lats, species, args.cpu_seconds)
@@ -271,7 +277,7 @@ def run_gb300(args):
             "plain": {"value": plain_value, "unit": "microbe-steps/s", "sim_steps": plain_steps,
                       "graph_speedup": value / world / plain_value},
             "roofline": roofline, "whole_step": whole, "kernels": kernels,
-            "e2e": e2e, "cpu_baseline": cpu, "clocks": clk,
+            "e2e": e2e, "cpu_baseline": cpu, "clocks": clk, "batched": batched, "adjoint": adjoint,
             "gpu_launches": int(round(launches_per_step * K)),
             "max_rounds": stats["max_rounds"],
             "mean_rounds": stats["rounds_total"] / max(stats["steps_total"], 1),
@@ -303,6 +309,151 @@ def run_e2e(fld, lons, lats, species, K, spg, local, stream):
     return {"value": n * K * spg / (t1 - t0), "unit": "microbe-steps/s", "h2d_bytes_per_step": h2d / K,
             "d2h_bytes_per_step": d2h / K, "seconds": t1 - t0,
             "note": "setup (field + particles upload, graph capture) + 720 steps + state download, wall clock"}
+
+
+B_ENSEMBLES = 256
+B_STEPS = 24
+B_BOX = (195.0, 215.0, 20.0, 35.0)
+B_WORKLOAD = ("256 ensembles, counts log-uniform in [1e3, 2e5] (rounded to square-ish lattices), patches of 0.5-3 deg side within lon "
+              "195-215E lat 20-35N, p ~ U[0.5, 0.9], own seed and own 32-mode psi field each on a shared 1/12 deg "
+              "hourly grid, RK4 dt=1h, r=0.01 deg; the first simulated day (24 of 240 steps)")
+
+
+def make_ensembles(n_ens: int, n_frames: int, seed: int = 2025):
+    """The batching configuration: per-ensemble lattices, probabilities, seeds and fields (seeded)."""
+    import numpy as np
+
+    import lagrangian_microbes_gb300 as lm
+    from lagrangian_microbes_gb300.particle_advecter import uniform_particle_locations
+    rng = np.random.default_rng(seed)
+    raw = np.exp(rng.uniform(np.log(1e3), np.log(2e5), n_ens))
+    # square-ish lattices: the count is rounded to rows x columns with rows = round(sqrt(count)), so
+    # that the lattice helper's factorisation never degenerates into a single dense line
+    rows = np.maximum(1, np.rint(np.sqrt(raw))).astype(np.int64)
+    counts = rows * np.maximum(1, np.rint(raw / rows)).astype(np.int64)
+    sides = rng.uniform(0.5, 3.0, n_ens)
+    margin = 0.5  # keeps a day of drift inside the field
+    lon0 = rng.uniform(B_BOX[0] + margin, B_BOX[1] - margin - sides)
+    lat0 = rng.uniform(B_BOX[2] + margin, B_BOX[3] - margin - sides)
+    ps = rng.uniform(0.5, 0.9, n_ens)
+    seeds = rng.integers(0, 2 ** 62, n_ens)
+    ens = []
+    for e in range(n_ens):
+        lons, lats = uniform_particle_locations(int(counts[e]), lat0[e], lat0[e] + sides[e], lon0[e], lon0[e] + sides[e])
+        sp = np.random.default_rng(int(seeds[e])).integers(1, 4, lons.size).astype(np.int8)
+        ens.append((lons, lats, sp))
+    fields = [lm.synthetic_psi_field(*B_BOX, RES, n_frames=n_frames, frame_seconds=DT, seed=SEED + 1 + e)
+              for e in range(n_ens)]
+    return fields, ens, ps, seeds
+
+
+def run_batched(local: int, stream):
+    """Config B: all ensembles in one context (CUDA graph of B_STEPS fused steps) against plain
+    per-step launches of each ensemble alone (its own context), the same simulated steps."""
+    import numpy as np
+    import torch
+
+    from lagrangian_microbes_gb300.engine import EnsembleSimulation, Simulation
+    t_gen = time.perf_counter()
+    fields, ens, ps, seeds = make_ensembles(B_ENSEMBLES, B_STEPS + 2)
+    t_gen = time.perf_counter() - t_gen
+    total = int(sum(x[0].size for x in ens))
+    sim = EnsembleSimulation(fields, ens, radius=RADIUS, p_rs=ps, p_pr=ps, p_sp=ps, seeds=seeds, device=local)
+    sim.set_stream(stream.cuda_stream)
+    sim.capture(0.0, DT, B_STEPS, step0=0)
+    sim.run_graph(1, sync=True)  # warm-up: sizes the long neighbour lists for this workload
+    reps = 3
+    times = []
+    for _ in range(reps):
+        sim.upload_ensembles(ens)
+        sim.set_step(0)
+        sim.ctx.call("lm_stats_reset")
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(stream)
+        sim.run_graph(1, sync=False)
+        b.record(stream)
+        torch.cuda.synchronize()
+        times.append(a.elapsed_time(b))
+    sim.sync()
+    st = sim.stats()
+    sim.close()
+    graph_ms = float(np.median(times))
+    graph_value = total * B_STEPS / (graph_ms / 1e3)
+    # plain: each ensemble alone through the drop-in engine, per-step launches
+    plain_ms = 0.0
+    sims = []
+    for e in range(B_ENSEMBLES):
+        one = Simulation(fields[e], ens[e][0], ens[e][1], ens[e][2], radius=RADIUS, p_rs=ps[e], p_pr=ps[e],
+                         p_sp=ps[e], seed=int(seeds[e]), device=local)
+        one.step(0.0, DT, 1, step0=0)  # warm-up (list capacities), then from the start again
+        one.upload_particles(ens[e][0], ens[e][1], ens[e][2])
+        sims.append(one)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for e, one in enumerate(sims):
+        one.step(0.0, DT, B_STEPS, step0=0)
+    torch.cuda.synchronize()
+    plain_ms = (time.perf_counter() - t0) * 1e3
+    for one in sims:
+        one.close()
+    plain_value = total * B_STEPS / (plain_ms / 1e3)
+    return {"workload": B_WORKLOAD, "ensembles": B_ENSEMBLES, "microbes": total, "sim_steps": B_STEPS,
+            "pairs_per_step": st["pairs_total"] / max(st["steps_total"], 1),
+            "graph": {"value": graph_value, "unit": "microbe-steps/s", "ms_per_sim_step": graph_ms / B_STEPS,
+                      "form": "one context, one CUDA graph of 24 fused steps for all ensembles"},
+            "plain_per_ensemble": {"value": plain_value, "unit": "microbe-steps/s",
+                                   "ms_per_sim_step": plain_ms / B_STEPS,
+                                   "form": "one context per ensemble, per-step launches, ensembles one after another"},
+            "batched_over_plain": graph_value / plain_value, "field_generation_s": t_gen}
+
+
+def run_adjoint(fld, local: int):
+    """Config D timing: 1M microbes on a 1000x1000 lattice, 720 steps, checkpoints every 32, the
+    mean squared great-circle distance to seeded targets, forward + backward (both precisions)."""
+    import numpy as np
+    import torch
+
+    from lagrangian_microbes_gb300.adjoint import AdjointTape, advect_rk4, mean_squared_distance
+    from lagrangian_microbes_gb300.particle_advecter import uniform_particle_locations
+    n, steps, k = 1_000_000, 720, 32
+    if fld.u.shape[0] < steps + 1:
+        return {"skipped": f"field has {fld.u.shape[0]} frames, need {steps + 1}"}
+    lons, lats = uniform_particle_locations(n, LAT[0], LAT[1], LON[0], LON[1])
+    rng = np.random.default_rng(7)
+    dev = torch.device("cuda", local)
+    tl = torch.from_numpy(lons + rng.normal(0, 20.0 / 111.32, n) / np.cos(np.deg2rad(lats))).to(dev)
+    ta = torch.from_numpy(lats + rng.normal(0, 20.0 / 111.32, n)).to(dev)
+    u = torch.from_numpy(fld.u[: steps + 1]).to(dev).requires_grad_(True)
+    v = torch.from_numpy(fld.v[: steps + 1]).to(dev).requires_grad_(True)
+    out = {"workload": "1M microbes, 1000x1000 lattice lon 200-205E lat 25-30N, 720 RK4 steps dt=1h on the 1/12 deg "
+                       "hourly field, checkpoints every 32 steps, loss = mean squared great-circle distance to "
+                       "targets x0 + N(0, 20 km)", "microbes": n, "sim_steps": steps}
+    for prec in ("f32", "f64"):
+        tape = AdjointTape(device=local, precision=prec)
+        res = []
+        for _ in range(3):
+            l0 = torch.from_numpy(lons.astype(np.float32)).to(dev).requires_grad_(True)
+            a0 = torch.from_numpy(lats.astype(np.float32)).to(dev).requires_grad_(True)
+            u.grad = v.grad = None
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+            torch.cuda.synchronize()
+            ev[0].record()
+            x, y = advect_rk4(l0, a0, u, v, fld.lon, fld.lat, fld.times[: steps + 1], 0.0, DT, steps,
+                              checkpoint_every=k, tape=tape)
+            ev[1].record()
+            loss = mean_squared_distance(x, y, tl, ta)
+            loss.backward()
+            ev[2].record()
+            torch.cuda.synchronize()
+            res.append((ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])))
+        tape.close()
+        fwd = float(np.median([r[0] for r in res]))
+        bwd = float(np.median([r[1] for r in res]))
+        out[prec] = {"forward_ms": fwd, "backward_ms": bwd,
+                     "value": n * steps / ((fwd + bwd) / 1e3), "unit": "microbe-steps/s (forward + backward)",
+                     "loss_m2": float(loss.detach())}
+    return out
 
 
 def cpu_threads():
@@ -374,10 +525,12 @@ def main():
     ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--plain-steps", type=int, default=240)
+    ap.add_argument("--plain-steps", type=int, default=720, help="plain steps (the same steps the graph runs)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 256-ensemble batching measurement")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint (differentiation) timing")
     ap.add_argument("--profile-run", action="store_true", help="only the warm-up and timed graph launches")
     ap.add_argument("--traffic-json", default=os.path.join(REPO, "profiles", "traffic.json"))
     args = ap.parse_args()

@@ -68,6 +68,7 @@ __device__ __forceinline__ void block_bbox(bool valid, float x, float y, uint32_
 }
 
 __global__ void __launch_bounds__(SLOT_BLOCK) k_advect(FieldView f, StepArgs a, Bufs b, Ctrl* ctrl) {
+  pdl_wait();
   __shared__ Stage sh[3];
   __shared__ uint32_t sh_step;
   __shared__ int sh_skip;
@@ -135,11 +136,12 @@ __global__ void __launch_bounds__(SLOT_BLOCK) k_advect(FieldView f, StepArgs a, 
 
 void launch_advect(const FieldView& f, const StepArgs& a, const Bufs& b, Ctrl* ctrl, cudaStream_t st) {
   if (b.nslots == 0) return;
-  k_advect<<<(b.nslots + SLOT_BLOCK - 1) / SLOT_BLOCK, SLOT_BLOCK, 0, st>>>(f, a, b, ctrl);
+  launch_dep(k_advect, dim3((b.nslots + SLOT_BLOCK - 1) / SLOT_BLOCK), dim3(SLOT_BLOCK), st, f, a, b, ctrl);
 }
 
 // Bounding boxes from the recorded positions (two-phase interaction path and step re-runs).
 __global__ void __launch_bounds__(SLOT_BLOCK) k_bbox(Bufs b, Ctrl* ctrl, int use_status) {
+  pdl_wait();
   if (ctrl->halt) return;
   const uint32_t p = blockIdx.x * SLOT_BLOCK + threadIdx.x;
   const uint32_t e = b.block_ens[blockIdx.x];
@@ -156,12 +158,13 @@ __global__ void __launch_bounds__(SLOT_BLOCK) k_bbox(Bufs b, Ctrl* ctrl, int use
 
 void launch_bbox(const Bufs& b, Ctrl* ctrl, bool use_status, cudaStream_t st) {
   if (b.nslots == 0) return;
-  k_bbox<<<(b.nslots + SLOT_BLOCK - 1) / SLOT_BLOCK, SLOT_BLOCK, 0, st>>>(b, ctrl, use_status ? 1 : 0);
+  launch_dep(k_bbox, dim3((b.nslots + SLOT_BLOCK - 1) / SLOT_BLOCK), dim3(SLOT_BLOCK), st, b, ctrl, use_status ? 1 : 0);
 }
 
 // Per-step bookkeeping: reset the per-step counters and the ensemble boxes (start), advance the
 // device step counter (end).
 __global__ void k_step_begin(Bufs b, FieldView f, StepArgs a, int bracket, Ctrl* ctrl) {
+  pdl_wait();
   if (ctrl->halt) return;
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   for (uint32_t e = t; e < b.n_ens; e += gridDim.x * blockDim.x) {
@@ -198,6 +201,7 @@ __global__ void k_step_begin(Bufs b, FieldView f, StepArgs a, int bracket, Ctrl*
 }
 
 __global__ void k_step_end(Ctrl* ctrl, int interact) {
+  pdl_wait();
   if (ctrl->halt) return;
   if (interact) {
     ctrl->pairs_total += ctrl->n_dir / 2;
@@ -213,9 +217,9 @@ void launch_step_begin(const Bufs& b, const FieldView* f, const StepArgs& a, Ctr
   if (grid > 64) grid = 64;
   FieldView fv{};
   if (f) fv = *f;
-  k_step_begin<<<grid, 256, 0, st>>>(b, fv, a, f ? 1 : 0, ctrl);
+  launch_dep(k_step_begin, dim3(grid), dim3(256), st, b, fv, a, f ? 1 : 0, ctrl);
 }
-void launch_step_end(Ctrl* ctrl, bool interact, cudaStream_t st) { k_step_end<<<1, 1, 0, st>>>(ctrl, interact ? 1 : 0); }
+void launch_step_end(Ctrl* ctrl, bool interact, cudaStream_t st) { launch_dep(k_step_end, dim3(1), dim3(1), st, ctrl, interact ? 1 : 0); }
 
 // Gathers from the padded slot layout into caller order (map[slot] = caller index or -1).
 template <class T>

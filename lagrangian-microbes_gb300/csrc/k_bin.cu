@@ -38,6 +38,7 @@ __device__ __forceinline__ float grid_dims(const uint32_t* box, float c, float* 
 // One block: grid geometry of every ensemble and the global cell numbering. If the cells would
 // exceed the capacity, the cell size grows (pairs stay exact because only c >= r matters).
 __global__ void __launch_bounds__(GRID_THREADS) k_grid(Bufs b, PairParams pp, Ctrl* ctrl) {
+  pdl_wait();
   if (ctrl->halt) return;
   __shared__ float ws[GRID_THREADS / 32];
   __shared__ float total_sh;
@@ -124,11 +125,12 @@ __global__ void __launch_bounds__(GRID_THREADS) k_grid(Bufs b, PairParams pp, Ct
 }
 
 void launch_grid(const Bufs& b, const PairParams& pp, Ctrl* ctrl, cudaStream_t st) {
-  k_grid<<<1, GRID_THREADS, 0, st>>>(b, pp, ctrl);
+  launch_dep(k_grid, dim3(1), dim3(GRID_THREADS), st, b, pp, ctrl);
 }
 
 // Cell key of every valid particle + its rank inside the cell (warp-aggregated atomics).
 __global__ void __launch_bounds__(SLOT_BLOCK) k_keys(Bufs b, Ctrl* ctrl, int use_status) {
+  pdl_wait();
   if (ctrl->halt) return;
   __shared__ EnsGrid g;
   __shared__ EnsInfo info;
@@ -171,7 +173,7 @@ __global__ void __launch_bounds__(SLOT_BLOCK) k_keys(Bufs b, Ctrl* ctrl, int use
 
 void launch_keys(const Bufs& b, Ctrl* ctrl, bool use_status, cudaStream_t st) {
   if (b.nslots == 0) return;
-  k_keys<<<(b.nslots + SLOT_BLOCK - 1) / SLOT_BLOCK, SLOT_BLOCK, 0, st>>>(b, ctrl, use_status ? 1 : 0);
+  launch_dep(k_keys, dim3((b.nslots + SLOT_BLOCK - 1) / SLOT_BLOCK), dim3(SLOT_BLOCK), st, b, ctrl, use_status ? 1 : 0);
 }
 
 // Exclusive scan of the cell counts in two launches over SCAN_BLOCKS fixed chunks:
@@ -195,6 +197,7 @@ __device__ __forceinline__ uint32_t block_sum(uint32_t v) {
 }
 
 __global__ void __launch_bounds__(1024) k_cscan_reduce(Bufs b, Ctrl* ctrl) {
+  pdl_wait();
   if (ctrl->halt) return;
   uint32_t c0, c1;
   chunk_of(ctrl->ncells, &c0, &c1);
@@ -205,6 +208,7 @@ __global__ void __launch_bounds__(1024) k_cscan_reduce(Bufs b, Ctrl* ctrl) {
 }
 
 __global__ void __launch_bounds__(1024) k_cscan_down(Bufs b, Ctrl* ctrl) {
+  pdl_wait();
   if (ctrl->halt) return;
   __shared__ uint32_t ws[32];
   __shared__ uint32_t carry;
@@ -252,12 +256,13 @@ __global__ void __launch_bounds__(1024) k_cscan_down(Bufs b, Ctrl* ctrl) {
 }
 
 void launch_cell_scan(const Bufs& b, Ctrl* ctrl, cudaStream_t st) {
-  k_cscan_reduce<<<SCAN_BLOCKS, 1024, 0, st>>>(b, ctrl);
-  k_cscan_down<<<SCAN_BLOCKS, 1024, 0, st>>>(b, ctrl);
+  launch_dep(k_cscan_reduce, dim3(SCAN_BLOCKS), dim3(1024), st, b, ctrl);
+  launch_dep(k_cscan_down, dim3(SCAN_BLOCKS), dim3(1024), st, b, ctrl);
 }
 
 // Particles into cell order: id, key, ensemble, position.
 __global__ void __launch_bounds__(SLOT_BLOCK) k_scatter(Bufs b, Ctrl* ctrl) {
+  pdl_wait();
   if (ctrl->halt) return;
   const uint32_t p = blockIdx.x * SLOT_BLOCK + threadIdx.x;
   if (p >= b.nslots) return;
@@ -272,7 +277,7 @@ __global__ void __launch_bounds__(SLOT_BLOCK) k_scatter(Bufs b, Ctrl* ctrl) {
 
 void launch_scatter(const Bufs& b, Ctrl* ctrl, cudaStream_t st) {
   if (b.nslots == 0) return;
-  k_scatter<<<(b.nslots + SLOT_BLOCK - 1) / SLOT_BLOCK, SLOT_BLOCK, 0, st>>>(b, ctrl);
+  launch_dep(k_scatter, dim3((b.nslots + SLOT_BLOCK - 1) / SLOT_BLOCK), dim3(SLOT_BLOCK), st, b, ctrl);
 }
 
 }  // namespace lm

@@ -121,6 +121,7 @@ __device__ __forceinline__ void append_active(const Bufs& b, Ctrl* ctrl, bool ac
 }
 
 __global__ void __launch_bounds__(SLOT_BLOCK) k_sweep(Bufs b, PairParams pp, StepArgs a, Ctrl* ctrl) {
+  pdl_wait();
   if (ctrl->halt) return;
   const uint32_t n_valid = ctrl->n_valid;
   const uint32_t step = a.use_ctrl_step ? ctrl->step : a.step0;
@@ -140,21 +141,27 @@ __global__ void __launch_bounds__(SLOT_BLOCK) k_sweep(Bufs b, PairParams pp, Ste
       nb[k] = NONE;
       pl[k] = NONE;
     }
+    // phase 1: collect the neighbours (compile-time slots, predicated); the divergent candidate
+    // loop does no more than the distance test
     for_neighbours(b, pp, v, [&](uint32_t t) {
-      if (m < SLAB) {  // append in registers (compile-time slots, predicated)
-        const uint32_t lb = b.sid[t] - v.base;
-        const unsigned long long p = pair_prio(min(la, lb), max(la, lb), step, k0, k1, v.ps, b.spos[t], pp.inv2r);
 #pragma unroll
-        for (int k = 0; k < (int)SLAB; ++k) {
-          if ((uint32_t)k == m) {
-            pr[k] = p;
-            nb[k] = t;
-            pl[k] = lb;
-          }
-        }
-      }
+      for (int k = 0; k < (int)SLAB; ++k)
+        if ((uint32_t)k == m) nb[k] = t;
       ++m;
     });
+    // phase 2: priorities over the slots, a loop whose trip count (the degree) is nearly the same
+    // across the warp
+    if (m <= SLAB) {
+#pragma unroll
+      for (int k = 0; k < (int)SLAB; ++k) {
+        if ((uint32_t)k < m) {
+          const uint32_t t = nb[k];
+          const uint32_t lb = b.sid[t] - v.base;
+          pr[k] = pair_prio(min(la, lb), max(la, lb), step, k0, k1, v.ps, b.spos[t], pp.inv2r);
+          pl[k] = lb;
+        }
+      }
+    }
     if (m > 1 && m <= SLAB) {
       // 19-comparator sorting network for 8 entries; empty slots (priority 0, partner NONE) sort last
 #define LM_CX(x, y)                                         \
@@ -209,7 +216,7 @@ __global__ void __launch_bounds__(SLOT_BLOCK) k_sweep(Bufs b, PairParams pp, Ste
 
 void launch_sweep(const Bufs& b, const PairParams& pp, const StepArgs& a, Ctrl* ctrl, cudaStream_t st) {
   if (b.nslots == 0) return;
-  k_sweep<<<(b.nslots + SLOT_BLOCK - 1) / SLOT_BLOCK, SLOT_BLOCK, 0, st>>>(b, pp, a, ctrl);
+  launch_dep(k_sweep, dim3((b.nslots + SLOT_BLOCK - 1) / SLOT_BLOCK), dim3(SLOT_BLOCK), st, b, pp, a, ctrl);
 }
 
 // In-place sort of one long list (priorities pr, cell-order neighbours nb) into `before` order.
@@ -261,54 +268,153 @@ __device__ void sort_segment(unsigned long long* __restrict__ pr, uint32_t* __re
   }
 }
 
-__global__ void __launch_bounds__(SLOT_BLOCK) k_sweep_long(Bufs b, PairParams pp, StepArgs a, Ctrl* ctrl) {
+// Long lists (more than SLAB neighbours): one warp per vertex. The warp reserves the overflow space
+// of 32 vertices at a time (one atomic per batch), gathers each vertex's neighbours with ballots
+// (lanes test 32 candidates of a row run at once), and sorts the list in shared memory with a
+// bitonic network over (priority, partner) pairs; lists longer than LONG_SMEM_MAX fall back to a
+// sort in global memory by one lane. Only the sorted partners are kept (the priorities were
+// needed for the order only).
+constexpr int LONG_WARPS = 8;
+constexpr uint32_t LONG_SMEM_MAX = 256;
+
+struct LongEntry {
+  unsigned long long p;  // pair priority
+  uint32_t id;           // partner's local id (ties)
+  uint32_t t;            // partner's cell-order index
+};
+
+__device__ __forceinline__ bool entry_before(const LongEntry& x, const LongEntry& y) { return before(x.p, x.id, y.p, y.id); }
+
+__global__ void __launch_bounds__(LONG_WARPS * 32) k_sweep_long(Bufs b, PairParams pp, StepArgs a, Ctrl* ctrl) {
+  pdl_wait();
   if (ctrl->halt) return;
+  __shared__ LongEntry sh_all[LONG_WARPS][LONG_SMEM_MAX];
+  const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+  LongEntry* sh = sh_all[w];
   const uint32_t n_long = ctrl->n_long;
   const uint32_t step = a.use_ctrl_step ? ctrl->step : a.step0;
-  const uint32_t stride = gridDim.x * SLOT_BLOCK;
-  const uint32_t lim = (n_long + 31u) & ~31u;
-  for (uint32_t x = blockIdx.x * SLOT_BLOCK + threadIdx.x; x < lim; x += stride) {
-    bool active = false;
-    uint32_t s = 0;
-    if (x < n_long) {
-      s = b.longv[x];
-      const uint32_t d = b.deg[s];
-      const unsigned long long o = atomicAdd(&ctrl->ovf_used, (unsigned long long)d);
-      if (d > MAX_DEGREE) {  // list positions no longer fit the state word
-        ctrl->halt = 1;
-        ctrl->halt_step = ctrl->step;
-        atomicOr(&ctrl->err, (uint32_t)ERRB_ROUNDCAP);
-      } else if (o + d > ctrl->ovf_cap) {  // the host regrows the overflow area and re-runs the step
-        ctrl->halt = 1;
-        ctrl->halt_step = ctrl->step;
-        atomicOr(&ctrl->err, (uint32_t)ERRB_OVERFLOW);
-      } else {
-        const Vertex v = load_vertex(b, s);
-        const EnsInfo& info = b.ens[v.e];
-        const uint32_t la = b.sid[s] - v.base;
-        uint32_t m = 0;
-        for_neighbours(b, pp, v, [&](uint32_t t) {
-          if (m < d) {
-            const uint32_t lb = b.sid[t] - v.base;
-            b.ovf[o + m] = t;
-            b.oprio[o + m] =
-                pair_prio(min(la, lb), max(la, lb), step, info.seed_lo, info.seed_hi, v.ps, b.spos[t], pp.inv2r);
+  const unsigned long long cap = ctrl->ovf_cap;
+  const uint32_t gw = blockIdx.x * LONG_WARPS + w, nw = gridDim.x * LONG_WARPS;
+  // this warp's vertices: gw, gw + nw, gw + 2 nw, ...; one atomic reserves the space of all of them
+  const uint32_t count = gw < n_long ? (n_long - gw + nw - 1) / nw : 0u;
+  if (count == 0) return;
+  unsigned long long sum = 0;
+  bool too_many = false;
+  for (uint32_t i = lane; i < count; i += 32) {
+    const uint32_t d = b.deg[b.longv[gw + i * nw]];
+    sum += d;
+    too_many |= d > MAX_DEGREE;
+  }
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  too_many = __any_sync(0xffffffffu, too_many);
+  unsigned long long run = 0;
+  if (lane == 0) run = atomicAdd(&ctrl->ovf_used, sum);
+  run = __shfl_sync(0xffffffffu, run, 0);
+  if (too_many || run + sum > cap) {  // positions would not fit the state word / the area is full
+    if (lane == 0) {
+      ctrl->halt = 1;
+      ctrl->halt_step = ctrl->step;
+      atomicOr(&ctrl->err, too_many ? (uint32_t)ERRB_ROUNDCAP : (uint32_t)ERRB_OVERFLOW);
+    }
+    return;
+  }
+  for (uint32_t ib = 0; ib < count; ib += 32) {
+    // lane k holds vertex ib + k of this warp's list
+    const bool mine = ib + lane < count;
+    const uint32_t s_l = mine ? b.longv[gw + (ib + lane) * nw] : 0u;
+    const uint32_t d_l = mine ? b.deg[s_l] : 0u;
+    unsigned long long incl = d_l;
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= (uint32_t)o) incl += y;
+    }
+    const unsigned long long o_l = run + incl - d_l;
+    run += __shfl_sync(0xffffffffu, incl, 31);
+    const uint32_t nk = min(32u, count - ib);
+    for (uint32_t k = 0; k < nk; ++k) {
+      const uint32_t s = __shfl_sync(0xffffffffu, s_l, k);
+      const uint32_t d = __shfl_sync(0xffffffffu, d_l, k);
+      const unsigned long long o = __shfl_sync(0xffffffffu, o_l, k);
+      const Vertex v = load_vertex(b, s);
+      const EnsInfo& info = b.ens[v.e];
+      const uint32_t la = b.sid[s] - v.base;
+      const bool in_smem = d <= LONG_SMEM_MAX;
+      uint32_t m = 0;
+      for (int dy = -1; dy <= 1; ++dy) {
+        const int ry = (int)v.cy + dy;
+        if (ry < 0 || ry >= v.g.ncy) continue;
+        const uint32_t row = v.g.cell_base + (uint32_t)ry * (uint32_t)v.g.ncx;
+        const uint32_t kl = row + (uint32_t)max((int)v.cx - 1, 0);
+        const uint32_t kh = row + (uint32_t)min((int)v.cx + 1, v.g.ncx - 1);
+        const uint32_t t0 = b.cstart[kl], t1 = b.cstart[kh + 1];
+        for (uint32_t tb = t0; tb < t1; tb += 32) {
+          const uint32_t t = tb + lane;
+          const bool ok = t < t1 && t != s && within(pp, v.ps, b.spos[t]);
+          const uint32_t mask = __ballot_sync(0xffffffffu, ok);
+          if (ok) {
+            const uint32_t pos = m + __popc(mask & lanemask_lt_p());
+            if (pos < d) {
+              const uint32_t lb = b.sid[t] - v.base;
+              const unsigned long long p =
+                  pair_prio(min(la, lb), max(la, lb), step, info.seed_lo, info.seed_hi, v.ps, b.spos[t], pp.inv2r);
+              if (in_smem) {
+                sh[pos] = LongEntry{p, lb, t};
+              } else {
+                b.ovf[o + pos] = t;
+                b.oprio[o + pos] = p;
+              }
+            }
           }
-          ++m;
-        });
-        sort_segment(b.oprio + o, b.ovf + o, b.sid, d);
+          m += __popc(mask);
+        }
+      }
+      uint32_t first;
+      if (in_smem) {
+        uint32_t n2 = 32;
+        while (n2 < d) n2 <<= 1;
+        for (uint32_t i = d + lane; i < n2; i += 32) sh[i] = LongEntry{0ull, NONE, NONE};  // sort last
+        __syncwarp();
+        for (uint32_t kk = 2; kk <= n2; kk <<= 1) {
+          for (uint32_t j = kk >> 1; j > 0; j >>= 1) {
+            for (uint32_t i = lane; i < n2; i += 32) {
+              const uint32_t l = i ^ j;
+              if (l > i) {
+                const LongEntry x = sh[i], y = sh[l];
+                const bool up = (i & kk) == 0;
+                if (up ? entry_before(y, x) : entry_before(x, y)) {
+                  sh[i] = y;
+                  sh[l] = x;
+                }
+              }
+            }
+            __syncwarp();
+          }
+        }
+        for (uint32_t i = lane; i < d; i += 32) b.ovf[o + i] = sh[i].t;
+        first = sh[0].t;
+        __syncwarp();  // the next vertex reuses the shared list
+      } else {
+        __syncwarp();
+        if (lane == 0) sort_segment(b.oprio + o, b.ovf + o, b.sid, d);
+        __syncwarp();
+        first = b.ovf[o];
+      }
+      if (lane == 0) {
         b.off[s] = (uint32_t)o;
-        b.wstate[s] = pack_state(b.ovf[o], 0u, b.species[b.sid[s]]);  // entry 0 of the list
-        active = true;
+        b.wstate[s] = pack_state(first, 0u, b.species[b.sid[s]]);  // entry 0 of the list
       }
     }
-    append_active(b, ctrl, active, s);
+    // every vertex of the batch is active (it has > SLAB pairs): one atomic per batch
+    uint32_t at = 0;
+    if (lane == 0) at = atomicAdd(&ctrl->act_n, nk);
+    at = __shfl_sync(0xffffffffu, at, 0);
+    if (lane < nk) b.act[at + lane] = s_l;
   }
 }
 
 void launch_sweep_long(const Bufs& b, const PairParams& pp, const StepArgs& a, Ctrl* ctrl, int sms,
                        cudaStream_t st) {
-  k_sweep_long<<<sms * 4, SLOT_BLOCK, 0, st>>>(b, pp, a, ctrl);
+  launch_dep(k_sweep_long, dim3(sms * 4), dim3(LONG_WARPS * 32), st, b, pp, a, ctrl);
 }
 
 }  // namespace lm

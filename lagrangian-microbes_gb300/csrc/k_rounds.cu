@@ -120,6 +120,7 @@ __device__ __forceinline__ uint32_t apply_pair(const Bufs& b, uint32_t step, uin
 constexpr int POLL_BATCH = 4;  // vertices whose state words one thread loads before testing them
 
 __global__ void __launch_bounds__(RD_THREADS) k_rounds(Bufs b, StepArgs a, Ctrl* ctrl) {
+  pdl_wait();
   if (((volatile uint32_t*)&ctrl->halt)[0]) return;
   const uint32_t step = a.use_ctrl_step ? ctrl->step : a.step0;
   const uint32_t cnt = ((volatile uint32_t*)&ctrl->act_n)[0];
@@ -194,6 +195,7 @@ cudaError_t launch_rounds(const Bufs& b, const StepArgs& a, Ctrl* ctrl, int grid
 
 // Species counts after the step, per ensemble and in total ([0] collects values outside 1..3).
 __global__ void __launch_bounds__(SLOT_BLOCK) k_census(Bufs b, Ctrl* ctrl) {
+  pdl_wait();
   if (ctrl->halt) return;
   __shared__ uint32_t h[4];
   if (threadIdx.x < 4) h[threadIdx.x] = 0;
@@ -218,7 +220,7 @@ __global__ void __launch_bounds__(SLOT_BLOCK) k_census(Bufs b, Ctrl* ctrl) {
 
 void launch_census(const Bufs& b, Ctrl* ctrl, cudaStream_t st) {
   if (b.nslots == 0) return;
-  k_census<<<(b.nslots + SLOT_BLOCK - 1) / SLOT_BLOCK, SLOT_BLOCK, 0, st>>>(b, ctrl);
+  launch_dep(k_census, dim3((b.nslots + SLOT_BLOCK - 1) / SLOT_BLOCK), dim3(SLOT_BLOCK), st, b, ctrl);
 }
 
 }  // namespace lm

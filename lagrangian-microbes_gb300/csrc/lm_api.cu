@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -1169,6 +1170,13 @@ int lm_profile_count(void) { return P_COUNT; }
 
 namespace lm {
 void set_thread_error(const char* msg) { g_create_error = msg ? msg : ""; }
+bool pdl_enabled() {
+  static const bool on = [] {
+    const char* v = std::getenv("LM_PDL");
+    return !(v && v[0] == '0');
+  }();
+  return on;
+}
 int ctx_device(const lm_ctx* c) { return c->device; }
 int ctx_sms(const lm_ctx* c) { return c->sms; }
 cudaStream_t ctx_stream(const lm_ctx* c) { return c->st; }

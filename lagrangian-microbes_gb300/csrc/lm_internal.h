@@ -21,6 +21,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <utility>
+
 struct lm_ctx;
 
 namespace lm {
@@ -163,6 +165,38 @@ struct Bufs {
   uint32_t* plog;     // 3 x uint32 per logged pair (slot i, slot j, level) or nullptr
   uint32_t plog_cap;
 };
+
+// ---- programmatic dependent launch ----
+// Per-step kernels start with pdl_wait() and are launched with launch_dep(): the next kernel's
+// launch and block setup then overlap the tail of the previous one, and griddepcontrol.wait holds
+// its threads until the previous grid has completed and its memory is visible. A kernel launched
+// without the attribute passes the wait at once. The cooperative interaction kernel is launched
+// without it (its blocks must all be resident together), and so is everything captured into a
+// CUDA graph: graphs already remove the launch overhead, and there the attribute measured neutral
+// to slightly slower.
+__device__ __forceinline__ void pdl_wait() {
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 900
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+#endif
+}
+bool pdl_enabled();  // off when the environment sets LM_PDL=0
+
+template <typename... KArgs, typename... Args>
+inline void launch_dep(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStream_t st, Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  cudaStreamIsCapturing(st, &cap);
+  cfg.numAttrs = (pdl_enabled() && cap == cudaStreamCaptureStatusNone) ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 // ---- launchers (each enqueues on `st`) ----
 void launch_interleave(const float* u, const float* v, float2* uv, size_t n, cudaStream_t st);

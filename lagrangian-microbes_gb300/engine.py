@@ -196,6 +196,19 @@ class EnsembleSimulation(Simulation):
         flds = fields if isinstance(fields, (list, tuple)) else [fields]
         self.field = flds[0]
         self.upload_fields(flds)
+        self.upload_ensembles(ensembles)
+        e = self.n_ensembles
+        as_arr = lambda v, dt: np.ascontiguousarray(np.broadcast_to(np.asarray(v, dtype=dt), (e,)))
+        seeds_u = np.array([int(x) & 0xFFFFFFFFFFFFFFFF for x in np.broadcast_to(np.asarray(seeds, dtype=object), (e,))],
+                           dtype=np.uint64)
+        self.ctx.call("lm_set_interaction", float(radius), norm_code(norm), 0.5, 0.5, 0.5, 0)
+        self.ctx.call("lm_set_ensemble_params", e, _lib.ptr(as_arr(p_rs, np.float64)), _lib.ptr(as_arr(p_pr, np.float64)),
+                      _lib.ptr(as_arr(p_sp, np.float64)), _lib.ptr(seeds_u))
+        self.step_index = 0
+        self._graph = None
+
+    def upload_ensembles(self, ensembles) -> None:
+        """(Re)place the microbes of every ensemble: a list of (lons, lats, species)."""
         e = len(ensembles)
         self.counts = np.array([np.asarray(x[0]).size for x in ensembles], dtype=np.int64)
         lons = np.concatenate([np.asarray(x[0], np.float64).ravel() for x in ensembles]) if e else np.zeros(0)
@@ -205,14 +218,6 @@ class EnsembleSimulation(Simulation):
                       _lib.ptr(sp))
         self.n = int(self.counts.sum())
         self.n_ensembles = e
-        as_arr = lambda v, dt: np.ascontiguousarray(np.broadcast_to(np.asarray(v, dtype=dt), (e,)))
-        seeds_u = np.array([int(x) & 0xFFFFFFFFFFFFFFFF for x in np.broadcast_to(np.asarray(seeds, dtype=object), (e,))],
-                           dtype=np.uint64)
-        self.ctx.call("lm_set_interaction", float(radius), norm_code(norm), 0.5, 0.5, 0.5, 0)
-        self.ctx.call("lm_set_ensemble_params", e, _lib.ptr(as_arr(p_rs, np.float64)), _lib.ptr(as_arr(p_pr, np.float64)),
-                      _lib.ptr(as_arr(p_sp, np.float64)), _lib.ptr(seeds_u))
-        self.step_index = 0
-        self._graph = None
 
     def upload_fields(self, flds) -> None:
         f0 = flds[0]
