@@ -253,9 +253,11 @@ def run_gb300(args):
     if not args.no_e2e:
         e2e = run_e2e(fld, lons, lats, species, K, spg, local, stream)
 
-    batched = adjoint = None
+    batched = adjoint = stress = None
     if rank == 0 and not args.no_batched:
         batched = run_batched(local, stream)
+    if rank == 0 and not args.no_stress:
+        stress = run_stress(fld, local)
     if rank == 0 and not args.no_adjoint:
         adjoint = run_adjoint(fld, local)
 
@@ -277,7 +279,7 @@ def run_gb300(args):
             "plain": {"value": plain_value, "unit": "microbe-steps/s", "sim_steps": plain_steps,
                       "graph_speedup": value / world / plain_value},
             "roofline": roofline, "whole_step": whole, "kernels": kernels,
-            "e2e": e2e, "cpu_baseline": cpu, "clocks": clk, "batched": batched, "adjoint": adjoint,
+            "e2e": e2e, "cpu_baseline": cpu, "clocks": clk, "batched": batched, "adjoint": adjoint, "stress": stress,
             "gpu_launches": int(round(launches_per_step * K)),
             "max_rounds": stats["max_rounds"],
             "mean_rounds": stats["rounds_total"] / max(stats["steps_total"], 1),
@@ -456,6 +458,65 @@ def run_adjoint(fld, local: int):
     return out
 
 
+X_MICROBES = 16_000_000
+X_CLUSTERS = 2000
+X_STEPS = 3
+X_WORKLOAD = ("16M microbes in 2,000 Gaussian clusters (sigma 0.03 deg = 3 km at 100 km/deg, centres uniform over "
+              "200-210E x 25-35N, sizes rank-size Zipf(1.2) normalised to 16M), 1/12 deg hourly psi field, RK4 dt=1h, "
+              "r=0.01 deg, count-only pairs (no lists, no interaction)")
+
+
+def make_clusters(n: int = X_MICROBES, k: int = X_CLUSTERS, seed: int = 2026):
+    """The neighbour-search stress configuration's positions (seeded)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    w = np.arange(1, k + 1, dtype=np.float64) ** -1.2
+    sizes = np.floor(n * w / w.sum()).astype(np.int64)
+    sizes[: n - sizes.sum()] += 1  # exactly n
+    cx = rng.uniform(200.0, 210.0, k)
+    cy = rng.uniform(25.0, 35.0, k)
+    lon = np.repeat(cx, sizes) + 0.03 * rng.standard_normal(n)
+    lat = np.repeat(cy, sizes) + 0.03 * rng.standard_normal(n)
+    return lon, lat, sizes
+
+
+def run_stress(fld, local: int):
+    """Config X: advect -> bin -> count pairs, per-kernel CUDA events; binning HBM GB/s."""
+    import numpy as np
+
+    from lagrangian_microbes_gb300.engine import Simulation
+    lons, lats, sizes = make_clusters()
+    n = lons.size
+    sim = Simulation(fld, lons, lats, np.ones(n, np.int8), radius=RADIUS, device=local)
+    sim.step(0.0, DT, 1, step0=0, count_pairs=True)  # warm-up
+    sim.upload_particles(lons, lats, np.ones(n, np.int8))
+    sim.ctx.call("lm_stats_reset")
+    sim.ctx.profile_enable(True)
+    t0 = time.perf_counter()
+    sim.step(0.0, DT, X_STEPS, step0=0, count_pairs=True)
+    wall = time.perf_counter() - t0
+    prof = sim.ctx.profile()
+    sim.ctx.profile_enable(False)
+    st = sim.stats()
+    cells = float(st["cells"])
+    sim.close()
+    per = {k: 1e3 * ms / cnt for k, (ms, cnt) in prof.items() if cnt}
+    bin_kernels = ("k_grid", "k_keys", "k_cscan", "k_scatter")
+    bin_us = sum(per.get(k, 0.0) for k in bin_kernels)
+    bin_bytes = sum(kernel_bytes(k, n, 0.0, 0, 2, cells) for k in bin_kernels)
+    peak, kind = measured_peaks()
+    pairs = st["pairs_total"] / max(st["steps_total"], 1)
+    return {"workload": X_WORKLOAD, "microbes": n, "largest_cluster": int(sizes.max()), "sim_steps": X_STEPS,
+            "pairs_per_step": pairs, "ms_per_step": 1e3 * wall / X_STEPS,
+            "value": n * X_STEPS / wall, "unit": "microbe-steps/s (count-only pipeline, plain launches)",
+            "kernels_us": per,
+            "binning": {"kernels": list(bin_kernels), "us_per_step": bin_us, "algorithmic_bytes": bin_bytes,
+                        "gbs": bin_bytes / (bin_us * 1e-6) / 1e9 if bin_us else None, "peak_gbs": peak,
+                        "frac": (bin_bytes / (bin_us * 1e-6) / 1e9) / peak if bin_us else None, "peak_source": kind},
+            "count": {"us_per_step": per.get("k_count_pairs"),
+                      "pairs_per_s": pairs / (per["k_count_pairs"] * 1e-6) if per.get("k_count_pairs") else None}}
+
+
 def cpu_threads():
     try:
         return len(os.sched_getaffinity(0))
@@ -531,6 +592,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the 256-ensemble batching measurement")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint (differentiation) timing")
+    ap.add_argument("--no-stress", action="store_true", help="skip the 16M clustered count-only measurement")
     ap.add_argument("--profile-run", action="store_true", help="only the warm-up and timed graph launches")
     ap.add_argument("--traffic-json", default=os.path.join(REPO, "profiles", "traffic.json"))
     args = ap.parse_args()

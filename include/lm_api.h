@@ -47,6 +47,8 @@ extern "C" {
 #define LM_STEP_INTERACT 2u   /* bin -> pair -> rock-paper-scissors rounds */
 #define LM_STEP_CENSUS 4u     /* species counts after each step */
 #define LM_STEP_LOG_PAIRS 8u  /* keep (i, j, round) of every pair applied in the last step */
+#define LM_STEP_COUNT_PAIRS 16u /* bin -> count the pairs within the radius, no lists and no interaction
+                                   (instead of LM_STEP_INTERACT; the counts land in lm_stats) */
 
 /* Norm codes for lm_set_interaction (cKDTree's Minkowski p). */
 #define LM_NORM_INF 0
@@ -148,6 +150,10 @@ int lm_step(lm_ctx* ctx, double t_sec, double dt_sec, int n_steps, int64_t step0
 int lm_query_pairs(lm_ctx* ctx, int64_t n, const float* lon, const float* lat, int32_t* pi, int32_t* pj,
                    int64_t cap, int64_t* n_pairs);
 
+/* Number of unordered pairs within the radius of lm_set_interaction, the size of
+ * cKDTree(X).query_pairs(r, p) (interaction_simulator.py:93-98), without listing them: for
+ * positions whose pair set is too large to hold. Pair semantics are lm_query_pairs'. */
+int lm_count_pairs(lm_ctx* ctx, int64_t n, const float* lon, const float* lat, int64_t* n_pairs);
 /* One interaction step on externally supplied float32 positions (the interaction phase of the
  * reference, interaction_simulator.py:83-117: pairs + pair loop), updating the context's species in
  * place; step_index keys the Philox draws. n must equal the particle count of the species array. */

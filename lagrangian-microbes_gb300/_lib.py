@@ -31,6 +31,7 @@ STEP_ADVECT = 1
 STEP_INTERACT = 2
 STEP_CENSUS = 4
 STEP_LOG_PAIRS = 8
+STEP_COUNT_PAIRS = 16
 
 NORM_INF = 0
 NORM_L1 = 1
@@ -111,6 +112,7 @@ SIGNATURES = {
     "lm_set_interaction": [P, F64, I32, F64, F64, F64, U64],
     "lm_step": [P, F64, F64, I32, I64, U32, F64, P, P, P, P],
     "lm_query_pairs": [P, I64, P, P, P, P, I64, ctypes.POINTER(I64)],
+    "lm_count_pairs": [P, I64, P, P, ctypes.POINTER(I64)],
     "lm_interact": [P, I64, P, P, I64, U32],
     "lm_pairs_get": [P, P, P, P, I64, ctypes.POINTER(I64)],
     "lm_graph_capture": [P, F64, F64, I64, I32, U32, F64],

@@ -219,6 +219,94 @@ void launch_sweep(const Bufs& b, const PairParams& pp, const StepArgs& a, Ctrl* 
   launch_dep(k_sweep, dim3((b.nslots + SLOT_BLOCK - 1) / SLOT_BLOCK), dim3(SLOT_BLOCK), st, b, pp, a, ctrl);
 }
 
+// Count-only pair search (the clustered stress workload, whose 1e11+ pairs per step cannot be
+// listed): every unordered pair within the radius is counted once, with the same cell grid and
+// the same distance test as the sweep. Microbe a (cell order) tests the members of its own cell
+// with a higher cell-order index and every member of its four "forward" cells: (cx+1, cy) and the
+// three cells of row cy+1 (cx-1 .. cx+1, one contiguous run). A block whose 256 microbes all lie
+// in one cell (cluster cores, thousands per cell) walks those runs through shared-memory tiles;
+// any other block lets each thread walk its own runs. Counts are summed per block and added to
+// the step's directed-entry counter (2 per pair) with one atomic.
+constexpr uint32_t COUNT_THREADS = 256;
+
+__device__ __forceinline__ void count_runs(const Vertex& v, const Bufs& b, uint32_t* r0, uint32_t* r1) {
+  // r[0] = the rest of the own cell, r[1] = (cx+1, cy), r[2] = row cy+1 from cx-1 to cx+1
+  const uint32_t kc = v.g.cell_base + v.cy * (uint32_t)v.g.ncx + v.cx;
+  r0[0] = v.s + 1;
+  r1[0] = b.cstart[kc + 1];
+  if ((int)v.cx + 1 < v.g.ncx) {
+    r0[1] = b.cstart[kc + 1];
+    r1[1] = b.cstart[kc + 2];
+  } else {
+    r0[1] = r1[1] = 0;
+  }
+  if ((int)v.cy + 1 < v.g.ncy) {
+    const uint32_t row = v.g.cell_base + (v.cy + 1) * (uint32_t)v.g.ncx;
+    const uint32_t kl = row + (uint32_t)max((int)v.cx - 1, 0);
+    const uint32_t kh = row + (uint32_t)min((int)v.cx + 1, v.g.ncx - 1);
+    r0[2] = b.cstart[kl];
+    r1[2] = b.cstart[kh + 1];
+  } else {
+    r0[2] = r1[2] = 0;
+  }
+}
+
+__global__ void __launch_bounds__(COUNT_THREADS) k_count_pairs(Bufs b, PairParams pp, Ctrl* ctrl) {
+  pdl_wait();
+  if (ctrl->halt) return;
+  __shared__ float2 tile[COUNT_THREADS];
+  __shared__ uint32_t first_key, last_key;
+  __shared__ unsigned long long tot;
+  const uint32_t n_valid = ctrl->n_valid;
+  const uint32_t blk0 = blockIdx.x * COUNT_THREADS;
+  if (blk0 >= n_valid) return;  // block-uniform
+  const uint32_t s = blk0 + threadIdx.x;
+  const uint32_t last = min(n_valid, blk0 + COUNT_THREADS) - 1;
+  if (threadIdx.x == 0) {
+    first_key = b.skey[blk0];
+    last_key = b.skey[last];
+    tot = 0;
+  }
+  __syncthreads();
+  unsigned long long cnt = 0;
+  const bool dense = first_key == last_key && last - blk0 + 1 == COUNT_THREADS;
+  if (dense) {
+    // all 256 microbes share one cell and hence the same forward runs; the own-cell run starts
+    // after the block's first microbe, each thread keeps only partners with a higher index
+    const Vertex v = load_vertex(b, blk0);
+    uint32_t r0[3], r1[3];
+    count_runs(v, b, r0, r1);
+    const float2 me = b.spos[s];
+    for (int q = 0; q < 3; ++q) {
+      for (uint32_t tb = r0[q]; tb < r1[q]; tb += COUNT_THREADS) {
+        const uint32_t n_t = min(COUNT_THREADS, r1[q] - tb);
+        if (threadIdx.x < n_t) tile[threadIdx.x] = b.spos[tb + threadIdx.x];
+        __syncthreads();
+        // own cell: partner index tb + k must exceed s
+        const uint32_t k0 = q == 0 ? (s + 1 > tb ? min(s + 1 - tb, n_t) : 0u) : 0u;
+        for (uint32_t k = k0; k < n_t; ++k) cnt += within(pp, me, tile[k]) ? 1u : 0u;
+        __syncthreads();
+      }
+    }
+  } else if (s < n_valid) {
+    const Vertex v = load_vertex(b, s);
+    uint32_t r0[3], r1[3];
+    count_runs(v, b, r0, r1);
+    for (int q = 0; q < 3; ++q)
+      for (uint32_t t = r0[q]; t < r1[q]; ++t) cnt += within(pp, v.ps, b.spos[t]) ? 1u : 0u;
+  }
+  for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+  if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(&tot, cnt);
+  __syncthreads();
+  if (threadIdx.x == 0 && tot) atomicAdd(&ctrl->n_dir, 2ull * tot);
+}
+
+void launch_count_pairs(const Bufs& b, const PairParams& pp, Ctrl* ctrl, cudaStream_t st) {
+  if (b.nslots == 0) return;
+  launch_dep(k_count_pairs, dim3((b.nslots + COUNT_THREADS - 1) / COUNT_THREADS), dim3(COUNT_THREADS), st, b, pp,
+             ctrl);
+}
+
 // In-place sort of one long list (priorities pr, cell-order neighbours nb) into `before` order.
 __device__ void sort_segment(unsigned long long* __restrict__ pr, uint32_t* __restrict__ nb,
                              const uint32_t* __restrict__ sid, uint32_t d) {

@@ -22,11 +22,11 @@ thread_local std::string g_create_error;
 
 enum ProfId {
   P_ADVECT, P_BBOX, P_GRID, P_KEYS, P_CELL_SCAN, P_SCATTER, P_SWEEP, P_SWEEP_LONG, P_ROUNDS, P_CENSUS,
-  P_BOOKKEEPING, P_COUNT
+  P_BOOKKEEPING, P_COUNT, P_NUM
 };
-const char* const kProfNames[P_COUNT] = {"k_advect",     "k_bbox",       "k_grid",   "k_keys",
-                                         "k_cscan",      "k_scatter",    "k_sweep",  "k_sweep_long",
-                                         "k_rounds",     "k_census",     "k_step_begin_end"};
+const char* const kProfNames[P_NUM] = {"k_advect", "k_bbox",   "k_grid",       "k_keys",   "k_cscan",
+                                       "k_scatter", "k_sweep", "k_sweep_long", "k_rounds", "k_census",
+                                       "k_step_begin_end", "k_count_pairs"};
 }  // namespace
 
 struct lm_ctx {
@@ -121,8 +121,8 @@ struct lm_ctx {
     cudaEvent_t a, b;
   };
   std::vector<Pend> pend;
-  double prof_ms[P_COUNT] = {};
-  int64_t prof_n[P_COUNT] = {};
+  double prof_ms[P_NUM] = {};
+  int64_t prof_n[P_NUM] = {};
 };
 
 namespace {
@@ -454,6 +454,10 @@ cudaError_t enqueue_interaction(lm_ctx* c, const StepArgs& a, uint32_t flags, bo
   PROF(c, P_KEYS, launch_keys(b, c->ctrl, use_status, st));
   PROF(c, P_CELL_SCAN, launch_cell_scan(b, c->ctrl, st));
   PROF(c, P_SCATTER, launch_scatter(b, c->ctrl, st));
+  if (flags & LM_STEP_COUNT_PAIRS) {  // count-only: no lists, no interaction
+    PROF(c, P_COUNT, launch_count_pairs(b, c->pp, c->ctrl, st));
+    return cudaGetLastError();
+  }
   PROF(c, P_SWEEP, launch_sweep(b, c->pp, a, c->ctrl, st));
   PROF(c, P_SWEEP_LONG, launch_sweep_long(b, c->pp, a, c->ctrl, c->sms, st));
   if (flags & LM_STEP_INTERACT) {
@@ -470,12 +474,13 @@ cudaError_t enqueue_step(lm_ctx* c, const StepArgs& a, uint32_t flags, bool adve
   const Bufs b = bufs(c, false);
   PROF(c, P_BOOKKEEPING, launch_step_begin(b, advect ? &c->fv : nullptr, a, c->ctrl, c->st));
   if (advect) PROF(c, P_ADVECT, launch_advect(c->fv, a, b, c->ctrl, c->st));
-  if (flags & LM_STEP_INTERACT) {
+  if (flags & (LM_STEP_INTERACT | LM_STEP_COUNT_PAIRS)) {
     cudaError_t e = enqueue_interaction(c, a, flags, !advect, true);
     if (e != cudaSuccess) return e;
   }
   if (flags & LM_STEP_CENSUS) PROF(c, P_CENSUS, launch_census(b, c->ctrl, c->st));
-  PROF(c, P_BOOKKEEPING, launch_step_end(c->ctrl, (flags & LM_STEP_INTERACT) != 0, c->st));
+  PROF(c, P_BOOKKEEPING,
+       launch_step_end(c->ctrl, (flags & (LM_STEP_INTERACT | LM_STEP_COUNT_PAIRS)) != 0, c->st));
   return cudaGetLastError();
 }
 
@@ -618,7 +623,10 @@ int capture(lm_ctx* c) {
 int check_ready(lm_ctx* c, uint32_t flags) {
   if (!(flags & LM_STEP_ADVECT)) return fail(c, LM_ERR_ARG, "steps need LM_STEP_ADVECT (use lm_interact)");
   if (!c->has_field || !c->has_particles) return fail(c, LM_ERR_STATE, "field and particles must be uploaded first");
-  if ((flags & LM_STEP_INTERACT) && !c->has_params) return fail(c, LM_ERR_STATE, "call lm_set_interaction first");
+  if ((flags & (LM_STEP_INTERACT | LM_STEP_COUNT_PAIRS)) && !c->has_params)
+    return fail(c, LM_ERR_STATE, "call lm_set_interaction first");
+  if ((flags & LM_STEP_INTERACT) && (flags & LM_STEP_COUNT_PAIRS))
+    return fail(c, LM_ERR_ARG, "LM_STEP_COUNT_PAIRS replaces the interaction: pass one of the two");
   if (c->n_fields != 1 && c->n_fields != (int)c->n_ens)
     return fail(c, LM_ERR_STATE, "%d fields for %u ensembles (need 1 or one per ensemble)", c->n_fields, c->n_ens);
   return LM_OK;
@@ -965,6 +973,25 @@ int lm_query_pairs(lm_ctx* c, int64_t n, const float* lon, const float* lat, int
   return LM_OK;
 }
 
+int lm_count_pairs(lm_ctx* c, int64_t n, const float* lon, const float* lat, int64_t* n_pairs) {
+  if (!c || !n_pairs || (n > 0 && (!lon || !lat))) return fail(c, LM_ERR_ARG, "NULL argument");
+  if (n < 0 || n > 0x7fffff00) return fail(c, LM_ERR_ARG, "particle count out of range");
+  if (!c->has_params) return fail(c, LM_ERR_STATE, "call lm_set_interaction first");
+  CK(cudaSetDevice(c->device));
+  *n_pairs = 0;
+  if (n == 0) return LM_OK;
+  int r;
+  if ((r = stage_positions(c, n, lon, lat))) return r;
+  c->has_particles = false;  // positions now hold query points, not an advected state
+  const StepArgs a = step_args(0.0, 1.0, 0, 0.0, false);
+  PROF(c, P_BOOKKEEPING, launch_step_begin(bufs(c, false), nullptr, a, c->ctrl, c->st));
+  CK(enqueue_interaction(c, a, LM_STEP_COUNT_PAIRS, true, false));
+  if ((r = read_ctrl(c))) return r;
+  if ((r = clear_err_bits(c, ERRB_NAN))) return r;  // non-finite query points are never paired
+  *n_pairs = (int64_t)(c->hctrl->n_dir / 2);
+  return LM_OK;
+}
+
 int lm_interact(lm_ctx* c, int64_t n, const float* lon, const float* lat, int64_t step_index, uint32_t flags) {
   if (!c || (n > 0 && (!lon || !lat))) return fail(c, LM_ERR_ARG, "NULL argument");
   if (!c->has_params) return fail(c, LM_ERR_STATE, "call lm_set_interaction first");
@@ -1144,7 +1171,7 @@ int lm_profile_enable(lm_ctx* c, int on) {
   CK(cudaSetDevice(c->device));
   CK(cudaStreamSynchronize(c->st));
   prof_collect(c);
-  for (int k = 0; k < P_COUNT; ++k) {
+  for (int k = 0; k < P_NUM; ++k) {
     c->prof_ms[k] = 0;
     c->prof_n[k] = 0;
   }
@@ -1154,7 +1181,7 @@ int lm_profile_enable(lm_ctx* c, int on) {
 
 int lm_profile_get(lm_ctx* c, int kernel, char* name, size_t name_len, double* total_ms, int64_t* launches) {
   if (!c) return LM_ERR_ARG;
-  if (kernel < 0 || kernel >= P_COUNT) return fail(c, LM_ERR_ARG, "kernel index %d out of range [0, %d)", kernel, P_COUNT);
+  if (kernel < 0 || kernel >= P_NUM) return fail(c, LM_ERR_ARG, "kernel index %d out of range [0, %d)", kernel, P_NUM);
   CK(cudaSetDevice(c->device));
   CK(cudaStreamSynchronize(c->st));
   prof_collect(c);
@@ -1164,7 +1191,7 @@ int lm_profile_get(lm_ctx* c, int kernel, char* name, size_t name_len, double* t
   return LM_OK;
 }
 
-int lm_profile_count(void) { return P_COUNT; }
+int lm_profile_count(void) { return P_NUM; }
 
 }  // extern "C"
 

@@ -215,6 +215,7 @@ void launch_scatter(const Bufs& b, Ctrl* ctrl, cudaStream_t st);
 
 // K3 neighbour lists.
 void launch_sweep(const Bufs& b, const PairParams& pp, const StepArgs& a, Ctrl* ctrl, cudaStream_t st);
+void launch_count_pairs(const Bufs& b, const PairParams& pp, Ctrl* ctrl, cudaStream_t st);
 void launch_sweep_long(const Bufs& b, const PairParams& pp, const StepArgs& a, Ctrl* ctrl, int sms,
                        cudaStream_t st);
 

@@ -15,7 +15,8 @@ from datetime import datetime, timedelta
 import numpy as np
 
 from . import _lib
-from ._lib import NORM_INF, NORM_L1, NORM_L2, STEP_ADVECT, STEP_CENSUS, STEP_INTERACT, STEP_LOG_PAIRS
+from ._lib import (NORM_INF, NORM_L1, NORM_L2, STEP_ADVECT, STEP_CENSUS, STEP_COUNT_PAIRS, STEP_INTERACT,
+                   STEP_LOG_PAIRS)
 from .fields import VelocityField
 
 
@@ -99,10 +100,15 @@ class Simulation:
 
     # ---- stepping ----
     def step(self, t0, dt, n_steps: int, interact: bool = True, census: bool = False, log_pairs: bool = False,
-             record: bool = False, step0: int | None = None):
-        """Run n_steps plain steps from field time t0. Returns a dict of the requested records."""
+             record: bool = False, step0: int | None = None, count_pairs: bool = False):
+        """Run n_steps plain steps from field time t0. Returns a dict of the requested records.
+
+        ``count_pairs`` replaces the interaction by a count of the pairs within the radius (no lists):
+        the count of the last step is ``stats()["pairs"]``, their sum ``stats()["pairs_total"]``."""
         n = self.n
+        interact = interact and not count_pairs
         flags = STEP_ADVECT | (STEP_INTERACT if interact else 0) | (STEP_CENSUS if census else 0)
+        flags |= STEP_COUNT_PAIRS if count_pairs else 0
         flags |= STEP_LOG_PAIRS if log_pairs else 0
         rec_lon = rec_lat = rec_sp = rec_c = None
         if record:
@@ -123,10 +129,12 @@ class Simulation:
         return out
 
     def capture(self, t_start, dt, steps_per_graph: int, interact: bool = True, census: bool = False,
-                step0: int | None = None) -> None:
+                step0: int | None = None, count_pairs: bool = False) -> None:
         """Capture steps_per_graph fused steps as one CUDA graph (time origin t_start at step0)."""
         s0 = self.step_index if step0 is None else int(step0)
+        interact = interact and not count_pairs
         flags = STEP_ADVECT | (STEP_INTERACT if interact else 0) | (STEP_CENSUS if census else 0)
+        flags |= STEP_COUNT_PAIRS if count_pairs else 0
         self.ctx.call("lm_graph_capture", self._t(t_start), self._dt(dt), s0, int(steps_per_graph), flags, self.kh)
         self.step_index = s0
         self._graph = int(steps_per_graph)
@@ -274,3 +282,11 @@ class PairQuery:
             break
         m = n.value
         return pi[:m].astype(np.int64), pj[:m].astype(np.int64)
+
+    def count(self, lon, lat) -> int:
+        """Number of pairs, without listing them (cKDTree.query_pairs' size)."""
+        lon = np.ascontiguousarray(lon, dtype=np.float32).ravel()
+        lat = np.ascontiguousarray(lat, dtype=np.float32).ravel()
+        n = ctypes.c_int64(0)
+        self.ctx.call("lm_count_pairs", lon.size, _lib.ptr(lon), _lib.ptr(lat), ctypes.byref(n))
+        return int(n.value)

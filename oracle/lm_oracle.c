@@ -444,6 +444,73 @@ static int64_t pairs_packed(int64_t n, const float* lon, const float* lat, doubl
   return (int64_t)total;
 }
 
+/* The number of pairs of orc_pairs without storing them (the clustered stress workload): the same
+ * cell list and distance test, summed per thread. */
+int64_t orc_count_pairs(int64_t n, const float* lon, const float* lat, double r, int norm, int n_threads) {
+  if (n <= 0) return 0;
+  double x0 = INFINITY, y0 = INFINITY, x1 = -INFINITY, y1 = -INFINITY;
+  for (int64_t p = 0; p < n; ++p) {
+    if (!(isfinite(lon[p]) && isfinite(lat[p]))) continue;
+    if (lon[p] < x0) x0 = lon[p];
+    if (lon[p] > x1) x1 = lon[p];
+    if (lat[p] < y0) y0 = lat[p];
+    if (lat[p] > y1) y1 = lat[p];
+  }
+  if (!(x0 <= x1)) return 0;
+  double c = r > 0 ? r * 1.0001 : 1.0;
+  int64_t ncx = (int64_t)((x1 - x0) / c) + 1, ncy = (int64_t)((y1 - y0) / c) + 1;
+  while (ncx * ncy > ((int64_t)1 << 26)) {
+    c *= 2;
+    ncx = (int64_t)((x1 - x0) / c) + 1;
+    ncy = (int64_t)((y1 - y0) / c) + 1;
+  }
+  const int64_t ncell = ncx * ncy;
+  int64_t* cell = (int64_t*)malloc(sizeof(int64_t) * n);
+  int64_t* start = (int64_t*)calloc(ncell + 1, sizeof(int64_t));
+  int64_t* order = (int64_t*)malloc(sizeof(int64_t) * n);
+  if (!cell || !start || !order) { free(cell); free(start); free(order); return -1; }
+  for (int64_t p = 0; p < n; ++p) {
+    if (!(isfinite(lon[p]) && isfinite(lat[p]))) { cell[p] = -1; continue; }
+    int64_t cx = (int64_t)((lon[p] - x0) / c), cy = (int64_t)((lat[p] - y0) / c);
+    if (cx >= ncx) cx = ncx - 1;
+    if (cy >= ncy) cy = ncy - 1;
+    cell[p] = cy * ncx + cx;
+    start[cell[p] + 1]++;
+  }
+  for (int64_t k = 0; k < ncell; ++k) start[k + 1] += start[k];
+  int64_t* fill = (int64_t*)malloc(sizeof(int64_t) * ncell);
+  if (!fill) { free(cell); free(start); free(order); return -1; }
+  memcpy(fill, start, sizeof(int64_t) * ncell);
+  for (int64_t p = 0; p < n; ++p)
+    if (cell[p] >= 0) order[fill[cell[p]]++] = p;
+  free(fill);
+  const double r2 = r * r;
+  int64_t total = 0;
+#ifdef _OPENMP
+  if (n_threads > 0) omp_set_num_threads(n_threads);
+#else
+  (void)n_threads;
+#endif
+#pragma omp parallel for schedule(dynamic, 1024) reduction(+ : total)
+  for (int64_t p = 0; p < n; ++p) {
+    if (cell[p] < 0) continue;
+    const int64_t cy = cell[p] / ncx, cx = cell[p] % ncx;
+    for (int64_t yy = cy - 1; yy <= cy + 1; ++yy) {
+      if (yy < 0 || yy >= ncy) continue;
+      for (int64_t xx = cx - 1; xx <= cx + 1; ++xx) {
+        if (xx < 0 || xx >= ncx) continue;
+        const int64_t k = yy * ncx + xx;
+        for (int64_t t = start[k]; t < start[k + 1]; ++t) {
+          const int64_t q = order[t];
+          if (q > p && within(r, r2, norm, lon[p], lat[p], lon[q], lat[q])) ++total;
+        }
+      }
+    }
+  }
+  free(cell); free(start); free(order);
+  return total;
+}
+
 int64_t orc_pairs(int64_t n, const float* lon, const float* lat, double r, int norm, int n_threads, int32_t* pi,
                   int32_t* pj, int64_t cap) {
   uint64_t* all = NULL;

@@ -39,6 +39,8 @@ int64_t orc_advect_f32(const orc_field* f, int64_t n, float* lon, float* lat, ui
 int64_t orc_pairs(int64_t n, const float* lon, const float* lat, double r, int norm, int n_threads, int32_t* pi,
                   int32_t* pj, int64_t cap);
 
+int64_t orc_count_pairs(int64_t n, const float* lon, const float* lat, double r, int norm, int n_threads);
+
 void orc_rps_apply(int8_t* species, int32_t p1, int32_t p2, uint64_t u53, uint64_t t_rs, uint64_t t_pr, uint64_t t_sp);
 void orc_rps_replay(int8_t* species, int64_t m, const int32_t* pi, const int32_t* pj, uint32_t step, uint64_t seed,
                     uint64_t t_rs, uint64_t t_pr, uint64_t t_sp);

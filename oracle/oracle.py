@@ -65,6 +65,7 @@ def lib():
             "orc_advect_f32": (I64, [P, I64, P, P, P, F64, F64, I, I]),
             "orc_advect_f64d": (I64, [P, I64, P, P, P, F64, F64, I, I, P]),
             "orc_pairs": (I64, [I64, P, P, F64, I, I, P, P, I64]),
+            "orc_count_pairs": (I64, [I64, P, P, F64, I, I]),
             "orc_rps_apply": (None, [P, ctypes.c_int32, ctypes.c_int32, U64, U64, U64, U64]),
             "orc_rps_replay": (None, [P, I64, P, P, U32, U64, U64, U64, U64]),
             "orc_priority_order": (None, [I64, P, P, U32, U64, P, P, F64]),
@@ -219,6 +220,16 @@ def pairs(lon, lat, r: float, p=2, n_threads: int = 0):
     pj = np.empty(m, np.int32)
     lib().orc_pairs(lon.size, _p(lon), _p(lat), float(r), norm_code(p), int(n_threads), _p(pi), _p(pj), m)
     return pi.astype(np.int64), pj.astype(np.int64)
+
+
+def count_pairs(lon, lat, r: float, p=2, n_threads: int = 0) -> int:
+    """Number of unordered pairs within r (the count of pairs(), without listing them)."""
+    lon = np.ascontiguousarray(lon, dtype=np.float32)
+    lat = np.ascontiguousarray(lat, dtype=np.float32)
+    m = int(lib().orc_count_pairs(lon.size, _p(lon), _p(lat), float(r), norm_code(p), int(n_threads)))
+    if m < 0:
+        raise MemoryError("oracle pair count failed")
+    return m
 
 
 def priority_order(pi, pj, step: int, seed: int, lon, lat, r: float):
