@@ -128,8 +128,43 @@ __global__ void __launch_bounds__(RD_THREADS) k_rounds(Bufs b, StepArgs a, Ctrl*
   const uint32_t first = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t max_level = 0;
   const unsigned long long t0 = globaltimer();
-  bool pending = first < cnt;
   uint32_t polls = 0;
+  if (cnt <= (uint32_t)POLL_BATCH * stride) {
+    // every thread owns at most POLL_BATCH vertices: keep their ids in registers and stop polling
+    // a vertex once its list is done (its partner stays NONE from then on)
+    uint32_t sv[POLL_BATCH];
+    uint32_t live = 0;
+#pragma unroll
+    for (int k = 0; k < POLL_BATCH; ++k) {
+      const uint32_t x = first + (uint32_t)k * stride;
+      sv[k] = x < cnt ? b.act[x] : NONE;
+      if (sv[k] != NONE) live |= 1u << k;
+    }
+    while (live) {
+      unsigned long long ws[POLL_BATCH], wu[POLL_BATCH];
+#pragma unroll
+      for (int k = 0; k < POLL_BATCH; ++k)
+        ws[k] = (live >> k) & 1u ? ld_relaxed(b.wstate + sv[k]) : (unsigned long long)NONE;
+#pragma unroll
+      for (int k = 0; k < POLL_BATCH; ++k) {
+        const uint32_t u = state_partner(ws[k]);
+        wu[k] = NONE;
+        if (u == NONE) live &= ~(1u << k);
+        else if (sv[k] < u) wu[k] = ld_relaxed(b.wstate + u);
+      }
+#pragma unroll
+      for (int k = 0; k < POLL_BATCH; ++k) {
+        const uint32_t u = state_partner(ws[k]);
+        if (u != NONE && sv[k] < u && state_partner(wu[k]) == sv[k])
+          max_level = max(max_level, apply_pair(b, step, sv[k], u, ws[k], wu[k], ctrl));
+      }
+      if (live && ((++polls & 63u) == 0u) && globaltimer() - t0 > ROUNDS_TIMEOUT_NS) {
+        atomicOr(&ctrl->err, (uint32_t)ERRB_TIMEOUT);
+        break;
+      }
+    }
+  }
+  bool pending = first < cnt && cnt > (uint32_t)POLL_BATCH * stride;
   while (pending) {
     pending = false;
     for (uint32_t x0 = first; x0 < cnt; x0 += POLL_BATCH * stride) {

@@ -517,7 +517,6 @@ void set_pair_params(lm_ctx* c, double r, int norm) {
     pp.r2f_lo = pp.rf_lo = -1.f;
     pp.r2f_hi = pp.rf_hi = INFINITY;
   }
-  pp.inv2r = r > 0 ? (float)(0.5 / r) : 0.f;
   pp.cell_factor = (float)c->cell_factor;
 }
 

@@ -115,7 +115,6 @@ struct PairParams {
   double r2;          // fl(r*r)
   float r2f_lo, r2f_hi;  // float32 accept / reject thresholds around r^2 (p = 2)
   float rf_lo, rf_hi;    // float32 accept / reject thresholds around r   (p = 1, inf)
-  float inv2r;        // 0.5 / r: scale of the colour grid of the pair order (0 when r == 0)
   float cell_factor;  // binning cell size = cell_factor * r (>= 1.004)
   int norm;           // 1, 2 or 0 (= infinity)
 };

@@ -24,9 +24,8 @@
  *       rock_paper_scissors_interaction (interactions.py:13-40), with r drawn per pair from
  *       Philox4x32-10 (Salmon et al., SC'11) keyed by (seed, step, i, j) instead of MT19937.
  *   orc_priority_order / orc_interact_step : the pair order used by the GPU, then the sequential
- *       replay. The order key is the pair's colour (2x2 checkerboard of cells of size r at the
- *       pair's midpoint, computed in float32 exactly as the GPU does) followed by a 62-bit order
- *       hash of (seed, step, i, j) (SplitMix64's output function); ties by (i, j).
+ *       replay. The order key is a 64-bit order hash of (seed, step, i, j) (SplitMix64's output
+ *       function, a bijection: no ties within a step), descending.
  */
 #include "lm_oracle.h"
 
@@ -79,12 +78,6 @@ void orc_diffusion_draw(uint32_t p, uint32_t step, uint64_t seed, float* ulat, f
   *ulon = (float)(2u * (o[1] >> 9) + 1u) * (1.0f / 8388608.0f) - 1.0f;
 }
 
-/* Parity of floor(v), exact for every float. */
-static uint32_t floor_parity(float v) {
-  const float f = floorf(v);
-  return (uint32_t)(f - 2.0f * floorf(f * 0.5f));
-}
-
 /* 64-bit order hash: the output function of SplitMix64 (Steele, Lea, Flood, OOPSLA 2014) applied to
  * (i << 32 | j) offset by Weyl multiples of seed and step. */
 uint64_t orc_order_hash(uint32_t i, uint32_t j, uint32_t step, uint64_t seed) {
@@ -94,15 +87,8 @@ uint64_t orc_order_hash(uint32_t i, uint32_t j, uint32_t step, uint64_t seed) {
   return z ^ (z >> 31);
 }
 
-uint64_t orc_pair_prio(uint32_t i, uint32_t j, uint32_t step, uint64_t seed, float xa, float ya, float xb, float yb,
-                       float inv2r) {
-  const uint64_t h = orc_order_hash(i, j, step, seed);
-  const float mx = xa + xb, my = ya + yb;
-  const uint32_t color = floor_parity(mx * inv2r) | (floor_parity(my * inv2r) << 1);
-  return ((uint64_t)(3u - color) << 62) | (h >> 2);
-}
-
-float orc_inv2r(double r) { return r > 0 ? (float)(0.5 / r) : 0.0f; }
+/* Application order key of pair (i < j) at `step`: the order hash alone, descending. */
+uint64_t orc_pair_prio(uint32_t i, uint32_t j, uint32_t step, uint64_t seed) { return orc_order_hash(i, j, step, seed); }
 
 uint64_t orc_prob_threshold(double p) {
   if (!(p > 0)) return 0;
@@ -567,17 +553,14 @@ static int cmp_prio(const void* a, const void* b) {
   return 0;
 }
 
-/* Reorder (pi, pj) in place into the GPU's application order: descending priority, ties by (i, j).
- * lon/lat are the float32 positions of the step (indexed by particle), r the interaction radius. */
-void orc_priority_order(int64_t m, int32_t* pi, int32_t* pj, uint32_t step, uint64_t seed, const float* lon,
-                        const float* lat, double r) {
-  const float inv2r = orc_inv2r(r);
+/* Reorder (pi, pj) in place into the GPU's application order: descending priority, ties by (i, j). */
+void orc_priority_order(int64_t m, int32_t* pi, int32_t* pj, uint32_t step, uint64_t seed) {
   prio_pair* a = (prio_pair*)malloc(sizeof(prio_pair) * (m ? m : 1));
   for (int64_t k = 0; k < m; ++k) {
     uint32_t x = (uint32_t)pi[k], y = (uint32_t)pj[k];
     a[k].i = x < y ? x : y;
     a[k].j = x < y ? y : x;
-    a[k].prio = orc_pair_prio(a[k].i, a[k].j, step, seed, lon[a[k].i], lat[a[k].i], lon[a[k].j], lat[a[k].j], inv2r);
+    a[k].prio = orc_pair_prio(a[k].i, a[k].j, step, seed);
   }
   qsort(a, (size_t)m, sizeof(prio_pair), cmp_prio);
   for (int64_t k = 0; k < m; ++k) {
@@ -592,13 +575,12 @@ int64_t orc_interact_step(int64_t n, const float* lon, const float* lat, int8_t*
   uint64_t* all = NULL;
   int64_t m = pairs_packed(n, lon, lat, r, norm, n_threads, &all);
   if (m < 0) return -1;
-  const float inv2r = orc_inv2r(r);
   prio_pair* a = (prio_pair*)malloc(sizeof(prio_pair) * (m ? m : 1));
 #pragma omp parallel for schedule(static) num_threads(n_threads > 0 ? n_threads : 1) if (m > 100000)
   for (int64_t k = 0; k < m; ++k) {
     a[k].i = (uint32_t)(all[k] >> 32);
     a[k].j = (uint32_t)(all[k] & 0xffffffffu);
-    a[k].prio = orc_pair_prio(a[k].i, a[k].j, step, seed, lon[a[k].i], lat[a[k].i], lon[a[k].j], lat[a[k].j], inv2r);
+    a[k].prio = orc_pair_prio(a[k].i, a[k].j, step, seed);
   }
   free(all);
   qsort(a, (size_t)m, sizeof(prio_pair), cmp_prio);

@@ -45,11 +45,8 @@ void orc_rps_apply(int8_t* species, int32_t p1, int32_t p2, uint64_t u53, uint64
 void orc_rps_replay(int8_t* species, int64_t m, const int32_t* pi, const int32_t* pj, uint32_t step, uint64_t seed,
                     uint64_t t_rs, uint64_t t_pr, uint64_t t_sp);
 uint64_t orc_order_hash(uint32_t i, uint32_t j, uint32_t step, uint64_t seed);
-uint64_t orc_pair_prio(uint32_t i, uint32_t j, uint32_t step, uint64_t seed, float xa, float ya, float xb, float yb,
-                       float inv2r);
-float orc_inv2r(double r);
-void orc_priority_order(int64_t m, int32_t* pi, int32_t* pj, uint32_t step, uint64_t seed, const float* lon,
-                        const float* lat, double r);
+uint64_t orc_pair_prio(uint32_t i, uint32_t j, uint32_t step, uint64_t seed);
+void orc_priority_order(int64_t m, int32_t* pi, int32_t* pj, uint32_t step, uint64_t seed);
 int64_t orc_interact_step(int64_t n, const float* lon, const float* lat, int8_t* species, double r, int norm,
                           uint64_t t_rs, uint64_t t_pr, uint64_t t_sp, uint64_t seed, uint32_t step, int n_threads);
 int64_t orc_run(const orc_field* f, int64_t n, float* lon, float* lat, uint8_t* status, int8_t* species, double t0,

@@ -68,10 +68,8 @@ def lib():
             "orc_count_pairs": (I64, [I64, P, P, F64, I, I]),
             "orc_rps_apply": (None, [P, ctypes.c_int32, ctypes.c_int32, U64, U64, U64, U64]),
             "orc_rps_replay": (None, [P, I64, P, P, U32, U64, U64, U64, U64]),
-            "orc_priority_order": (None, [I64, P, P, U32, U64, P, P, F64]),
-            "orc_pair_prio": (U64, [U32, U32, U32, U64, ctypes.c_float, ctypes.c_float, ctypes.c_float,
-                                    ctypes.c_float, ctypes.c_float]),
-            "orc_inv2r": (ctypes.c_float, [F64]),
+            "orc_priority_order": (None, [I64, P, P, U32, U64]),
+            "orc_pair_prio": (U64, [U32, U32, U32, U64]),
             "orc_interact_step": (I64, [I64, P, P, P, F64, I, U64, U64, U64, U64, U32, I]),
             "orc_run": (I64, [P, I64, P, P, P, P, F64, F64, I, U32, F64, I, U64, U64, U64, U64, I]),
         }
@@ -232,19 +230,16 @@ def count_pairs(lon, lat, r: float, p=2, n_threads: int = 0) -> int:
     return m
 
 
-def priority_order(pi, pj, step: int, seed: int, lon, lat, r: float):
-    """Pairs in the GPU's application order (colour of the midpoint cell, then Philox hash)."""
+def priority_order(pi, pj, step: int, seed: int):
+    """Pairs in the GPU's application order (descending 64-bit order hash of (seed, step, i, j))."""
     a = np.ascontiguousarray(pi, dtype=np.int32).copy()
     b = np.ascontiguousarray(pj, dtype=np.int32).copy()
-    lo = np.ascontiguousarray(lon, dtype=np.float32)
-    la = np.ascontiguousarray(lat, dtype=np.float32)
-    lib().orc_priority_order(a.size, _p(a), _p(b), int(step), seed & 0xFFFFFFFFFFFFFFFF, _p(lo), _p(la), float(r))
+    lib().orc_priority_order(a.size, _p(a), _p(b), int(step), seed & 0xFFFFFFFFFFFFFFFF)
     return a.astype(np.int64), b.astype(np.int64)
 
 
-def pair_prio(i: int, j: int, step: int, seed: int, a, b, r: float) -> int:
-    return lib().orc_pair_prio(i, j, step, seed & 0xFFFFFFFFFFFFFFFF, float(a[0]), float(a[1]), float(b[0]),
-                               float(b[1]), lib().orc_inv2r(float(r)))
+def pair_prio(i: int, j: int, step: int, seed: int) -> int:
+    return lib().orc_pair_prio(i, j, step, seed & 0xFFFFFFFFFFFFFFFF)
 
 
 def rps_replay(species, pi, pj, step: int, seed: int, pRS: float, pPR: float, pSP: float):

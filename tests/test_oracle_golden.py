@@ -111,7 +111,7 @@ def test_priority_order_is_a_linear_extension(orc):
     g = golden("interaction_sim.npz")
     lon, lat = g["lon"][:, 0], g["lat"][:, 0]
     pi, pj = orc.pairs(lon, lat, float(g["radius"]), 2)
-    a, b = orc.priority_order(pi, pj, 0, 99, lon, lat, float(g["radius"]))
+    a, b = orc.priority_order(pi, pj, 0, 99)
     # build rounds greedily from the priority order and check the replay is unchanged
     level = {}
     rnd = np.empty(a.size, np.int64)
