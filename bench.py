@@ -167,6 +167,7 @@ def run_gb300(args):
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     sim.set_stream(stream.cuda_stream)
+    cell_factor, tune = sim.autotune(0.0, DT, 3)  # binning cell size; results do not depend on it
     sim.capture(0.0, DT, spg, step0=0)
     sim.run_graph(W, sync=True)  # warm-up (also grows neighbour lists if needed)
 
@@ -274,7 +275,8 @@ def run_gb300(args):
             "dtype": "f32 (positions), f64 (pair-boundary refine), int8 (species)", "data": "synthetic",
             "config": {"workload": WORKLOAD, "microbes": n, "sim_steps_per_bench_step": spg,
                        "sim_steps_timed": sim_steps, "parallelism": f"replicas x{world}",
-                       "l2": "512 MiB buffer written between timed bench steps", "form": "cuda-graph, 24 steps/launch"},
+                       "l2": "512 MiB buffer written between timed bench steps", "form": "cuda-graph, 24 steps/launch",
+                       "cell_factor": cell_factor, "autotune_s": tune},
             "pairs_per_step": pairs_per_step,
             "plain": {"value": plain_value, "unit": "microbe-steps/s", "sim_steps": plain_steps,
                       "graph_speedup": value / world / plain_value},
@@ -362,6 +364,7 @@ def run_batched(local: int, stream):
     total = int(sum(x[0].size for x in ens))
     sim = EnsembleSimulation(fields, ens, radius=RADIUS, p_rs=ps, p_pr=ps, p_sp=ps, seeds=seeds, device=local)
     sim.set_stream(stream.cuda_stream)
+    cell_factor, _ = sim.autotune(0.0, DT, 2)
     sim.capture(0.0, DT, B_STEPS, step0=0)
     sim.run_graph(1, sync=True)  # warm-up: sizes the long neighbour lists for this workload
     reps = 3
@@ -403,7 +406,8 @@ def run_batched(local: int, stream):
     return {"workload": B_WORKLOAD, "ensembles": B_ENSEMBLES, "microbes": total, "sim_steps": B_STEPS,
             "pairs_per_step": st["pairs_total"] / max(st["steps_total"], 1),
             "graph": {"value": graph_value, "unit": "microbe-steps/s", "ms_per_sim_step": graph_ms / B_STEPS,
-                      "form": "one context, one CUDA graph of 24 fused steps for all ensembles"},
+                      "form": "one context, one CUDA graph of 24 fused steps for all ensembles",
+                      "cell_factor": cell_factor},
             "plain_per_ensemble": {"value": plain_value, "unit": "microbe-steps/s",
                                    "ms_per_sim_step": plain_ms / B_STEPS,
                                    "form": "one context per ensemble, per-step launches, ensembles one after another"},

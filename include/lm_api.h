@@ -116,6 +116,18 @@ int lm_ensembles_upload(lm_ctx* ctx, int n_ens, const int64_t* counts, const dou
 /* Current state: absolute float32 lon/lat (after any diffusion kick), species, status (0 ok,
  * 1 out of domain, 2 non-finite). Any pointer may be NULL. */
 int lm_particles_download(lm_ctx* ctx, float* lon, float* lat, int8_t* species, uint8_t* status);
+/* Device snapshot of the state (positions, species, status, step counter) and its restoration, bit
+ * for bit, e.g. to time candidates from one state (autotuning) or to rewind. The reference's
+ * equivalent is its per-chunk pickle of positions (particle_advecter.py:246-249). */
+int lm_snapshot_save(lm_ctx* ctx);
+int lm_snapshot_restore(lm_ctx* ctx);
+/* Exact state in caller order for checkpoint files: float32 offsets from the field's float32
+ * origin (lon[0], lat[0] of the field axes), species, status and the step counter. Import needs
+ * the same field and particle layout (lm_particles_upload / lm_ensembles_upload first); a run
+ * resumed from an exported state continues bit-identically. */
+int lm_state_export(lm_ctx* ctx, float* xo, float* yo, int8_t* species, uint8_t* status, int64_t* step);
+int lm_state_import(lm_ctx* ctx, const float* xo, const float* yo, const int8_t* species, const uint8_t* status,
+                    int64_t step);
 /* Set the species array (int8[n]). With particles uploaded, n must match their count; without
  * (the two-phase workflow, where positions arrive per step through lm_interact) it sizes the
  * context for n microbes. */

@@ -108,6 +108,10 @@ SIGNATURES = {
     "lm_census_get": [P, P, I64],
     "lm_particles_upload": [P, I64, P, P, P],
     "lm_particles_download": [P, P, P, P, P],
+    "lm_snapshot_save": [P],
+    "lm_snapshot_restore": [P],
+    "lm_state_export": [P, P, P, P, P, ctypes.POINTER(I64)],
+    "lm_state_import": [P, P, P, P, P, I64],
     "lm_species_upload": [P, I64, P],
     "lm_set_interaction": [P, F64, I32, F64, F64, F64, U64],
     "lm_step": [P, F64, F64, I32, I64, U32, F64, P, P, P, P],

@@ -97,6 +97,13 @@ struct lm_ctx {
   uint32_t* hstage = nullptr;
   size_t hstage_n = 0;
 
+  // device snapshot of the state (lm_snapshot_save / lm_snapshot_restore)
+  float *snap_xo = nullptr, *snap_yo = nullptr;
+  int8_t* snap_sp = nullptr;
+  uint8_t* snap_st = nullptr;
+  uint32_t snap_slots = 0;
+  int64_t snap_step = -1;
+
   // pair log
   uint32_t* plog = nullptr;
   uint32_t plog_cap = 0;
@@ -680,7 +687,8 @@ int lm_ctx_destroy(lm_ctx* c) {
                    c->rank,   c->sid,   c->skey,   c->sens,   c->deg,    c->slab,    c->off,    c->longv,
                    c->wstate, c->level,  c->act,    c->spos,   c->rlon,    c->rlat,   c->rsp,
                    c->map_d,  c->block_ens, c->ens_d, c->grids, c->ebox, c->census,  c->ccount, c->cstart,
-                   c->csum,   c->ovf,   c->oprio,  c->ctrl,   c->plog};
+                   c->csum,   c->ovf,   c->oprio,  c->ctrl,   c->plog,  c->snap_xo, c->snap_yo, c->snap_sp,
+                   c->snap_st};
   for (void* p : bufs_)
     if (p) cudaFree(p);
   if (c->hctrl) cudaFreeHost(c->hctrl);
@@ -861,6 +869,98 @@ int lm_particles_download(lm_ctx* c, float* lon, float* lat, int8_t* species, ui
     if (status) status[q] = st[k];
   }
   return LM_OK;
+}
+
+int lm_snapshot_save(lm_ctx* c) {
+  if (!c) return LM_ERR_ARG;
+  if (!c->has_particles) return fail(c, LM_ERR_STATE, "no particles");
+  CK(cudaSetDevice(c->device));
+  const uint32_t S = c->nslots;
+  int r;
+  if (S > c->snap_slots || !c->snap_xo) {
+    if ((r = dalloc(c, &c->snap_xo, S)) || (r = dalloc(c, &c->snap_yo, S)) || (r = dalloc(c, &c->snap_sp, S)) ||
+        (r = dalloc(c, &c->snap_st, S)))
+      return r;
+  }
+  if (S) {
+    CK(cudaMemcpyAsync(c->snap_xo, c->xo, S * sizeof(float), cudaMemcpyDeviceToDevice, c->st));
+    CK(cudaMemcpyAsync(c->snap_yo, c->yo, S * sizeof(float), cudaMemcpyDeviceToDevice, c->st));
+    CK(cudaMemcpyAsync(c->snap_sp, c->species, S, cudaMemcpyDeviceToDevice, c->st));
+    CK(cudaMemcpyAsync(c->snap_st, c->status, S, cudaMemcpyDeviceToDevice, c->st));
+  }
+  if ((r = read_ctrl(c))) return r;
+  c->snap_slots = S;
+  c->snap_step = c->hctrl->step;
+  return LM_OK;
+}
+
+int lm_snapshot_restore(lm_ctx* c) {
+  if (!c) return LM_ERR_ARG;
+  if (c->snap_step < 0 || !c->has_particles || c->snap_slots != c->nslots)
+    return fail(c, LM_ERR_STATE, "no snapshot of the current particle layout");
+  CK(cudaSetDevice(c->device));
+  const uint32_t S = c->nslots;
+  if (S) {
+    CK(cudaMemcpyAsync(c->xo, c->snap_xo, S * sizeof(float), cudaMemcpyDeviceToDevice, c->st));
+    CK(cudaMemcpyAsync(c->yo, c->snap_yo, S * sizeof(float), cudaMemcpyDeviceToDevice, c->st));
+    CK(cudaMemcpyAsync(c->species, c->snap_sp, S, cudaMemcpyDeviceToDevice, c->st));
+    CK(cudaMemcpyAsync(c->status, c->snap_st, S, cudaMemcpyDeviceToDevice, c->st));
+  }
+  return write_ctrl_step(c, c->snap_step);
+}
+
+int lm_state_export(lm_ctx* c, float* xo, float* yo, int8_t* species, uint8_t* status, int64_t* step) {
+  if (!c || !xo || !yo || !species || !status || !step) return fail(c, LM_ERR_ARG, "NULL argument");
+  if (!c->has_particles) return fail(c, LM_ERR_STATE, "no particles");
+  CK(cudaSetDevice(c->device));
+  const uint32_t S = c->nslots;
+  std::vector<float> hx(S), hy(S);
+  std::vector<int8_t> hs(S);
+  std::vector<uint8_t> ht(S);
+  if (S) {
+    CK(cudaMemcpyAsync(hx.data(), c->xo, S * sizeof(float), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaMemcpyAsync(hy.data(), c->yo, S * sizeof(float), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaMemcpyAsync(hs.data(), c->species, S, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaMemcpyAsync(ht.data(), c->status, S, cudaMemcpyDeviceToHost, c->st));
+  }
+  int r;
+  if ((r = read_ctrl(c))) return r;
+  for (uint32_t k = 0; k < S; ++k) {
+    const int32_t q = c->hmap[k];
+    if (q < 0) continue;
+    xo[q] = hx[k];
+    yo[q] = hy[k];
+    species[q] = hs[k];
+    status[q] = ht[k];
+  }
+  *step = c->hctrl->step;
+  return LM_OK;
+}
+
+int lm_state_import(lm_ctx* c, const float* xo, const float* yo, const int8_t* species, const uint8_t* status,
+                    int64_t step) {
+  if (!c || !xo || !yo || !species || !status) return fail(c, LM_ERR_ARG, "NULL argument");
+  if (!c->has_particles) return fail(c, LM_ERR_STATE, "upload particles (the layout) before importing a state");
+  CK(cudaSetDevice(c->device));
+  const uint32_t S = c->nslots;
+  std::vector<float> hx(S, 0.f), hy(S, 0.f);
+  std::vector<int8_t> hs(S, 0);
+  std::vector<uint8_t> ht(S, STATUS_PAD);
+  for (uint32_t k = 0; k < S; ++k) {
+    const int32_t q = c->hmap[k];
+    if (q < 0) continue;
+    hx[k] = xo[q];
+    hy[k] = yo[q];
+    hs[k] = species[q];
+    ht[k] = status[q] == STATUS_PAD ? STATUS_NAN : status[q];
+  }
+  if (S) {
+    CK(cudaMemcpyAsync(c->xo, hx.data(), S * sizeof(float), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(c->yo, hy.data(), S * sizeof(float), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(c->species, hs.data(), S, cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(c->status, ht.data(), S, cudaMemcpyHostToDevice, c->st));
+  }
+  return write_ctrl_step(c, step);
 }
 
 int lm_set_interaction(lm_ctx* c, double radius, int norm, double p_rs, double p_pr, double p_sp, uint64_t seed) {

@@ -86,6 +86,57 @@ class Simulation:
         """Binning cell size in units of the radius (>= 1.004; the pair set does not change)."""
         self.ctx.call("lm_set_cell_factor", float(factor))
 
+    # ---- state snapshots, checkpoints, autotuning ----
+    def snapshot(self) -> None:
+        """Keep a device copy of the state (positions, species, status, step counter)."""
+        self.ctx.call("lm_snapshot_save")
+
+    def restore(self) -> None:
+        """Return to the last snapshot, bit for bit."""
+        self.ctx.call("lm_snapshot_restore")
+        self.step_index = int(self.ctx.stats()["step"])
+
+    def export_state(self) -> dict:
+        """Exact state for a checkpoint file: float32 offsets from the field origin, species, status, step."""
+        n = self.n
+        xo = np.empty(n, np.float32)
+        yo = np.empty(n, np.float32)
+        sp = np.empty(n, np.int8)
+        st = np.empty(n, np.uint8)
+        step = ctypes.c_int64(0)
+        self.ctx.call("lm_state_export", _lib.ptr(xo), _lib.ptr(yo), _lib.ptr(sp), _lib.ptr(st), ctypes.byref(step))
+        return {"xo": xo, "yo": yo, "species": sp, "status": st, "step": int(step.value)}
+
+    def import_state(self, state: dict) -> None:
+        """Resume from export_state() (same field and particle layout)."""
+        arr = lambda k, dt: np.ascontiguousarray(state[k], dtype=dt)
+        self.ctx.call("lm_state_import", _lib.ptr(arr("xo", np.float32)), _lib.ptr(arr("yo", np.float32)),
+                      _lib.ptr(arr("species", np.int8)), _lib.ptr(arr("status", np.uint8)), int(state["step"]))
+        self.step_index = int(state["step"])
+
+    def autotune(self, t0, dt, n_steps: int = 3, factors=(1.004, 1.25, 1.5, 2.0), count_pairs: bool = False):
+        """Pick the binning cell size (in units of the radius) that runs n_steps fastest from the
+        current state, then return to that state. The pair sets, and so all results, are the same
+        for every cell size; only the speed changes. Capture graphs after tuning. Returns
+        (best factor, {factor: seconds})."""
+        import time as _time
+        s0 = self.step_index
+        self.snapshot()
+        times = {}
+        for f in factors:
+            self.set_cell_factor(f)
+            self.restore()
+            self.step(t0, dt, 1, step0=s0, count_pairs=count_pairs)  # sizes the lists for this cell size
+            self.restore()
+            t = _time.perf_counter()
+            self.step(t0, dt, n_steps, step0=s0, count_pairs=count_pairs)
+            times[f] = _time.perf_counter() - t
+        best = min(times, key=times.get)
+        self.set_cell_factor(best)
+        self.restore()
+        self._graph = None
+        return best, times
+
     def set_stream(self, stream_handle: int) -> None:
         """Run on an external CUDA stream (e.g. torch.cuda.current_stream().cuda_stream)."""
         self.ctx.call("lm_ctx_set_stream", int(stream_handle))
