@@ -32,7 +32,8 @@ __device__ __forceinline__ float grid_dims(const uint32_t* box, float c, float* 
   }
   *ncx = floorf((mxx - mnx) / c) + 3.f;
   *ncy = floorf((mxy - mny) / c) + 3.f;
-  return *ncx * *ncy;
+  // the key range covers whole TILE x TILE tiles
+  return ceilf(*ncx / (float)TILE) * ceilf(*ncy / (float)TILE) * (float)(TILE * TILE);
 }
 
 // One block: grid geometry of every ensemble and the global cell numbering. If the cells would
@@ -76,10 +77,7 @@ __global__ void __launch_bounds__(GRID_THREADS) k_grid(Bufs b, PairParams pp, Ct
     const uint32_t e = e0 + threadIdx.x;
     float nx = 0.f, ny = 0.f;
     uint32_t cells = 0;
-    if (e < b.n_ens) {
-      grid_dims(b.ebox + 4 * e, c, &nx, &ny);
-      cells = (uint32_t)fminf(nx * ny, 4.0e9f);
-    }
+    if (e < b.n_ens) cells = (uint32_t)fminf(grid_dims(b.ebox + 4 * e, c, &nx, &ny), 4.0e9f);
     uint32_t y = cells;
     for (int o = 1; o < 32; o <<= 1) {
       const uint32_t t = __shfl_up_sync(0xffffffffu, y, o);
@@ -153,7 +151,7 @@ __global__ void __launch_bounds__(SLOT_BLOCK) k_keys(Bufs b, Ctrl* ctrl, int use
   if (valid) {
     const float fx = fminf(fmaxf((x - g.x0) * g.inv_c, 0.f), (float)(g.ncx - 1));
     const float fy = fminf(fmaxf((y - g.y0) * g.inv_c, 0.f), (float)(g.ncy - 1));
-    key = g.cell_base + (uint32_t)(int)fy * (uint32_t)g.ncx + (uint32_t)(int)fx;
+    key = g.cell_base + cell_index(g, (uint32_t)(int)fx, (uint32_t)(int)fy);
   }
   const uint32_t peers = __match_any_sync(0xffffffffu, key);
   uint32_t rank = 0;

@@ -71,9 +71,7 @@ __device__ __forceinline__ Vertex load_vertex(const Bufs& b, uint32_t s) {
   v.e = b.sens[s];
   v.g = b.grids[v.e];
   v.base = b.ens[v.e].base;
-  const uint32_t k = b.skey[s] - v.g.cell_base;
-  v.cy = k / (uint32_t)v.g.ncx;
-  v.cx = k - v.cy * (uint32_t)v.g.ncx;
+  cell_coords(v.g, b.skey[s] - v.g.cell_base, &v.cx, &v.cy);
   v.ps = b.spos[s];
   return v;
 }
@@ -84,12 +82,11 @@ __device__ __forceinline__ void for_neighbours(const Bufs& b, const PairParams& 
   for (int dy = -1; dy <= 1; ++dy) {
     const int ry = (int)v.cy + dy;
     if (ry < 0 || ry >= v.g.ncy) continue;
-    const uint32_t row = v.g.cell_base + (uint32_t)ry * (uint32_t)v.g.ncx;
-    const uint32_t kl = row + (uint32_t)max((int)v.cx - 1, 0);
-    const uint32_t kh = row + (uint32_t)min((int)v.cx + 1, v.g.ncx - 1);
-    const uint32_t t1 = b.cstart[kh + 1];
-    for (uint32_t t = b.cstart[kl]; t < t1; ++t)
-      if (t != v.s && within(pp, v.ps, b.spos[t])) f(t);
+    row_runs(v.g, max((int)v.cx - 1, 0), min((int)v.cx + 1, v.g.ncx - 1), ry, [&](uint32_t kl, uint32_t kh) {
+      const uint32_t t1 = b.cstart[kh + 1];
+      for (uint32_t t = b.cstart[kl]; t < t1; ++t)
+        if (t != v.s && within(pp, v.ps, b.spos[t])) f(t);
+    });
   }
 }
 
@@ -219,26 +216,28 @@ void launch_sweep(const Bufs& b, const PairParams& pp, const StepArgs& a, Ctrl* 
 // any other block lets each thread walk its own runs. Counts are summed per block and added to
 // the step's directed-entry counter (2 per pair) with one atomic.
 constexpr uint32_t COUNT_THREADS = 256;
+constexpr int COUNT_RUNS = 4;
 
 __device__ __forceinline__ void count_runs(const Vertex& v, const Bufs& b, uint32_t* r0, uint32_t* r1) {
-  // r[0] = the rest of the own cell, r[1] = (cx+1, cy), r[2] = row cy+1 from cx-1 to cx+1
-  const uint32_t kc = v.g.cell_base + v.cy * (uint32_t)v.g.ncx + v.cx;
+  // r[0] = the rest of the own cell, r[1] = (cx+1, cy), r[2..3] = row cy+1 from cx-1 to cx+1 (one
+  // or two key runs: the row may cross a tile edge); unused runs are empty
+  const uint32_t kc = v.g.cell_base + cell_index(v.g, v.cx, v.cy);
   r0[0] = v.s + 1;
   r1[0] = b.cstart[kc + 1];
+  for (int q = 1; q < COUNT_RUNS; ++q) r0[q] = r1[q] = 0;
   if ((int)v.cx + 1 < v.g.ncx) {
-    r0[1] = b.cstart[kc + 1];
-    r1[1] = b.cstart[kc + 2];
-  } else {
-    r0[1] = r1[1] = 0;
+    const uint32_t ke = v.g.cell_base + cell_index(v.g, v.cx + 1, v.cy);
+    r0[1] = b.cstart[ke];
+    r1[1] = b.cstart[ke + 1];
   }
   if ((int)v.cy + 1 < v.g.ncy) {
-    const uint32_t row = v.g.cell_base + (v.cy + 1) * (uint32_t)v.g.ncx;
-    const uint32_t kl = row + (uint32_t)max((int)v.cx - 1, 0);
-    const uint32_t kh = row + (uint32_t)min((int)v.cx + 1, v.g.ncx - 1);
-    r0[2] = b.cstart[kl];
-    r1[2] = b.cstart[kh + 1];
-  } else {
-    r0[2] = r1[2] = 0;
+    int q = 2;
+    row_runs(v.g, max((int)v.cx - 1, 0), min((int)v.cx + 1, v.g.ncx - 1), (int)v.cy + 1,
+             [&](uint32_t kl, uint32_t kh) {
+               r0[q] = b.cstart[kl];
+               r1[q] = b.cstart[kh + 1];
+               ++q;
+             });
   }
 }
 
@@ -265,10 +264,10 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_count_pairs(Bufs b, PairParam
     // all 256 microbes share one cell and hence the same forward runs; the own-cell run starts
     // after the block's first microbe, each thread keeps only partners with a higher index
     const Vertex v = load_vertex(b, blk0);
-    uint32_t r0[3], r1[3];
+    uint32_t r0[COUNT_RUNS], r1[COUNT_RUNS];
     count_runs(v, b, r0, r1);
     const float2 me = b.spos[s];
-    for (int q = 0; q < 3; ++q) {
+    for (int q = 0; q < COUNT_RUNS; ++q) {
       for (uint32_t tb = r0[q]; tb < r1[q]; tb += COUNT_THREADS) {
         const uint32_t n_t = min(COUNT_THREADS, r1[q] - tb);
         if (threadIdx.x < n_t) tile[threadIdx.x] = b.spos[tb + threadIdx.x];
@@ -301,9 +300,9 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_count_pairs(Bufs b, PairParam
     }
   } else if (s < n_valid) {
     const Vertex v = load_vertex(b, s);
-    uint32_t r0[3], r1[3];
+    uint32_t r0[COUNT_RUNS], r1[COUNT_RUNS];
     count_runs(v, b, r0, r1);
-    for (int q = 0; q < 3; ++q)
+    for (int q = 0; q < COUNT_RUNS; ++q)
       for (uint32_t t = r0[q]; t < r1[q]; ++t) cnt += within(pp, v.ps, b.spos[t]) ? 1u : 0u;
   }
   for (int o = 16; o > 0; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
@@ -442,9 +441,7 @@ __global__ void __launch_bounds__(LONG_WARPS * 32) k_sweep_long(Bufs b, PairPara
       for (int dy = -1; dy <= 1; ++dy) {
         const int ry = (int)v.cy + dy;
         if (ry < 0 || ry >= v.g.ncy) continue;
-        const uint32_t row = v.g.cell_base + (uint32_t)ry * (uint32_t)v.g.ncx;
-        const uint32_t kl = row + (uint32_t)max((int)v.cx - 1, 0);
-        const uint32_t kh = row + (uint32_t)min((int)v.cx + 1, v.g.ncx - 1);
+        row_runs(v.g, max((int)v.cx - 1, 0), min((int)v.cx + 1, v.g.ncx - 1), ry, [&](uint32_t kl, uint32_t kh) {
         const uint32_t t0 = b.cstart[kl], t1 = b.cstart[kh + 1];
         for (uint32_t tb = t0; tb < t1; tb += 32) {
           const uint32_t t = tb + lane;
@@ -465,6 +462,7 @@ __global__ void __launch_bounds__(LONG_WARPS * 32) k_sweep_long(Bufs b, PairPara
           }
           m += __popc(mask);
         }
+        });
       }
       uint32_t first;
       if (in_smem) {

@@ -24,6 +24,10 @@
 // always ready, so the loop always progresses; every wait is still bounded (error flag + return
 // after a timeout).
 //
+// When every block can own its share of the vertices in shared memory (up to 1,024 each), the
+// pairs are applied by the tile-local path (rounds_tiled): handshakes between vertices of one
+// block go through shared memory and only pairs crossing blocks through global memory.
+//
 // In pair-log runs each applied pair also gets a level = 1 + max(level of the previous pair at
 // either endpoint): pairs of one level share no microbe, and (level, i, j) is a deterministic
 // sequential order equal in effect to the priority order. The step's "rounds" is the max level.
@@ -119,6 +123,160 @@ __device__ __forceinline__ uint32_t apply_pair(const Bufs& b, uint32_t step, uin
 
 constexpr int POLL_BATCH = 4;  // vertices whose state words one thread loads before testing them
 
+// ---- tile-local interaction: block-owned vertex ranges with handshakes in shared memory ----
+//
+// Cell keys are tile-major, so a contiguous range of cell-ordered vertices is a compact 2D patch.
+// Block b owns the vertices [b V, b V + V) (V = 256 x up to TL_VPT) and keeps their state words,
+// slot ids, degrees and list entries in shared memory. A pair whose two microbes the block owns
+// hands off through shared memory (tens of cycles instead of an L2 round trip); a pair that
+// crosses blocks goes through the global state words: the vertex's word is published there while
+// its current partner is outside the block, the owner of the lower endpoint applies the pair and
+// writes the other endpoint's global word, and that endpoint's owner pulls the change back into
+// shared memory. As in the global path, only the applier of a vertex's current pair writes the
+// vertex's word, so no fences are needed.
+constexpr int TL_VPT = 4;                              // vertices per thread at most
+constexpr uint32_t TL_VMAX = RD_THREADS * TL_VPT;      // vertices per block at most
+constexpr size_t TL_SMEM = TL_VMAX * (8 + 4 + 4 + 4 * SLAB);  // words, slot ids, degrees, lists
+
+__device__ __forceinline__ unsigned long long ld_sh(const unsigned long long* p) {
+  return *(const volatile unsigned long long*)p;
+}
+__device__ __forceinline__ void st_sh(unsigned long long* p, unsigned long long v) {
+  *(volatile unsigned long long*)p = v;
+}
+
+struct TileSmem {
+  unsigned long long* w;  // [TL_VMAX] state words
+  uint32_t* sid;          // [TL_VMAX] slot ids
+  uint32_t* deg;          // [TL_VMAX] list lengths
+  uint32_t* lst;          // [SLAB][TL_VMAX] list entries (slab vertices) / [0][l] = overflow offset
+};
+
+// Entry h of the list of local vertex l (NONE past the end).
+__device__ __forceinline__ uint32_t tl_entry(const Bufs& b, const TileSmem& t, uint32_t l, uint32_t h) {
+  const uint32_t d = t.deg[l];
+  if (h >= d) return NONE;
+  return d <= SLAB ? t.lst[h * TL_VMAX + l] : b.ovf[(size_t)t.lst[l] + h];
+}
+
+// Species of the pair (a, b) after the rock-paper-scissors rule (the reference's table, Philox
+// draw); `vertex` is a's cell-order index, which names the pair's ensemble.
+__device__ __forceinline__ void rps_pair(const Bufs& b, uint32_t vertex, uint32_t step, uint32_t pa, uint32_t pb,
+                                         unsigned long long wa, unsigned long long wb, int* new_a, int* new_b) {
+  const bool a_is_i = pa < pb;
+  const uint32_t pi = a_is_i ? pa : pb, pj = a_is_i ? pb : pa;
+  const int si = state_species(a_is_i ? wa : wb), sj = state_species(a_is_i ? wb : wa);
+  int ni = si, nj = sj;
+  if (si != sj) {
+    const EnsInfo& info = b.ens[b.sens[vertex]];  // the ensemble is read only when a draw may be needed
+    unsigned long long t = 0;
+    bool valid = true;
+    if ((si == 1 && sj == 3) || (si == 3 && sj == 1)) t = info.t_rs;
+    else if ((si == 2 && sj == 1) || (si == 1 && sj == 2)) t = info.t_pr;
+    else if ((si == 3 && sj == 2) || (si == 2 && sj == 3)) t = info.t_sp;
+    else valid = false;  // species outside {1,2,3}: the reference's table has no case -> no change
+    if (valid) {
+      const PairDraw d = pair_draw(pi - info.base, pj - info.base, step, info.seed_lo, info.seed_hi);
+      const bool fwd_wins = d.u53 < t;
+      if (beats(si, sj) == fwd_wins) nj = si;
+      else ni = sj;
+    }
+  }
+  *new_a = a_is_i ? ni : nj;
+  *new_b = a_is_i ? nj : ni;
+}
+
+// Returns false (nothing done) when the step does not fit the tile path.
+__device__ bool rounds_tiled(const Bufs& b, uint32_t step, Ctrl* ctrl, unsigned long long t0) {
+  const uint32_t n_valid = ((volatile uint32_t*)&ctrl->n_valid)[0];
+  const uint32_t vpt = (n_valid + gridDim.x * RD_THREADS - 1) / (gridDim.x * RD_THREADS);
+  if (b.plog || vpt > (uint32_t)TL_VPT) return false;  // grid-uniform decision
+  extern __shared__ unsigned long long tl_raw[];
+  TileSmem t;
+  t.w = tl_raw;
+  t.sid = reinterpret_cast<uint32_t*>(t.w + TL_VMAX);
+  t.deg = t.sid + TL_VMAX;
+  t.lst = t.deg + TL_VMAX;
+  const uint32_t V = max(vpt, 1u) * RD_THREADS;
+  const uint32_t lo = blockIdx.x * V;
+  const uint32_t hi = min(n_valid, lo + V);
+  const uint32_t nloc = hi > lo ? hi - lo : 0u;
+  for (uint32_t l = threadIdx.x; l < nloc; l += RD_THREADS) {
+    const uint32_t s = lo + l;
+    t.w[l] = ld_relaxed(b.wstate + s);  // written by the sweep, which also published every first pair
+    t.sid[l] = b.sid[s];
+    const uint32_t d = b.deg[s];
+    t.deg[l] = d;
+    if (d <= SLAB) {
+      for (uint32_t h = 0; h < d; ++h) t.lst[h * TL_VMAX + l] = b.slab[(size_t)s * SLAB + h];
+    } else {
+      t.lst[l] = b.off[s];
+    }
+  }
+  __syncthreads();
+  uint32_t live = 0;
+  for (int k = 0; k < TL_VPT; ++k)
+    if (threadIdx.x + (uint32_t)k * RD_THREADS < nloc) live |= 1u << k;
+  uint32_t polls = 0;
+  while (live) {
+#pragma unroll
+    for (int k = 0; k < TL_VPT; ++k) {
+      if (!((live >> k) & 1u)) continue;
+      const uint32_t l = threadIdx.x + (uint32_t)k * RD_THREADS, s = lo + l;
+      const unsigned long long ws = ld_sh(t.w + l);
+      const uint32_t u = state_partner(ws);
+      if (u == NONE) {
+        live &= ~(1u << k);
+        continue;
+      }
+      const bool u_local = u >= lo && u < hi;
+      if (s > u) {
+        // the owner of u applies; while u is outside the block, take the result from global memory.
+        // Positions only grow: a global word behind the shared one (published a moment after a
+        // local apply wrote the shared word, or left from an earlier publish) is not taken.
+        if (!u_local) {
+          const unsigned long long g = ld_relaxed(b.wstate + s);
+          if (state_pos(g) > state_pos(ws)) st_sh(t.w + l, g);
+        }
+        continue;
+      }
+      const unsigned long long wu = u_local ? ld_sh(t.w + (u - lo)) : ld_relaxed(b.wstate + u);
+      if (state_partner(wu) != s) continue;
+      // apply (s, u): this thread owns the lower endpoint
+      const uint32_t hs = state_pos(ws), hu = state_pos(wu);
+      const uint32_t ns = tl_entry(b, t, l, hs + 1u);
+      uint32_t nu, pu;
+      if (u_local) {
+        nu = tl_entry(b, t, u - lo, hu + 1u);
+        pu = t.sid[u - lo];
+      } else {
+        const uint32_t du = b.deg[u];
+        nu = hu + 1u < du ? (du <= SLAB ? b.slab[(size_t)u * SLAB + hu + 1u] : b.ovf[(size_t)b.off[u] + hu + 1u]) : NONE;
+        pu = b.sid[u];
+      }
+      const uint32_t ps = t.sid[l];
+      int new_s, new_u;
+      rps_pair(b, s, step, ps, pu, ws, wu, &new_s, &new_u);
+      if (nu == NONE) b.species[pu] = (int8_t)new_u;
+      if (ns == NONE) b.species[ps] = (int8_t)new_s;
+      const unsigned long long nwu = pack_state(nu, hu + 1u, new_u), nws = pack_state(ns, hs + 1u, new_s);
+      if (u_local) {
+        st_sh(t.w + (u - lo), nwu);
+        if (nu != NONE && (nu < lo || nu >= hi)) st_relaxed(b.wstate + u, nwu);  // u's next pair crosses
+      } else {
+        st_relaxed(b.wstate + u, nwu);  // u's owner pulls it
+      }
+      st_sh(t.w + l, nws);
+      if (ns != NONE && (ns < lo || ns >= hi)) st_relaxed(b.wstate + s, nws);  // s's next pair crosses
+    }
+    if (live && ((++polls & 63u) == 0u) && globaltimer() - t0 > ROUNDS_TIMEOUT_NS) {
+      atomicOr(&ctrl->err, (uint32_t)ERRB_TIMEOUT);
+      break;
+    }
+  }
+  return true;
+}
+
 __global__ void __launch_bounds__(RD_THREADS) k_rounds(Bufs b, StepArgs a, Ctrl* ctrl) {
   pdl_wait();
   if (((volatile uint32_t*)&ctrl->halt)[0]) return;
@@ -128,6 +286,7 @@ __global__ void __launch_bounds__(RD_THREADS) k_rounds(Bufs b, StepArgs a, Ctrl*
   const uint32_t first = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t max_level = 0;
   const unsigned long long t0 = globaltimer();
+  if (rounds_tiled(b, step, ctrl, t0)) return;  // levels are tracked only in pair-log runs
   uint32_t polls = 0;
   if (cnt <= (uint32_t)POLL_BATCH * stride) {
     // every thread owns at most POLL_BATCH vertices: keep their ids in registers and stop polling
@@ -207,7 +366,8 @@ __global__ void __launch_bounds__(RD_THREADS) k_rounds(Bufs b, StepArgs a, Ctrl*
 int rounds_grid(int device, int* block) {
   int sms = 0, per_sm = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rounds, RD_THREADS, 0);
+  cudaFuncSetAttribute(k_rounds, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TL_SMEM);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rounds, RD_THREADS, TL_SMEM);
   if (per_sm < 1) per_sm = 1;
   if (per_sm > 4) per_sm = 4;
   *block = RD_THREADS;
@@ -218,7 +378,7 @@ cudaError_t launch_rounds(const Bufs& b, const StepArgs& a, Ctrl* ctrl, int grid
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)grid);
   cfg.blockDim = dim3((unsigned)block);
-  cfg.dynamicSmemBytes = 0;
+  cfg.dynamicSmemBytes = TL_SMEM;  // the tile-local path's vertex state
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeCooperative;

@@ -97,6 +97,30 @@ struct EnsGrid {
   uint32_t pad;
 };
 
+// Cell numbering inside an ensemble's key range is tile-major: TILE x TILE cells form a tile,
+// tiles are numbered row by row, cells inside a tile row by row. Cell-ordered particles of one
+// tile are then contiguous, so a contiguous range of them is a compact 2D patch (the interaction
+// kernel gives such ranges to its blocks). A grid's key range is padded to whole tiles.
+constexpr uint32_t TILE = 16;
+__host__ __device__ inline uint32_t tiles_x(const EnsGrid& g) { return ((uint32_t)g.ncx + TILE - 1) / TILE; }
+__host__ __device__ inline uint32_t cell_index(const EnsGrid& g, uint32_t cx, uint32_t cy) {
+  return ((cy / TILE) * tiles_x(g) + cx / TILE) * (TILE * TILE) + (cy % TILE) * TILE + (cx % TILE);
+}
+__host__ __device__ inline void cell_coords(const EnsGrid& g, uint32_t k, uint32_t* cx, uint32_t* cy) {
+  const uint32_t t = k / (TILE * TILE), in = k % (TILE * TILE), ntx = tiles_x(g);
+  *cx = (t % ntx) * TILE + in % TILE;
+  *cy = (t / ntx) * TILE + in / TILE;
+}
+// Calls f(first key, last key) for the cells x0..x1 of row ry, one contiguous key run per tile.
+template <class F>
+__device__ __forceinline__ void row_runs(const EnsGrid& g, int x0, int x1, int ry, F&& f) {
+  for (int a = x0; a <= x1;) {
+    const int b = min(x1, (a / (int)TILE) * (int)TILE + (int)TILE - 1);
+    f(g.cell_base + cell_index(g, (uint32_t)a, (uint32_t)ry), g.cell_base + cell_index(g, (uint32_t)b, (uint32_t)ry));
+    a = b + 1;
+  }
+}
+
 // Velocity field geometry shared by all ensembles.
 struct FieldView {
   const float2* uv;   // [F][nt][ny][nx]
