@@ -82,11 +82,14 @@ __device__ __forceinline__ void for_neighbours(const Bufs& b, const PairParams& 
   for (int dy = -1; dy <= 1; ++dy) {
     const int ry = (int)v.cy + dy;
     if (ry < 0 || ry >= v.g.ncy) continue;
-    row_runs(v.g, max((int)v.cx - 1, 0), min((int)v.cx + 1, v.g.ncx - 1), ry, [&](uint32_t kl, uint32_t kh) {
-      const uint32_t t1 = b.cstart[kh + 1];
-      for (uint32_t t = b.cstart[kl]; t < t1; ++t)
+    const RowRuns rr = row_runs(v.g, max((int)v.cx - 1, 0), min((int)v.cx + 1, v.g.ncx - 1), ry);
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      if (q >= rr.n) break;
+      const uint32_t t1 = b.cstart[rr.hi[q] + 1];
+      for (uint32_t t = b.cstart[rr.lo[q]]; t < t1; ++t)
         if (t != v.s && within(pp, v.ps, b.spos[t])) f(t);
-    });
+    }
   }
 }
 
@@ -231,13 +234,13 @@ __device__ __forceinline__ void count_runs(const Vertex& v, const Bufs& b, uint3
     r1[1] = b.cstart[ke + 1];
   }
   if ((int)v.cy + 1 < v.g.ncy) {
-    int q = 2;
-    row_runs(v.g, max((int)v.cx - 1, 0), min((int)v.cx + 1, v.g.ncx - 1), (int)v.cy + 1,
-             [&](uint32_t kl, uint32_t kh) {
-               r0[q] = b.cstart[kl];
-               r1[q] = b.cstart[kh + 1];
-               ++q;
-             });
+    const RowRuns rr = row_runs(v.g, max((int)v.cx - 1, 0), min((int)v.cx + 1, v.g.ncx - 1), (int)v.cy + 1);
+    r0[2] = b.cstart[rr.lo[0]];
+    r1[2] = b.cstart[rr.hi[0] + 1];
+    if (rr.n == 2) {
+      r0[3] = b.cstart[rr.lo[1]];
+      r1[3] = b.cstart[rr.hi[1] + 1];
+    }
   }
 }
 
@@ -441,8 +444,11 @@ __global__ void __launch_bounds__(LONG_WARPS * 32) k_sweep_long(Bufs b, PairPara
       for (int dy = -1; dy <= 1; ++dy) {
         const int ry = (int)v.cy + dy;
         if (ry < 0 || ry >= v.g.ncy) continue;
-        row_runs(v.g, max((int)v.cx - 1, 0), min((int)v.cx + 1, v.g.ncx - 1), ry, [&](uint32_t kl, uint32_t kh) {
-        const uint32_t t0 = b.cstart[kl], t1 = b.cstart[kh + 1];
+        const RowRuns rr = row_runs(v.g, max((int)v.cx - 1, 0), min((int)v.cx + 1, v.g.ncx - 1), ry);
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+        if (q >= rr.n) break;
+        const uint32_t t0 = b.cstart[rr.lo[q]], t1 = b.cstart[rr.hi[q] + 1];
         for (uint32_t tb = t0; tb < t1; tb += 32) {
           const uint32_t t = tb + lane;
           const bool ok = t < t1 && t != s && within(pp, v.ps, b.spos[t]);
@@ -462,7 +468,7 @@ __global__ void __launch_bounds__(LONG_WARPS * 32) k_sweep_long(Bufs b, PairPara
           }
           m += __popc(mask);
         }
-        });
+        }
       }
       uint32_t first;
       if (in_smem) {

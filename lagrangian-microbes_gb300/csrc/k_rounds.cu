@@ -134,6 +134,7 @@ constexpr int POLL_BATCH = 4;  // vertices whose state words one thread loads be
 // writes the other endpoint's global word, and that endpoint's owner pulls the change back into
 // shared memory. As in the global path, only the applier of a vertex's current pair writes the
 // vertex's word, so no fences are needed.
+static_assert(SLAB == 8, "the tile path copies a slab row as two 16-byte loads");
 constexpr int TL_VPT = 4;                              // vertices per thread at most
 constexpr uint32_t TL_VMAX = RD_THREADS * TL_VPT;      // vertices per block at most
 constexpr size_t TL_SMEM = TL_VMAX * (8 + 4 + 4 + 4 * SLAB);  // words, slot ids, degrees, lists
@@ -201,16 +202,27 @@ __device__ bool rounds_tiled(const Bufs& b, uint32_t step, Ctrl* ctrl, unsigned 
   const uint32_t lo = blockIdx.x * V;
   const uint32_t hi = min(n_valid, lo + V);
   const uint32_t nloc = hi > lo ? hi - lo : 0u;
-  for (uint32_t l = threadIdx.x; l < nloc; l += RD_THREADS) {
-    const uint32_t s = lo + l;
-    t.w[l] = ld_relaxed(b.wstate + s);  // written by the sweep, which also published every first pair
-    t.sid[l] = b.sid[s];
-    const uint32_t d = b.deg[s];
-    t.deg[l] = d;
-    if (d <= SLAB) {
-      for (uint32_t h = 0; h < d; ++h) t.lst[h * TL_VMAX + l] = b.slab[(size_t)s * SLAB + h];
-    } else {
-      t.lst[l] = b.off[s];
+  // every load of the set-up is independent: the whole slab row (two 16-byte loads; entries past
+  // the degree are never read) and the overflow offset, for all of the thread's vertices at once
+#pragma unroll
+  for (int k = 0; k < TL_VPT; ++k) {
+    const uint32_t l = threadIdx.x + (uint32_t)k * RD_THREADS;
+    if (l < nloc) {
+      const uint32_t s = lo + l;
+      const unsigned long long w0 = ld_relaxed(b.wstate + s);  // written by the sweep, which published every first pair
+      const uint32_t sid = b.sid[s], d = b.deg[s], off = b.off[s];
+      const uint4* row = reinterpret_cast<const uint4*>(b.slab + (size_t)s * SLAB);
+      const uint4 r0 = row[0], r1 = row[1];
+      t.w[l] = w0;
+      t.sid[l] = sid;
+      t.deg[l] = d;
+      if (d <= SLAB) {
+        t.lst[0 * TL_VMAX + l] = r0.x, t.lst[1 * TL_VMAX + l] = r0.y, t.lst[2 * TL_VMAX + l] = r0.z;
+        t.lst[3 * TL_VMAX + l] = r0.w, t.lst[4 * TL_VMAX + l] = r1.x, t.lst[5 * TL_VMAX + l] = r1.y;
+        t.lst[6 * TL_VMAX + l] = r1.z, t.lst[7 * TL_VMAX + l] = r1.w;
+      } else {
+        t.lst[l] = off;
+      }
     }
   }
   __syncthreads();

@@ -111,14 +111,25 @@ __host__ __device__ inline void cell_coords(const EnsGrid& g, uint32_t k, uint32
   *cx = (t % ntx) * TILE + in % TILE;
   *cy = (t / ntx) * TILE + in / TILE;
 }
-// Calls f(first key, last key) for the cells x0..x1 of row ry, one contiguous key run per tile.
-template <class F>
-__device__ __forceinline__ void row_runs(const EnsGrid& g, int x0, int x1, int ry, F&& f) {
-  for (int a = x0; a <= x1;) {
-    const int b = min(x1, (a / (int)TILE) * (int)TILE + (int)TILE - 1);
-    f(g.cell_base + cell_index(g, (uint32_t)a, (uint32_t)ry), g.cell_base + cell_index(g, (uint32_t)b, (uint32_t)ry));
-    a = b + 1;
+// The keys of cells x0..x1 (at most three) of row ry: one contiguous run, or two when the cells
+// straddle a tile edge. Fixed-size, so the callers' loops unroll with static indices.
+struct RowRuns {
+  uint32_t lo[2], hi[2];  // first and last key of each run
+  int n;
+};
+__device__ __forceinline__ RowRuns row_runs(const EnsGrid& g, int x0, int x1, int ry) {
+  RowRuns r;
+  const int split = (x0 / (int)TILE) != (x1 / (int)TILE) ? (x0 / (int)TILE) * (int)TILE + (int)TILE - 1 : x1;
+  r.lo[0] = g.cell_base + cell_index(g, (uint32_t)x0, (uint32_t)ry);
+  r.hi[0] = g.cell_base + cell_index(g, (uint32_t)split, (uint32_t)ry);
+  r.n = 1;
+  r.lo[1] = r.hi[1] = 0;
+  if (split < x1) {
+    r.lo[1] = g.cell_base + cell_index(g, (uint32_t)split + 1, (uint32_t)ry);
+    r.hi[1] = g.cell_base + cell_index(g, (uint32_t)x1, (uint32_t)ry);
+    r.n = 2;
   }
+  return r;
 }
 
 // Velocity field geometry shared by all ensembles.
