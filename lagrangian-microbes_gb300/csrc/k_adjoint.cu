@@ -17,6 +17,8 @@
 // a node pass adds, for every grid node, the four cells around it in a fixed order and spreads the
 // three stage times onto the field's frames with the linear-in-time weights. No float atomics: the
 // gradient is bit-identical from run to run.
+#include <algorithm>
+
 #include "lm_field.cuh"
 #include "lm_internal.h"
 
@@ -260,7 +262,8 @@ template <class T>
 __global__ void __launch_bounds__(256) k_adj_step(FieldView f, AdjStep s, T dt, uint32_t n, const T* __restrict__ xs,
                                                   const T* __restrict__ ys, const uint8_t* __restrict__ sts,
                                                   T* __restrict__ lx, T* __restrict__ ly, float4* __restrict__ rec,
-                                                  uint32_t* __restrict__ key, uint32_t sent) {
+                                                  uint32_t* __restrict__ key, uint32_t sent, uint32_t* __restrict__ mkey,
+                                                  uint32_t* __restrict__ mcode, uint32_t msent, uint32_t* err) {
   const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
   const Geo<T> g(f);
@@ -277,10 +280,32 @@ __global__ void __launch_bounds__(256) k_adj_step(FieldView f, AdjStep s, T dt, 
     const T ny = y + (J1.flat + T(2) * J2.flat + T(2) * J3.flat + J4.flat) * (dt * (T(1) / T(6)));
     ok = isfinite(nx) && isfinite(ny);
   }
-  uint4* kq = reinterpret_cast<uint4*>(key) + p;
   if (!ok) {  // frozen this step: x_{m+1} = x_m, the adjoint passes through
-    *kq = make_uint4(sent, sent, sent, sent);
+    if (mkey)
+      mkey[p] = msent;
+    else
+      reinterpret_cast<uint4*>(key)[p] = make_uint4(sent, sent, sent, sent);
     return;
+  }
+  if (mkey) {
+    // gather form: every stage is coded by the slot (dj + 1) * 3 + (di + 1) of its cell around the
+    // cell where the step starts (stage 1), 4 bits a stage; the microbe is keyed by that cell * 2 +
+    // (1 when a stage leaves the cell). A stage outside the 3 x 3 cells sets ADJ_WIDE and the
+    // backward is redone with the record sort.
+    const uint32_t cw = (uint32_t)(f.nx - 1);
+    const int bi = (int)(J1.cell % cw), bj = (int)(J1.cell / cw);
+    const uint32_t cs[3] = {J2.cell, J3.cell, J4.cell};
+    uint32_t code = 4u;
+    bool wide = false;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      const int di = (int)(cs[q] % cw) - bi, dj = (int)(cs[q] / cw) - bj;
+      wide |= abs(di) > 1 || abs(dj) > 1;
+      code |= (uint32_t)((dj + 1) * 3 + (di + 1)) << (4 * (q + 1));
+    }
+    mcode[p] = code;
+    mkey[p] = 2u * J1.cell + (code != 0x4444u ? 1u : 0u);
+    if (wide) atomicOr(err, ADJ_WIDE);
   }
   const T gx = lx[p], gy = ly[p];
   const T h6 = dt * (T(1) / T(6)), h3 = dt * (T(1) / T(3)), h2 = T(0.5) * dt;
@@ -302,7 +327,9 @@ __global__ void __launch_bounds__(256) k_adj_step(FieldView f, AdjStep s, T dt, 
   rq[1] = make_float4((float)J2.a, (float)J2.b, (float)(g2x * J2.inv_mc), (float)(g2y * invM));
   rq[2] = make_float4((float)J3.a, (float)J3.b, (float)(g3x * J3.inv_mc), (float)(g3y * invM));
   rq[3] = make_float4((float)J4.a, (float)J4.b, (float)(g4x * J4.inv_mc), (float)(g4y * invM));
-  *kq = make_uint4(4u * J1.cell + 0u, 4u * J2.cell + 1u, 4u * J3.cell + 1u, 4u * J4.cell + 2u);
+  if (!mkey)
+    reinterpret_cast<uint4*>(key)[p] =
+        make_uint4(4u * J1.cell + 0u, 4u * J2.cell + 1u, 4u * J3.cell + 1u, 4u * J4.cell + 2u);
 }
 
 // Cell path of every microbe over steps [0, n_steps): the grid cell (j * nx + i) of each stage that
@@ -554,9 +581,162 @@ __global__ void __launch_bounds__(256) k_adj_reduce(uint32_t ncells, uint32_t* _
   }
 }
 
+// Gather form, after the stable sort of the microbe keys (cell * 2 + leaves-the-cell, so in index
+// order within a key): bounds of every key, the stage codes in sorted order, and the list of target
+// cells: a cell with microbes, and the 3 x 3 cells around one whose microbes leave it, each listed
+// once a step (mark[c] takes the step's stamp when c is listed; tcnt counts the list).
+__global__ void k_adj_cells(const uint32_t* __restrict__ skey, const uint32_t* __restrict__ sval, uint32_t m,
+                            uint32_t cw, uint32_t ch, const uint32_t* __restrict__ mcode,
+                            uint32_t* __restrict__ scode, uint32_t* __restrict__ cst, uint32_t* __restrict__ cen,
+                            uint32_t* __restrict__ mark, uint32_t stamp, uint32_t* __restrict__ tlist,
+                            uint32_t* __restrict__ tcnt) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const uint32_t k = skey[i];
+  if (k >= 2u * cw * ch) return;  // frozen microbes sort last
+  scode[i] = mcode[sval[i]];
+  if (i + 1 == m || skey[i + 1] != k) cen[k] = i + 1;
+  if (i != 0 && skey[i - 1] == k) return;
+  cst[k] = i;
+  const uint32_t b = k >> 1;
+  if (!(k & 1u)) {
+    if (atomicExch(&mark[b], stamp) != stamp) tlist[atomicAdd(tcnt, 1u)] = b;
+    return;
+  }
+  const int bi = (int)(b % cw), bj = (int)(b / cw);
+  const uint32_t cells = cw * ch;
+  uint32_t tc[9], old[9], fresh = 0;
+#pragma unroll
+  for (int r = 0; r < 9; ++r) {  // no branch between the exchanges: they are issued together
+    const int ti = bi + r % 3 - 1, tj = bj + r / 3 - 1;
+    const bool in = ti >= 0 && tj >= 0 && ti < (int)cw && tj < (int)ch;
+    tc[r] = in ? (uint32_t)tj * cw + (uint32_t)ti : cells;  // mark[cells]: a slot no target reads
+    old[r] = atomicExch(&mark[tc[r]], stamp);
+  }
+#pragma unroll
+  for (int r = 0; r < 9; ++r) fresh |= (tc[r] != cells && old[r] != stamp) ? 1u << r : 0u;
+  if (!fresh) return;
+  uint32_t o = atomicAdd(tcnt, (uint32_t)__popc(fresh));
+#pragma unroll
+  for (int r = 0; r < 9; ++r)
+    if (fresh & (1u << r)) tlist[o++] = tc[r];
+}
+
+template <int G>
+__device__ __forceinline__ void gather_add(const float4& rr, float (&acc)[3][8], float (&cmp)[3][8]) {
+  const float a = rr.x, b = rr.y;
+  const float w[4] = {(1.f - a) * (1.f - b), a * (1.f - b), (1.f - a) * b, a * b};
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    neumaier(acc[G][q], cmp[G][q], w[q] * rr.z);
+    neumaier(acc[G][4 + q], cmp[G][4 + q], w[q] * rr.w);
+  }
+}
+
+// One warp per listed target cell c. Neighbour cell r = (dj + 1) * 3 + (di + 1) in turn: its whole
+// run for r = 4 (c itself), else only its microbes that leave it; lane l takes entries l, l + 32,
+// ... of each run, and a stage of a microbe of neighbour r lands in c when its slot is 8 - r. Stage
+// times: stage 1 at t (group 0), stages 2 and 3 at t + dt/2 (group 1), stage 4 at t + dt (group 2).
+// Sums as in k_adj_reduce (Neumaier float32 per lane, fixed warp tree), so the result does not
+// depend on which warp took c.
+__global__ void __launch_bounds__(256) k_adj_gather(uint32_t cw, uint32_t ch, const uint32_t* __restrict__ tcnt,
+                                                    const uint32_t* __restrict__ tlist,
+                                                    const uint32_t* __restrict__ cst,
+                                                    const uint32_t* __restrict__ cen,
+                                                    const uint32_t* __restrict__ scode,
+                                                    const uint32_t* __restrict__ sval,
+                                                    const float4* __restrict__ rec, float* __restrict__ csum) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t nt = *tcnt;
+  const uint32_t stride = gridDim.x * (blockDim.x >> 5);
+  for (uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < nt; t += stride) {
+    const uint32_t c = tlist[t];
+    const int ci = (int)(c % cw), cj = (int)(c / cw);
+    uint32_t lo = 0, hi = 0;
+    if (lane < 9) {
+      const int bi = ci + (int)(lane % 3) - 1, bj = cj + (int)(lane / 3) - 1;
+      if (bi >= 0 && bj >= 0 && bi < (int)cw && bj < (int)ch) {
+        const uint32_t k1 = 2u * ((uint32_t)bj * cw + (uint32_t)bi) + 1u;
+        const uint32_t e1 = cen[k1];  // bounds of absent keys: cen = 0
+        if (lane == 4) {              // keys 2b and 2b + 1 are adjacent in sorted order
+          const uint32_t e0 = cen[k1 - 1];
+          lo = e0 ? cst[k1 - 1] : (e1 ? cst[k1] : 0u);
+          hi = e1 ? e1 : e0;
+        } else if (e1) {
+          lo = cst[k1];
+          hi = e1;
+        }
+      }
+    }
+    float acc[3][8], cmp[3][8];
+#pragma unroll
+    for (int g = 0; g < 3; ++g)
+#pragma unroll
+      for (int q = 0; q < 8; ++q) acc[g][q] = cmp[g][q] = 0.f;
+    {  // c's own microbes: stage 1 always lands in c, the others mostly; two entries in flight
+      const uint32_t rlo = __shfl_sync(0xffffffffu, lo, 4), rhi = __shfl_sync(0xffffffffu, hi, 4);
+      for (uint32_t s = rlo + lane; s < rhi; s += 64) {
+        const uint32_t s2 = s + 32;
+        const bool two = s2 < rhi;
+        const uint32_t code0 = scode[s], code1 = two ? scode[s2] : 0u;
+        const float4* rp0 = rec + 4 * (size_t)sval[s];
+        const float4* rp1 = rec + 4 * (size_t)(two ? sval[s2] : 0u);
+        float4 r[2][4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) r[0][q] = rp0[q];
+        if (two) {
+#pragma unroll
+          for (int q = 0; q < 4; ++q) r[1][q] = rp1[q];
+        }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          if (h == 1 && !two) break;
+          const uint32_t code = h ? code1 : code0;
+          gather_add<0>(r[h][0], acc, cmp);
+          if (((code >> 4) & 15u) == 4u) gather_add<1>(r[h][1], acc, cmp);
+          if (((code >> 8) & 15u) == 4u) gather_add<1>(r[h][2], acc, cmp);
+          if (((code >> 12) & 15u) == 4u) gather_add<2>(r[h][3], acc, cmp);
+        }
+      }
+    }
+#pragma unroll 1
+    for (int r = 0; r < 9; ++r) {
+      if (r == 4) continue;
+      const uint32_t rlo = __shfl_sync(0xffffffffu, lo, r), rhi = __shfl_sync(0xffffffffu, hi, r);
+      const uint32_t slot = 8u - (uint32_t)r;
+      for (uint32_t s = rlo + lane; s < rhi; s += 64) {
+        const uint32_t s2 = s + 32;
+        const uint32_t c0 = scode[s];
+        const uint32_t c1 = s2 < rhi ? scode[s2] : 0xffffffffu;  // slot 15 matches nothing
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const uint32_t code = h ? c1 : c0;
+          const bool m1 = ((code >> 4) & 15u) == slot, m2 = ((code >> 8) & 15u) == slot;
+          const bool m3 = ((code >> 12) & 15u) == slot;  // stage 1 never leaves its cell
+          if (!(m1 | m2 | m3)) continue;
+          const float4* rp = rec + 4 * (size_t)sval[h ? s2 : s];
+          if (m1) gather_add<1>(rp[1], acc, cmp);
+          if (m2) gather_add<1>(rp[2], acc, cmp);
+          if (m3) gather_add<2>(rp[3], acc, cmp);
+        }
+      }
+    }
+    float* out = csum + (size_t)c * 24;
+#pragma unroll
+    for (int g = 0; g < 3; ++g)
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        float v = acc[g][q] + cmp[g][q];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == (uint32_t)(g * 8 + q)) out[g * 8 + q] = v;
+      }
+  }
+}
+
 // One thread per grid node: the four cells around it in a fixed order, then the three stage times
 // spread onto frames k_g (weight 1 - w_g) and k_g + 1 (weight w_g), added to the gradient.
 __global__ void __launch_bounds__(256) k_adj_nodes(int nx, int ny, AdjStep s, const float* __restrict__ csum,
+                                                   const uint32_t* __restrict__ mark, uint32_t stamp,
                                                    float* __restrict__ gu, float* __restrict__ gv) {
   const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= (uint32_t)nx * (uint32_t)ny) return;
@@ -569,7 +749,9 @@ __global__ void __launch_bounds__(256) k_adj_nodes(int nx, int ny, AdjStep s, co
   for (int t = 0; t < 4; ++t) {
     const int ci = ci_[t], cj = cj_[t];
     if (ci < 0 || cj < 0 || ci > nx - 2 || cj > ny - 2) continue;
-    const float* cs = csum + ((size_t)cj * cw + ci) * 24;
+    const size_t cell = (size_t)cj * cw + ci;
+    if (mark && mark[cell] != stamp) continue;  // gather form: only listed cells were summed
+    const float* cs = csum + cell * 24;
 #pragma unroll
     for (int g = 0; g < 3; ++g) {
       U[g] += cs[g * 8 + corner[t]];
@@ -673,14 +855,33 @@ void launch_adj_forward(const FieldView& f, int prec, const AdjStep* table, int 
 
 void launch_adj_step(const FieldView& f, int prec, const AdjStep& s, double dt, uint32_t n, const void* x,
                      const void* y, const uint8_t* status, void* lx, void* ly, float4* rec, uint32_t* key, uint32_t sent,
-                     cudaStream_t st) {
+                     uint32_t* mkey, uint32_t* mcode, uint32_t msent, uint32_t* err, cudaStream_t st) {
   if (!n) return;
   if (prec == ADJ_F64)
     k_adj_step<double><<<grid_for(n, 256), 256, 0, st>>>(f, s, dt, n, (const double*)x, (const double*)y, status,
-                                                         (double*)lx, (double*)ly, rec, key, sent);
+                                                         (double*)lx, (double*)ly, rec, key, sent, mkey, mcode, msent,
+                                                         err);
   else
     k_adj_step<float><<<grid_for(n, 256), 256, 0, st>>>(f, s, (float)dt, n, (const float*)x, (const float*)y, status,
-                                                        (float*)lx, (float*)ly, rec, key, sent);
+                                                        (float*)lx, (float*)ly, rec, key, sent, mkey, mcode, msent,
+                                                        err);
+}
+
+void launch_adj_cells(const uint32_t* skey, const uint32_t* sval, uint32_t m, uint32_t cw, uint32_t ch,
+                      const uint32_t* mcode, uint32_t* scode, uint32_t* cst, uint32_t* cen, uint32_t* mark,
+                      uint32_t stamp, uint32_t* tlist, uint32_t* tcnt, cudaStream_t st) {
+  if (m) k_adj_cells<<<grid_for(m, 256), 256, 0, st>>>(skey, sval, m, cw, ch, mcode, scode, cst, cen, mark, stamp,
+                                                       tlist, tcnt);
+}
+
+void launch_adj_gather(uint32_t cw, uint32_t ch, const uint32_t* tcnt, const uint32_t* tlist, const uint32_t* cst,
+                       const uint32_t* cen, const uint32_t* scode, const uint32_t* sval, const float4* rec,
+                       float* csum, int sms, cudaStream_t st) {
+  const size_t ncells = (size_t)cw * ch;
+  unsigned blocks = grid_for(ncells * 32, 256);
+  const unsigned cap = (unsigned)(sms > 0 ? sms : 152) * 8u;
+  if (blocks > cap) blocks = cap;
+  if (ncells) k_adj_gather<<<blocks, 256, 0, st>>>(cw, ch, tcnt, tlist, cst, cen, scode, sval, rec, csum);
 }
 
 void launch_adj_signature(const FieldView& f, int prec, const AdjStep* table, int n_steps, double dt, uint32_t n,
@@ -736,8 +937,9 @@ void launch_adj_reduce(uint32_t ncells, uint32_t* cst, uint32_t* cen, const uint
   if (ncells) k_adj_reduce<<<blocks, 256, 0, st>>>(ncells, cst, cen, sval, rec, csum);
 }
 
-void launch_adj_nodes(int nx, int ny, const AdjStep& s, const float* csum, float* gu, float* gv, cudaStream_t st) {
-  k_adj_nodes<<<grid_for((size_t)nx * ny, 256), 256, 0, st>>>(nx, ny, s, csum, gu, gv);
+void launch_adj_nodes(int nx, int ny, const AdjStep& s, const float* csum, const uint32_t* mark, uint32_t stamp,
+                      float* gu, float* gv, cudaStream_t st) {
+  k_adj_nodes<<<grid_for((size_t)nx * ny, 256), 256, 0, st>>>(nx, ny, s, csum, mark, stamp, gu, gv);
 }
 
 }  // namespace lm

@@ -9,6 +9,9 @@
 //   seg_*   T, T, uint8 [K][n]             state before every step of the segment being reversed
 //   lx, ly  T [n]                          the adjoint dL/dx_m
 //   rec     float4 [4n], key/k1/k2/v1/v2 uint32 [4n]  stage records and the radix-sort ping-pong
+//   mkey, mcode, scode  uint32 [n]         gather form: key 2 * (cell where the step starts) + (a stage
+//                                          leaves it), slots of the stages around it (sorted: scode)
+//   mark [C + 1], tlist [C], tcnt [S]      gather form: target cells listed per step (stamped in mark)
 //   cst/cen uint32 [4C + 1], csum float [C][3][8]     segment bounds, per-cell corner sums
 #include <cuda_runtime.h>
 
@@ -54,7 +57,7 @@ struct lm_adjoint {
   DBuf<float> csum;
   DBuf<uint8_t> st, ck_st, seg_st;
   DBuf<float4> rec;
-  DBuf<uint32_t> key, k1, k2, v1, v2, hist, hscan, bsum, cst, cen;
+  DBuf<uint32_t> key, k1, k2, v1, v2, hist, hscan, bsum, cst, cen, mkey, mcode, scode, mark, tlist, tcnt;
   uint32_t* err_d = nullptr;
   uint32_t* err_h = nullptr;
 };
@@ -158,7 +161,7 @@ int lm_adjoint_destroy(lm_adjoint* a) {
   release(a->x), release(a->y), release(a->ck_x), release(a->ck_y), release(a->seg_x), release(a->seg_y);
   release(a->lx), release(a->ly), release(a->fin_x), release(a->fin_y), release(a->csum), release(a->st), release(a->ck_st), release(a->seg_st);
   release(a->rec), release(a->key), release(a->k1), release(a->k2), release(a->v1), release(a->v2);
-  release(a->hist), release(a->hscan), release(a->bsum), release(a->cst), release(a->cen);
+  release(a->hist), release(a->hscan), release(a->bsum), release(a->cst), release(a->cen), release(a->mkey);
   if (a->err_d) cudaFree(a->err_d);
   if (a->err_h) cudaFreeHost(a->err_h);
   delete a;
@@ -215,7 +218,9 @@ int lm_adjoint_forward(lm_adjoint* a, const float* u, const float* v, int nt, in
       (r = grow(a, a->seg_x, es * checkpoint_every * N)) || (r = grow(a, a->seg_y, es * checkpoint_every * N)) ||
       (r = grow(a, a->seg_st, (size_t)checkpoint_every * N)) || (r = grow(a, a->lx, es * N)) ||
       (r = grow(a, a->ly, es * N)) || (r = grow(a, a->fin_x, es * N)) || (r = grow(a, a->fin_y, es * N)) ||
-      (r = grow(a, a->rec, M)) || (r = grow(a, a->key, M)) ||
+      (r = grow(a, a->rec, M)) || (r = grow(a, a->key, M)) || (r = grow(a, a->mkey, N)) ||
+      (r = grow(a, a->mcode, N)) || (r = grow(a, a->scode, N)) || (r = grow(a, a->mark, cells + 1)) ||
+      (r = grow(a, a->tlist, cells)) || (r = grow(a, a->tcnt, (size_t)n_steps)) ||
       (r = grow(a, a->k1, M)) || (r = grow(a, a->k2, M)) || (r = grow(a, a->v1, M)) || (r = grow(a, a->v2, M)) ||
       (r = grow(a, a->hist, adj_sort_hist_len((uint32_t)M))) || (r = grow(a, a->hscan, adj_sort_hist_len((uint32_t)M))) ||
       (r = grow(a, a->bsum, SCAN_BLOCKS)) || (r = grow(a, a->cst, 4 * cells + 1, true)) ||
@@ -280,30 +285,61 @@ int lm_adjoint_backward(lm_adjoint* a, const float* g_lon, const float* g_lat, f
   const int kb = key_bits_for(sent);
   const uint32_t M = 4u * N;
   const size_t es = a->prec == ADJ_F64 ? sizeof(double) : sizeof(float);
-  ACK(cudaMemsetAsync(g_u, 0, fe * sizeof(float), st));
-  ACK(cudaMemsetAsync(g_v, 0, fe * sizeof(float), st));
-  if (N) {
-    launch_adj_seed(a->prec, N, g_lon, g_lat, a->lx.p, a->ly.p, st);
-  }
-  AdjSortBufs sb{a->key.p, a->k1.p, a->k2.p, a->v1.p, a->v2.p, a->hist.p, a->hscan.p, a->bsum.p};
-  for (int s = a->n_ck - 1; s >= 0 && N; --s) {
-    const int m0 = s * a->K, m1 = std::min(m0 + a->K, a->n_steps);
-    ACK(cudaMemcpyAsync(a->x.p, a->ck_x.p + es * s * N, es * N, cudaMemcpyDeviceToDevice, st));
-    ACK(cudaMemcpyAsync(a->y.p, a->ck_y.p + es * s * N, es * N, cudaMemcpyDeviceToDevice, st));
-    ACK(cudaMemcpyAsync(a->st.p, a->ck_st.p + (size_t)s * N, N, cudaMemcpyDeviceToDevice, st));
-    launch_adj_forward(a->fv, a->prec, a->table.p, m0, m1, a->dt, N, a->x.p, a->y.p, a->st.p, a->seg_x.p, a->seg_y.p,
-                       a->seg_st.p, a->err_d, st);
-    for (int m = m1 - 1; m >= m0; --m) {
-      const size_t o = (size_t)(m - m0) * N;
-      const AdjStep& sg = a->table_h[m];
-      launch_adj_step(a->fv, a->prec, sg, a->dt, N, a->seg_x.p + es * o, a->seg_y.p + es * o, a->seg_st.p + o,
-                      a->lx.p, a->ly.p, a->rec.p, a->key.p, sent, st);
-      const uint32_t *skey, *sval;
-      adj_sort(sb, M, kb, st, &skey, &sval);
-      launch_adj_bounds(skey, M, sent, a->cst.p, a->cen.p, st);
-      launch_adj_reduce(cells, a->cst.p, a->cen.p, sval, a->rec.p, a->csum.p, a->sms, st);
-      launch_adj_nodes(a->nx, a->ny, sg, a->csum.p, g_u, g_v, st);
+  const uint32_t cw = (uint32_t)(a->nx - 1), ch = (uint32_t)(a->ny - 1);
+  const int kbm = key_bits_for(2u * cells);
+  int r;
+  // Gather form first (microbes sorted by the cell where each step starts, records gathered from
+  // the 3 x 3 cells around every cell); if a stage left that neighbourhood anywhere, the whole
+  // sweep is redone with the records themselves sorted by cell.
+  for (int form = 0; form < 2; ++form) {
+    const bool gather = form == 0;
+    ACK(cudaMemsetAsync(g_u, 0, fe * sizeof(float), st));
+    ACK(cudaMemsetAsync(g_v, 0, fe * sizeof(float), st));
+    ACK(cudaMemsetAsync(a->err_d, 0, sizeof(uint32_t), st));
+    if (gather) {  // target lists start empty, stamps at 0 (step m stamps m + 1)
+      ACK(cudaMemsetAsync(a->mark.p, 0, sizeof(uint32_t) * (cells + 1), st));
+      ACK(cudaMemsetAsync(a->tcnt.p, 0, sizeof(uint32_t) * a->n_steps, st));
+    } else {  // the record form needs every segment bound at zero
+      ACK(cudaMemsetAsync(a->cst.p, 0, sizeof(uint32_t) * (4 * (size_t)cells + 1), st));
+      ACK(cudaMemsetAsync(a->cen.p, 0, sizeof(uint32_t) * (4 * (size_t)cells + 1), st));
     }
+    if (N) launch_adj_seed(a->prec, N, g_lon, g_lat, a->lx.p, a->ly.p, st);
+    const AdjSortBufs sb{gather ? a->mkey.p : a->key.p, a->k1.p, a->k2.p, a->v1.p, a->v2.p,
+                         a->hist.p, a->hscan.p, a->bsum.p};
+    for (int s = a->n_ck - 1; s >= 0 && N; --s) {
+      const int m0 = s * a->K, m1 = std::min(m0 + a->K, a->n_steps);
+      ACK(cudaMemcpyAsync(a->x.p, a->ck_x.p + es * s * N, es * N, cudaMemcpyDeviceToDevice, st));
+      ACK(cudaMemcpyAsync(a->y.p, a->ck_y.p + es * s * N, es * N, cudaMemcpyDeviceToDevice, st));
+      ACK(cudaMemcpyAsync(a->st.p, a->ck_st.p + (size_t)s * N, N, cudaMemcpyDeviceToDevice, st));
+      launch_adj_forward(a->fv, a->prec, a->table.p, m0, m1, a->dt, N, a->x.p, a->y.p, a->st.p, a->seg_x.p,
+                         a->seg_y.p, a->seg_st.p, a->err_d, st);
+      for (int m = m1 - 1; m >= m0; --m) {
+        const size_t o = (size_t)(m - m0) * N;
+        const AdjStep& sg = a->table_h[m];
+        launch_adj_step(a->fv, a->prec, sg, a->dt, N, a->seg_x.p + es * o, a->seg_y.p + es * o, a->seg_st.p + o,
+                        a->lx.p, a->ly.p, a->rec.p, a->key.p, sent, gather ? a->mkey.p : nullptr, a->mcode.p,
+                        2u * cells, a->err_d, st);
+        const uint32_t *skey, *sval;
+        const uint32_t stamp = (uint32_t)m + 1u;
+        if (gather) {
+          ACK(cudaMemsetAsync(a->cen.p, 0, sizeof(uint32_t) * 2 * cells, st));
+          adj_sort(sb, N, kbm, st, &skey, &sval);
+          launch_adj_cells(skey, sval, N, cw, ch, a->mcode.p, a->scode.p, a->cst.p, a->cen.p, a->mark.p, stamp,
+                           a->tlist.p, a->tcnt.p + m, st);
+          launch_adj_gather(cw, ch, a->tcnt.p + m, a->tlist.p, a->cst.p, a->cen.p, a->scode.p, sval, a->rec.p,
+                            a->csum.p, a->sms, st);
+        } else {
+          adj_sort(sb, M, kb, st, &skey, &sval);
+          launch_adj_bounds(skey, M, sent, a->cst.p, a->cen.p, st);
+          launch_adj_reduce(cells, a->cst.p, a->cen.p, sval, a->rec.p, a->csum.p, a->sms, st);
+        }
+        launch_adj_nodes(a->nx, a->ny, sg, a->csum.p, gather ? a->mark.p : nullptr, stamp, g_u, g_v, st);
+      }
+    }
+    ACK(cudaGetLastError());
+    uint32_t err = 0;
+    if ((r = read_err(a, st, &err))) return r;
+    if (!(gather && (err & ADJ_WIDE))) break;
   }
   if (N) launch_adj_unseed(a->prec, N, a->lx.p, a->ly.p, g_lon0, g_lat0, st);
   ACK(cudaGetLastError());

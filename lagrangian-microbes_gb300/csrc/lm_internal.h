@@ -294,9 +294,21 @@ void launch_adj_unseed(int prec, uint32_t n, const void* lx, const void* ly, flo
 void launch_adj_forward(const FieldView& f, int prec, const AdjStep* table, int m0, int m1, double dt, uint32_t n,
                         void* x, void* y, uint8_t* status, void* rec_x, void* rec_y, uint8_t* rec_st, uint32_t* err,
                         cudaStream_t st);
+// mkey (or nullptr): gather form of the reduction. Per microbe, in mcode, 4 bits a stage: the slot
+// (dj + 1) * 3 + (di + 1) of the stage's cell around the cell b where the step starts, and in mkey
+// 2b + (1 when a stage leaves b), msent when frozen; a stage outside those 3 x 3 cells sets
+// ADJ_WIDE. Without mkey the step writes the four record keys (cell * 4 + stage time, or `sent`).
+constexpr uint32_t ADJ_WIDE = 1u << 8;
 void launch_adj_step(const FieldView& f, int prec, const AdjStep& s, double dt, uint32_t n, const void* x,
                      const void* y, const uint8_t* status, void* lx, void* ly, float4* rec, uint32_t* key, uint32_t sent,
-                     cudaStream_t st);
+                     uint32_t* mkey, uint32_t* mcode, uint32_t msent, uint32_t* err, cudaStream_t st);
+// After the sort of mkey: cell bounds, stage codes in sorted order, target cells listed once a step.
+void launch_adj_cells(const uint32_t* skey, const uint32_t* sval, uint32_t m, uint32_t cw, uint32_t ch,
+                      const uint32_t* mcode, uint32_t* scode, uint32_t* cst, uint32_t* cen, uint32_t* mark,
+                      uint32_t stamp, uint32_t* tlist, uint32_t* tcnt, cudaStream_t st);
+void launch_adj_gather(uint32_t cw, uint32_t ch, const uint32_t* tcnt, const uint32_t* tlist, const uint32_t* cst,
+                       const uint32_t* cen, const uint32_t* scode, const uint32_t* sval, const float4* rec,
+                       float* csum, int sms, cudaStream_t st);
 void launch_adj_signature(const FieldView& f, int prec, const AdjStep* table, int n_steps, double dt, uint32_t n,
                           const void* x, const void* y, const uint8_t* status, unsigned long long* sig,
                           cudaStream_t st);
@@ -308,7 +320,9 @@ void launch_adj_bounds(const uint32_t* skey, uint32_t m, uint32_t sent, uint32_t
                        cudaStream_t st);
 void launch_adj_reduce(uint32_t ncells, uint32_t* cst, uint32_t* cen, const uint32_t* sval, const float4* rec,
                        float* csum, int sms, cudaStream_t st);
-void launch_adj_nodes(int nx, int ny, const AdjStep& s, const float* csum, float* gu, float* gv, cudaStream_t st);
+// mark (or nullptr): only cells with mark[c] == stamp hold sums (the gather form's target list).
+void launch_adj_nodes(int nx, int ny, const AdjStep& s, const float* csum, const uint32_t* mark, uint32_t stamp,
+                      float* gu, float* gv, cudaStream_t st);
 
 // Field geometry from uniform axes (shared by lm_field_upload_batch and the adjoint tape).
 bool uniform_axis(const double* a, int n, double* d);

@@ -224,3 +224,23 @@ def test_adjoint_f64_trajectories_track_the_fp64_scheme(lm, orc, small_field):
     again = _gpu_grads(f, lon, lat, tlon, tlat, t0, dt, n_steps, 5, precision="f64")
     for a, b in zip(again[3], g):
         np.testing.assert_array_equal(a, b)
+
+
+def test_adjoint_steps_longer_than_a_cell_fall_back_to_the_record_form(lm, orc):
+    """Stages that leave the 3 x 3 cells around a step's start (a fine grid, fast flow) switch the
+    backward to sorting the stage records themselves; the gradient still matches the FP64 scheme
+    and is deterministic."""
+    f = lm.synthetic_psi_field(199.0, 203.0, 24.0, 28.0, 0.02, n_frames=8, frame_seconds=3600.0, rms_speed=2.0,
+                               seed=3)
+    lon, lat, tlon, tlat = _case(f, 2000, 9, box=(200.5, 201.5, 25.5, 26.5))
+    t0, dt, n_steps = float(f.times[0]), 3600.0, 6
+    _, _, _, g, sig = _gpu_grads(f, lon, lat, tlon, tlat, t0, dt, n_steps, 4)
+    same = sig == _fp64_signature(orc, f, lon, lat, t0, dt, n_steps)
+    assert same.mean() >= 0.9
+    _, _, _, gs, _ = _gpu_grads(f, lon, lat, tlon, tlat, t0, dt, n_steps, 4, weight=same)
+    _, g64 = _fp64_grads(f, lon, lat, tlon, tlat, t0, dt, n_steps, weight=same)
+    errs = [_rel(a, b) for a, b in zip(gs, g64)]
+    assert max(errs) < 1e-4, errs
+    again = _gpu_grads(f, lon, lat, tlon, tlat, t0, dt, n_steps, 3)
+    for a, b in zip(again[3], g):
+        np.testing.assert_array_equal(a, b)
