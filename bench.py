@@ -254,13 +254,15 @@ def run_gb300(args):
     if not args.no_e2e:
         e2e = run_e2e(fld, lons, lats, species, K, spg, local, stream)
 
-    batched = adjoint = stress = None
+    batched = adjoint = stress = histogram = None
     if rank == 0 and not args.no_batched:
         batched = run_batched(local, stream)
     if rank == 0 and not args.no_stress:
         stress = run_stress(fld, local)
     if rank == 0 and not args.no_adjoint:
         adjoint = run_adjoint(fld, local)
+    if rank == 0 and not args.no_histogram:
+        histogram = run_histogram(lons, lats, species)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -282,6 +284,7 @@ def run_gb300(args):
                       "graph_speedup": value / world / plain_value},
             "roofline": roofline, "whole_step": whole, "kernels": kernels,
             "e2e": e2e, "cpu_baseline": cpu, "clocks": clk, "batched": batched, "adjoint": adjoint, "stress": stress,
+            "distance_histogram": histogram,
             "gpu_launches": int(round(launches_per_step * K)),
             "max_rounds": stats["max_rounds"],
             "mean_rounds": stats["rounds_total"] / max(stats["steps_total"], 1),
@@ -521,6 +524,43 @@ def run_stress(fld, local: int):
                       "pairs_per_s": pairs / (per["k_count_pairs"] * 1e-6) if per.get("k_count_pairs") else None}}
 
 
+def run_histogram(lons, lats, species):
+    """Pairwise distance histograms per species of the 490k lattice (sandbox/pairwise_distance_
+    histogram_distributed.jl:133-147, 70 bins) through the public API from host arrays; the oracle
+    (float64, all host threads) on a bounded sample of the same pairs beside it."""
+    import numpy as np
+
+    from lagrangian_microbes_gb300 import _lib
+    from lagrangian_microbes_gb300.pairwise_distance_histogram import species_distance_histograms
+    ctx = _lib.Context(0)
+    sizes = [int(np.count_nonzero(species == k)) for k in (1, 2, 3)]
+    pairs = sum(m * (m - 1) // 2 for m in sizes)
+    species_distance_histograms(lons, lats, species, 70, ctx=ctx)  # warm-up
+    t0 = time.perf_counter()
+    got = species_distance_histograms(lons, lats, species, 70, ctx=ctx)
+    wall = time.perf_counter() - t0
+    ctx.close()
+    assert sum(int(c.sum()) + o for c, o in got.values()) == pairs
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    sel = np.flatnonzero(species == 1)[:20_000]
+    la, lo = np.asarray(lats, np.float32)[sel], np.asarray(lons, np.float32)[sel]
+    oracle.distance_histogram(la[:2000], lo[:2000], 70)  # build, threads up
+    t0 = time.perf_counter()
+    oracle.distance_histogram(la, lo, 70)
+    cpu_wall = time.perf_counter() - t0
+    cpu_pairs = sel.size * (sel.size - 1) // 2
+    return {"workload": "one histogram per species of the 490k lattice (i.i.d. species), 70 bins of "
+                        "round(10 log10(max(1 m, d))), float32 haversine",
+            "pairs": pairs, "ms": 1e3 * wall, "value": pairs / wall,
+            "unit": "pairs/s (public API, host arrays in and out)",
+            "cpu_baseline": {"value": cpu_pairs / cpu_wall, "unit": "pairs/s", "cores": cpu_threads(), "kind": "port",
+                             "sample": f"all pairs of the first {sel.size} rock microbes (float64 oracle)"},
+            "reference_published": {"pairs_per_s_1_process": 5e7 / 4.035, "pairs_per_s_60_processes": 5e7 / 0.268,
+                                    "source": "timing comment of sandbox/pairwise_distance_histogram_distributed.jl "
+                                              "(10,000 random points)"}}
+
+
 def cpu_threads():
     try:
         return len(os.sched_getaffinity(0))
@@ -597,6 +637,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the 256-ensemble batching measurement")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint (differentiation) timing")
     ap.add_argument("--no-stress", action="store_true", help="skip the 16M clustered count-only measurement")
+    ap.add_argument("--no-histogram", action="store_true", help="skip the pairwise distance histogram measurement")
     ap.add_argument("--profile-run", action="store_true", help="only the warm-up and timed graph launches")
     ap.add_argument("--traffic-json", default=os.path.join(REPO, "profiles", "traffic.json"))
     args = ap.parse_args()

@@ -258,6 +258,19 @@ int lm_adjoint_final_positions(lm_adjoint* adj, double* lon, double* lat);
  * sampled the same pieces. Used to compare gradients with an FP64 run cell path by cell path. */
 int lm_adjoint_cell_signature(lm_adjoint* adj, unsigned long long* sig);
 
+/* ---- pairwise distance histogram ----
+ * Replaces pairwise_distance_histogram_parallel / pairwise_distance_histogram_1point
+ * (sandbox/pairwise_distance_histogram_distributed.jl:56-76) and pairwise_dist_gpu
+ * (sandbox/pairwise_distance_histogram_gpu.jl:45-77): for every unordered pair of points inside
+ * each segment [seg[s], seg[s+1]) (the reference: one segment per species), the float32 haversine
+ * distance d of haversine_distance32 (:35-46, latitude first, radius_m as `radius`) is counted in
+ * bin round-half-even(10 log10(max(1, d))); bins >= `bins` are counted in the last column.
+ * lat, lon: host float32 [n] (finite, else LM_ERR_NAN); seg: host int64 [n_seg + 1] from 0 to n
+ * (NULL with n_seg = 1: one segment); counts: host uint64 [n_seg][bins + 1], overwritten.
+ * 1 <= bins <= 256. */
+int lm_distance_histogram(lm_ctx* ctx, const float* lat, const float* lon, int64_t n, const int64_t* seg, int n_seg,
+                          int bins, double radius_m, uint64_t* counts);
+
 #ifdef __cplusplus
 }
 #endif

@@ -7,6 +7,7 @@ Reference-facing modules (same names and call surface as ali-ramadhan/lagrangian
 Device-resident engine:
   engine                 Simulation (fused steps, CUDA graphs), PairQuery (cKDTree.query_pairs)
   fields                 VelocityField, synthetic_psi_field
+  pairwise_distance_histogram   species / all-pairs great-circle distance histograms
 All compute runs in liblmgb300.so (CUDA, sm_103a) through the C-ABI of include/lm_api.h.
 """
 

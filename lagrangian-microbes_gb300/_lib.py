@@ -135,6 +135,7 @@ SIGNATURES = {
     "lm_adjoint_backward": [P, P, P, P, P, P, P],
     "lm_adjoint_cell_signature": [P, P],
     "lm_adjoint_final_positions": [P, P, P],
+    "lm_distance_histogram": [P, P, P, I64, P, I32, I32, F64, P],
 }
 
 

@@ -606,3 +606,58 @@ int64_t orc_run(const orc_field* f, int64_t n, float* lon, float* lat, uint8_t* 
   }
   return pairs;
 }
+
+/* ---- pairwise distance histogram (sandbox/pairwise_distance_histogram_distributed.jl) ----
+ * haversine_distance32 (:35-46) evaluated in float64 on the float32 inputs:
+ *   a = sin(pi dlat / 360)^2 + cos(pi lat1 / 180) cos(pi lat2 / 180) sin(pi dlon / 360)^2,
+ *   d = radius * 2 asin(min(1, sqrt(a))),
+ * and the bin of pairwise_distance_histogram_1point (:56-66): round(10 log10(max(1, d))). */
+double orc_haversine(double lat1, double lon1, double lat2, double lon2, double radius) {
+  const double c1 = cos(M_PI * (lat1 / 180.0)), c2 = cos(M_PI * (lat2 / 180.0));
+  const double d1 = sin(M_PI * ((lat2 - lat1) / 360.0)), d2 = sin(M_PI * ((lon2 - lon1) / 360.0));
+  const double a = d1 * d1 + d2 * d2 * c1 * c2;
+  return radius * (2.0 * asin(fmin(1.0, sqrt(a))));
+}
+
+/* All pairs i < j: x = 10 log10(max(1, d)). A pair whose x lies within `delta` of a bin boundary
+ * k + 1/2 is ambiguous between bins k and k + 1 (float32 rounding may put it on either side) and
+ * counted in amb[min(k, bins)]; every other pair in def[min(round(x), bins)] (bins = overflow).
+ * def, amb: uint64 [bins + 1], overwritten. */
+void orc_distance_histogram(int64_t n, const float* lat, const float* lon, int bins, double radius, double delta,
+                            int n_threads, uint64_t* def, uint64_t* amb) {
+  const int nb = bins + 1;
+  memset(def, 0, sizeof(uint64_t) * nb);
+  memset(amb, 0, sizeof(uint64_t) * nb);
+#ifdef _OPENMP
+  if (n_threads > 0) omp_set_num_threads(n_threads);
+#else
+  (void)n_threads;
+#endif
+#pragma omp parallel
+  {
+    uint64_t* hd = (uint64_t*)calloc((size_t)nb, sizeof(uint64_t));
+    uint64_t* ha = (uint64_t*)calloc((size_t)nb, sizeof(uint64_t));
+#pragma omp for schedule(dynamic, 64)
+    for (int64_t i = 0; i < n; ++i) {
+      for (int64_t j = i + 1; j < n; ++j) {
+        const double d = orc_haversine(lat[i], lon[i], lat[j], lon[j], radius);
+        const double x = 10.0 * log10(fmax(1.0, d));
+        const double k0 = floor(x);
+        const int lo = k0 < bins ? (int)k0 : bins, hi = k0 + 1 < bins ? (int)k0 + 1 : bins;
+        if (lo != hi && fabs(x - (k0 + 0.5)) < delta) {
+          ha[lo]++;
+        } else {
+          const double kr = nearbyint(x);
+          hd[kr < bins ? (int)kr : bins]++;
+        }
+      }
+    }
+#pragma omp critical
+    for (int k = 0; k < nb; ++k) {
+      def[k] += hd[k];
+      amb[k] += ha[k];
+    }
+    free(hd);
+    free(ha);
+  }
+}

@@ -53,6 +53,10 @@ int64_t orc_run(const orc_field* f, int64_t n, float* lon, float* lat, uint8_t* 
                 double dt, int n_steps, uint32_t step0, double r, int norm, uint64_t t_rs, uint64_t t_pr,
                 uint64_t t_sp, uint64_t seed, int n_threads);
 
+double orc_haversine(double lat1, double lon1, double lat2, double lon2, double radius);
+void orc_distance_histogram(int64_t n, const float* lat, const float* lon, int bins, double radius, double delta,
+                            int n_threads, uint64_t* def, uint64_t* amb);
+
 #ifdef __cplusplus
 }
 #endif

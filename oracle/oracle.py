@@ -72,6 +72,8 @@ def lib():
             "orc_pair_prio": (U64, [U32, U32, U32, U64]),
             "orc_interact_step": (I64, [I64, P, P, P, F64, I, U64, U64, U64, U64, U32, I]),
             "orc_run": (I64, [P, I64, P, P, P, P, F64, F64, I, U32, F64, I, U64, U64, U64, U64, I]),
+            "orc_haversine": (F64, [F64, F64, F64, F64, F64]),
+            "orc_distance_histogram": (None, [I64, P, P, I, F64, F64, I, P, P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -284,3 +286,36 @@ def great_circle_m(lon1, lat1, lon2, lat2, radius_km: float = 6371.228):
     dl = np.deg2rad(np.asarray(lon2, np.float64) - np.asarray(lon1, np.float64))
     a = np.sin(dphi / 2) ** 2 + np.cos(p1) * np.cos(p2) * np.sin(dl / 2) ** 2
     return 2 * radius_km * 1e3 * np.arcsin(np.sqrt(np.minimum(a, 1.0)))
+
+
+R_EARTH = 6371.228e3  # the reference's R64 / R32 (sandbox/pairwise_distance_histogram_distributed.jl:94)
+
+
+def haversine(lat1, lon1, lat2, lon2, radius: float = R_EARTH) -> float:
+    """haversine_distance32's formula in float64 (metres)."""
+    return float(lib().orc_haversine(float(lat1), float(lon1), float(lat2), float(lon2), float(radius)))
+
+
+def distance_histogram(lats, lons, bins: int, radius: float = R_EARTH, delta: float = 1e-4, n_threads: int = 0):
+    """All-pairs histogram of round(10 log10(max(1, d))): (definite[bins + 1], ambiguous[bins + 1]).
+
+    ambiguous[k] counts pairs within `delta` (in units of 10 log10 d) of the boundary between bins
+    k and k + 1, which float32 arithmetic may put on either side; the last column is the overflow."""
+    lats = np.ascontiguousarray(lats, dtype=np.float32)
+    lons = np.ascontiguousarray(lons, dtype=np.float32)
+    d = np.zeros(bins + 1, np.uint64)
+    a = np.zeros(bins + 1, np.uint64)
+    lib().orc_distance_histogram(lats.size, _p(lats), _p(lons), int(bins), float(radius), float(delta), int(n_threads),
+                                 _p(d), _p(a))
+    return d.astype(np.int64), a.astype(np.int64)
+
+
+def histogram_consistent(counts, definite, ambiguous) -> bool:
+    """True when counts[bins + 1] is definite plus each ambiguous pair on one side of its boundary:
+    for every k, sum(counts[:k+1]) lies between sum(definite[:k+1]) + sum(ambiguous[:k]) and
+    sum(definite[:k+1]) + sum(ambiguous[:k+1])."""
+    c = np.cumsum(np.asarray(counts, np.int64))
+    d = np.cumsum(np.asarray(definite, np.int64))
+    a = np.cumsum(np.asarray(ambiguous, np.int64))
+    a_before = np.concatenate([[0], a[:-1]])
+    return bool(np.all(c >= d + a_before) and np.all(c <= d + a) and c[-1] == d[-1] + a[-1])
