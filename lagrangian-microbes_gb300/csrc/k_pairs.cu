@@ -371,27 +371,80 @@ __device__ void sort_segment(unsigned long long* __restrict__ pr, uint32_t* __re
 
 // Long lists (more than SLAB neighbours): one warp per vertex. The warp reserves the overflow space
 // of 32 vertices at a time (one atomic per batch), gathers each vertex's neighbours with ballots
-// (lanes test 32 candidates of a row run at once), and sorts the list in shared memory with a
-// bitonic network over (priority, partner) pairs; lists longer than LONG_SMEM_MAX fall back to a
-// sort in global memory by one lane. Only the sorted partners are kept (the priorities were
-// needed for the order only).
-constexpr int LONG_WARPS = 8;
-constexpr uint32_t LONG_SMEM_MAX = 256;
+// (lanes test 32 candidates of a row run at once) into shared memory, and orders the list there by
+// a bucket sort: the priorities are uniform 64-bit hashes, so 256 buckets on their top 8 bits
+// (descending) hold about d / 256 entries each, and an insertion sort inside each bucket by the
+// exact order (priority descending, partner's local id ascending) finishes it. Lists longer than
+// LONG_SMEM_MAX fall back to a sort in global memory by one lane. Only the sorted partners are
+// kept (the priorities were needed for the order only).
+constexpr int LONG_WARPS = 4;
+constexpr uint32_t LONG_SMEM_MAX = 512;
+constexpr uint32_t LONG_BUCKETS = 256;
 
-struct LongEntry {
-  unsigned long long p;  // pair priority
-  uint32_t id;           // partner's local id (ties)
-  uint32_t t;            // partner's cell-order index
+struct LongSmem {
+  unsigned long long p[LONG_SMEM_MAX];  // pair priority of entry i (gather order)
+  uint32_t t[LONG_SMEM_MAX];            // partner's cell-order index
+  uint16_t ord[LONG_SMEM_MAX];          // entries in list order
+  uint32_t start[LONG_BUCKETS], cur[LONG_BUCKETS];
 };
 
-__device__ __forceinline__ bool entry_before(const LongEntry& x, const LongEntry& y) { return before(x.p, x.id, y.p, y.id); }
+// Does entry x come before entry y? Ties of the 64-bit priority (rare) go by the partner's local id.
+__device__ __forceinline__ bool long_before(const Bufs& b, const LongSmem& sh, uint32_t base, uint32_t x, uint32_t y) {
+  const unsigned long long px = sh.p[x], py = sh.p[y];
+  if (px != py) return px > py;
+  return b.sid[sh.t[x]] - base < b.sid[sh.t[y]] - base;
+}
+
+// The bucket sort of entries [0, d) of sh into sh.ord (one warp).
+__device__ __forceinline__ void long_sort(const Bufs& b, LongSmem& sh, uint32_t base, uint32_t d, uint32_t lane) {
+  for (uint32_t i = lane; i < LONG_BUCKETS; i += 32) sh.cur[i] = 0;
+  __syncwarp();
+  for (uint32_t i = lane; i < d; i += 32) atomicAdd(&sh.cur[255u - (uint32_t)(sh.p[i] >> 56)], 1u);
+  __syncwarp();
+  // exclusive scan of the bucket counts: lane holds buckets 8 lane .. 8 lane + 7
+  uint32_t c[8], tot = 0;
+#pragma unroll
+  for (int r = 0; r < 8; ++r) {
+    c[r] = sh.cur[8 * lane + r];
+    tot += c[r];
+  }
+  uint32_t incl = tot;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= (uint32_t)o) incl += y;
+  }
+  uint32_t run = incl - tot;
+#pragma unroll
+  for (int r = 0; r < 8; ++r) {
+    sh.start[8 * lane + r] = run;
+    sh.cur[8 * lane + r] = run;
+    run += c[r];
+  }
+  __syncwarp();
+  for (uint32_t i = lane; i < d; i += 32)
+    sh.ord[atomicAdd(&sh.cur[255u - (uint32_t)(sh.p[i] >> 56)], 1u)] = (uint16_t)i;
+  __syncwarp();
+  for (uint32_t k = lane; k < LONG_BUCKETS; k += 32) {
+    const uint32_t lo = sh.start[k], hi = sh.cur[k];
+    for (uint32_t x = lo + 1; x < hi; ++x) {
+      const uint16_t e = sh.ord[x];
+      uint32_t y = x;
+      while (y > lo && long_before(b, sh, base, e, sh.ord[y - 1])) {
+        sh.ord[y] = sh.ord[y - 1];
+        --y;
+      }
+      sh.ord[y] = e;
+    }
+  }
+  __syncwarp();
+}
 
 __global__ void __launch_bounds__(LONG_WARPS * 32) k_sweep_long(Bufs b, PairParams pp, StepArgs a, Ctrl* ctrl) {
   pdl_wait();
   if (ctrl->halt) return;
-  __shared__ LongEntry sh_all[LONG_WARPS][LONG_SMEM_MAX];
+  __shared__ LongSmem sh_all[LONG_WARPS];
   const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
-  LongEntry* sh = sh_all[w];
+  LongSmem& sh = sh_all[w];
   const uint32_t n_long = ctrl->n_long;
   const uint32_t step = a.use_ctrl_step ? ctrl->step : a.step0;
   const unsigned long long cap = ctrl->ovf_cap;
@@ -459,7 +512,8 @@ __global__ void __launch_bounds__(LONG_WARPS * 32) k_sweep_long(Bufs b, PairPara
               const uint32_t lb = b.sid[t] - v.base;
               const unsigned long long p = pair_prio(min(la, lb), max(la, lb), step, info.seed_lo, info.seed_hi);
               if (in_smem) {
-                sh[pos] = LongEntry{p, lb, t};
+                sh.p[pos] = p;
+                sh.t[pos] = t;
               } else {
                 b.ovf[o + pos] = t;
                 b.oprio[o + pos] = p;
@@ -472,28 +526,10 @@ __global__ void __launch_bounds__(LONG_WARPS * 32) k_sweep_long(Bufs b, PairPara
       }
       uint32_t first;
       if (in_smem) {
-        uint32_t n2 = 32;
-        while (n2 < d) n2 <<= 1;
-        for (uint32_t i = d + lane; i < n2; i += 32) sh[i] = LongEntry{0ull, NONE, NONE};  // sort last
         __syncwarp();
-        for (uint32_t kk = 2; kk <= n2; kk <<= 1) {
-          for (uint32_t j = kk >> 1; j > 0; j >>= 1) {
-            for (uint32_t i = lane; i < n2; i += 32) {
-              const uint32_t l = i ^ j;
-              if (l > i) {
-                const LongEntry x = sh[i], y = sh[l];
-                const bool up = (i & kk) == 0;
-                if (up ? entry_before(y, x) : entry_before(x, y)) {
-                  sh[i] = y;
-                  sh[l] = x;
-                }
-              }
-            }
-            __syncwarp();
-          }
-        }
-        for (uint32_t i = lane; i < d; i += 32) b.ovf[o + i] = sh[i].t;
-        first = sh[0].t;
+        long_sort(b, sh, v.base, d, lane);
+        for (uint32_t i = lane; i < d; i += 32) b.ovf[o + i] = sh.t[sh.ord[i]];
+        first = sh.t[sh.ord[0]];
         __syncwarp();  // the next vertex reuses the shared list
       } else {
         __syncwarp();
@@ -516,7 +552,7 @@ __global__ void __launch_bounds__(LONG_WARPS * 32) k_sweep_long(Bufs b, PairPara
 
 void launch_sweep_long(const Bufs& b, const PairParams& pp, const StepArgs& a, Ctrl* ctrl, int sms,
                        cudaStream_t st) {
-  launch_dep(k_sweep_long, dim3(sms * 4), dim3(LONG_WARPS * 32), st, b, pp, a, ctrl);
+  launch_dep(k_sweep_long, dim3(sms * 6), dim3(LONG_WARPS * 32), st, b, pp, a, ctrl);  // 6 x 36 KB per SM
 }
 
 }  // namespace lm

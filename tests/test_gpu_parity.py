@@ -139,6 +139,21 @@ def test_gpu_interaction_large_random(engine, orc):
     np.testing.assert_array_equal(got, want)
 
 
+def test_gpu_interaction_dense_lists_match_oracle(engine, orc):
+    # blob A (sigma 0.004 deg): ~2,000-3,000 neighbours per microbe, lists ordered in global memory;
+    # blob B (sigma 0.02 deg): 10 to ~375 neighbours, lists bucket-sorted in shared memory with
+    # several entries per bucket. The species depend on every list's order.
+    rng = np.random.default_rng(31)
+    lon = np.concatenate([200.0 + rng.normal(0, 0.004, 3000), 200.5 + rng.normal(0, 0.02, 3000)]).astype(np.float32)
+    lat = np.concatenate([25.0 + rng.normal(0, 0.004, 3000), 25.5 + rng.normal(0, 0.02, 3000)]).astype(np.float32)
+    sp = rng.integers(1, 4, lon.size).astype(np.int8)
+    probs = (0.6, 0.7, 0.55)
+    got, _, stats = _interact(engine, lon, lat, sp, 0.01, 2, probs, 77, 3, log=False)
+    want, m = orc.interact_step(lon, lat, sp, 0.01, 2, *probs, 77, 3)
+    assert stats["pairs"] == m > 3_000_000
+    np.testing.assert_array_equal(got, want)
+
+
 def test_gpu_interaction_other_species_values_unchanged(engine, orc):
     rng = np.random.default_rng(3)
     n = 2000
