@@ -187,21 +187,22 @@ __device__ __forceinline__ void rps_pair(const Bufs& b, uint32_t vertex, uint32_
   *new_b = a_is_i ? nj : ni;
 }
 
-// Returns false (nothing done) when the step does not fit the tile path.
-__device__ bool rounds_tiled(const Bufs& b, uint32_t step, Ctrl* ctrl, unsigned long long t0) {
-  const uint32_t n_valid = ((volatile uint32_t*)&ctrl->n_valid)[0];
-  const uint32_t vpt = (n_valid + gridDim.x * RD_THREADS - 1) / (gridDim.x * RD_THREADS);
-  if (b.plog || vpt > (uint32_t)TL_VPT) return false;  // grid-uniform decision
+// The pairs among cell-order vertices [g_lo, g_hi) (a group of whole ensembles, so no pair leaves
+// it), at most TL_VMAX per block: each block owns an equal share of whole 256-vertex columns.
+__device__ void tl_group(const Bufs& b, uint32_t step, Ctrl* ctrl, unsigned long long t0, uint32_t g_lo,
+                         uint32_t g_hi) {
   extern __shared__ unsigned long long tl_raw[];
   TileSmem t;
   t.w = tl_raw;
   t.sid = reinterpret_cast<uint32_t*>(t.w + TL_VMAX);
   t.deg = t.sid + TL_VMAX;
   t.lst = t.deg + TL_VMAX;
+  const uint32_t n_g = g_hi - g_lo;
+  const uint32_t vpt = (n_g + gridDim.x * RD_THREADS - 1) / (gridDim.x * RD_THREADS);
   const uint32_t V = max(vpt, 1u) * RD_THREADS;
-  const uint32_t lo = blockIdx.x * V;
-  const uint32_t hi = min(n_valid, lo + V);
-  const uint32_t nloc = hi > lo ? hi - lo : 0u;
+  const uint32_t lo = min(g_hi, g_lo + blockIdx.x * V);
+  const uint32_t hi = min(g_hi, lo + V);
+  const uint32_t nloc = hi - lo;
   // every load of the set-up is independent: the whole slab row (two 16-byte loads; entries past
   // the degree are never read) and the overflow offset, for all of the thread's vertices at once
 #pragma unroll
@@ -285,6 +286,66 @@ __device__ bool rounds_tiled(const Bufs& b, uint32_t step, Ctrl* ctrl, unsigned 
       atomicOr(&ctrl->err, (uint32_t)ERRB_TIMEOUT);
       break;
     }
+  }
+}
+
+// Groups of whole ensembles (consecutive in cell order) whose vertices fit the blocks' shared
+// memory, run one after another by every block. No barrier separates the groups: pairs never join
+// two ensembles, and a block that is still in group g while another has moved to g + 1 only
+// delays the handoffs of g + 1 that cross into it, whose words it loads from global memory when it
+// gets there (the same rule that covers blocks starting at different times).
+constexpr int TL_GROUPS_MAX = 64;
+
+// Returns false (nothing done) when the step does not fit the tile path (grid-uniform).
+__device__ bool rounds_tiled(const Bufs& b, uint32_t step, Ctrl* ctrl, unsigned long long t0) {
+  const uint32_t n_valid = ((volatile uint32_t*)&ctrl->n_valid)[0];
+  if (b.plog) return false;
+  const uint32_t cap = gridDim.x * TL_VMAX;
+  __shared__ uint32_t gb[TL_GROUPS_MAX + 1];
+  __shared__ int ng;
+  if (n_valid <= cap) {
+    if (threadIdx.x == 0) {
+      gb[0] = 0;
+      gb[1] = n_valid;
+      ng = 1;
+    }
+  } else {
+    // ensemble e holds the vertices [cstart[cell_base_e], cstart[cell_base_e+1]); greedy groups
+    // of whole ensembles, each at most `cap` vertices (none when one ensemble alone is larger)
+    extern __shared__ unsigned long long tl_raw[];
+    uint32_t* es = reinterpret_cast<uint32_t*>(tl_raw);
+    const uint32_t E = b.n_ens;
+    const bool fits = E + 1 <= (uint32_t)(TL_SMEM / sizeof(uint32_t));
+    if (fits) {
+      for (uint32_t e = threadIdx.x; e < E; e += blockDim.x) es[e] = b.cstart[b.grids[e].cell_base];
+      if (threadIdx.x == 0) es[E] = n_valid;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      bool ok = fits;
+      int g = 0;  // the open group starts at gb[g]
+      if (ok) gb[0] = es[0];
+      for (uint32_t e = 1; e <= E && ok; ++e) {
+        if (es[e] - gb[g] <= cap) continue;  // ensemble e - 1 fits the open group
+        if (es[e - 1] != gb[g]) {            // close the group before ensemble e - 1
+          if (g + 1 >= TL_GROUPS_MAX) {
+            ok = false;
+            break;
+          }
+          gb[++g] = es[e - 1];
+        }
+        ok = es[e] - gb[g] <= cap;  // else ensemble e - 1 alone is larger than the blocks hold
+      }
+      if (ok) gb[g + 1] = n_valid;
+      ng = ok ? g + 1 : 0;  // groups [gb[k], gb[k + 1]), k < ng
+    }
+  }
+  __syncthreads();
+  const int groups = ng;
+  if (groups <= 0) return false;
+  for (int g = 0; g < groups; ++g) {
+    tl_group(b, step, ctrl, t0, gb[g], gb[g + 1]);
+    __syncthreads();  // the block's shared lists are reused by the next group
   }
   return true;
 }

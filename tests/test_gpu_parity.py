@@ -349,6 +349,30 @@ def test_gpu_batched_ensembles_equal_single_runs(engine, lm, orc):
     bat.close()
 
 
+def test_gpu_batched_beyond_one_tile_pass_equals_single_runs(engine, lm):
+    # 1.2M microbes in 6 ensembles: more than the blocks' shared memory holds at once (608 x 1024),
+    # so the interaction runs in groups of whole ensembles; one ensemble is dense (long lists)
+    fld = lm.synthetic_psi_field(195.0, 206.0, 20.0, 31.0, 1.0 / 12.0, n_frames=4, frame_seconds=3600.0, seed=4)
+    rng = np.random.default_rng(17)
+    ens = []
+    for e, (n, side) in enumerate([(250_000, 2.0), (40_000, 0.3), (300_000, 3.0), (260_000, 2.5), (200_000, 2.0),
+                                   (150_000, 1.5)]):
+        x0, y0 = 197.0 + (e % 3) * 2.5, 23.0 + (e // 3) * 3.0
+        ens.append(((x0 + side * rng.random(n)), (y0 + side * rng.random(n)), rng.integers(1, 4, n).astype(np.int8)))
+    p = [0.55, 0.6, 0.65, 0.7, 0.75, 0.8]
+    seeds = [11, 12, 13, 14, 15, 16]
+    bat = engine.EnsembleSimulation([fld] * len(ens), ens, radius=0.01, p_rs=p, p_pr=p, p_sp=p, seeds=seeds)
+    rec = bat.step(0.0, 3600.0, 2, record=True)
+    sp_e = bat.split(rec["species"])
+    assert bat.stats()["pairs"] > 1_000_000
+    for e, (lons, lats, sp0) in enumerate(ens):
+        one = engine.Simulation(fld, lons, lats, sp0, radius=0.01, p_rs=p[e], p_pr=p[e], p_sp=p[e], seed=seeds[e])
+        r1 = one.step(0.0, 3600.0, 2, record=True)
+        np.testing.assert_array_equal(sp_e[e], r1["species"], err_msg=f"ensemble {e}")
+        one.close()
+    bat.close()
+
+
 def test_gpu_batched_graph_equals_plain(engine, lm, orc):
     fields, ens, p, seeds = _batched_setup(lm, orc, E=7, seed=4)
     a = engine.EnsembleSimulation(fields, ens, radius=0.01, p_rs=p, p_pr=p, p_sp=p, seeds=seeds)
