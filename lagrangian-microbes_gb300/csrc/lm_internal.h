@@ -201,16 +201,18 @@ struct Bufs {
 };
 
 // ---- programmatic dependent launch ----
-// Per-step kernels start with pdl_wait() and are launched with launch_dep(): the next kernel's
-// launch and block setup then overlap the tail of the previous one, and griddepcontrol.wait holds
-// its threads until the previous grid has completed and its memory is visible. A kernel launched
-// without the attribute passes the wait at once. The cooperative interaction kernel is launched
-// without it (its blocks must all be resident together), and so is everything captured into a
-// CUDA graph: graphs already remove the launch overhead, and there the attribute measured neutral
-// to slightly slower.
+// Per-step kernels start with pdl_wait() and are launched with launch_dep() (plain launches and
+// captured graphs alike). pdl_wait() holds the kernel's threads until the previous grid has
+// completed and its memory is visible (griddepcontrol.wait), then lets the next kernel of the
+// stream launch (griddepcontrol.launch_dependents): once every block of this grid has started, the
+// next grid's blocks are placed on the SMs as they free up and wait there, so the launch and ramp
+// of each step kernel overlap the tail of the one before. A kernel launched without the attribute
+// passes the wait at once. The cooperative interaction kernel is launched without it (its blocks
+// must all be resident together).
 __device__ __forceinline__ void pdl_wait() {
 #if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 900
   asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 #endif
 }
 bool pdl_enabled();  // off when the environment sets LM_PDL=0
@@ -226,9 +228,7 @@ inline void launch_dep(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStre
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
-  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-  cudaStreamIsCapturing(st, &cap);
-  cfg.numAttrs = (pdl_enabled() && cap == cudaStreamCaptureStatusNone) ? 1 : 0;
+  cfg.numAttrs = pdl_enabled() ? 1 : 0;
   cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
 }
 
