@@ -126,18 +126,70 @@ void launch_grid(const Bufs& b, const PairParams& pp, Ctrl* ctrl, cudaStream_t s
   launch_dep(k_grid, dim3(1), dim3(GRID_THREADS), st, b, pp, ctrl);
 }
 
-// Cell key of every valid particle + its rank inside the cell (warp-aggregated atomics).
-__global__ void __launch_bounds__(SLOT_BLOCK) k_keys(Bufs b, Ctrl* ctrl, int use_status) {
+// The grid of a context with one ensemble, as k_grid computes it: the cell size grows until the
+// cells fit the capacity; `fits` is false when they still do not (the step halts).
+__device__ __forceinline__ EnsGrid single_grid(const Bufs& b, const PairParams& pp, bool* fits, uint32_t* cells) {
+  float c = pp.cell_factor * (float)pp.r;
+  if (!(c > 0.f)) c = 1e-3f;
+  const float cap = (float)b.cells_cap;
+  float nx, ny, total = 0.f;
+  for (int attempt = 0; attempt < 16; ++attempt) {
+    total = grid_dims(b.ebox, c, &nx, &ny);
+    if (total <= cap * 0.999f) break;
+    c = c * sqrtf(total / cap) * 1.02f;
+  }
+  total = grid_dims(b.ebox, c, &nx, &ny);
+  EnsGrid g;
+  const bool empty = !(dec_f(b.ebox[0]) <= dec_f(b.ebox[2]));
+  g.c = c;
+  g.inv_c = 1.f / c;
+  g.x0 = empty ? 0.f : dec_f(b.ebox[0]) - c;
+  g.y0 = empty ? 0.f : dec_f(b.ebox[1]) - c;
+  g.ncx = (int)nx;
+  g.ncy = (int)ny;
+  g.cell_base = 0;
+  g.pad = 0;
+  *cells = (uint32_t)fminf(total, 4.0e9f);
+  *fits = *cells <= b.cells_cap;
+  return g;
+}
+
+// Cell key of every valid particle + its rank inside the cell (warp-aggregated atomics). With
+// `own_grid` (one ensemble) every block computes the grid itself and block 0 publishes it for the
+// later kernels, in place of a k_grid launch.
+__global__ void __launch_bounds__(SLOT_BLOCK) k_keys(Bufs b, PairParams pp, Ctrl* ctrl, int use_status,
+                                                     int own_grid) {
   pdl_wait();
   if (ctrl->halt) return;
   __shared__ EnsGrid g;
   __shared__ EnsInfo info;
+  __shared__ int fits;
   if (threadIdx.x == 0) {
     const uint32_t e = b.block_ens[blockIdx.x];
-    g = b.grids[e];
     info = b.ens[e];
+    if (own_grid) {
+      bool ok;
+      uint32_t cells;
+      g = single_grid(b, pp, &ok, &cells);
+      fits = ok ? 1 : 0;
+      if (blockIdx.x == 0) {
+        b.grids[0] = g;
+        if (ok) {
+          ctrl->ncells = cells;
+        } else {
+          ctrl->ncells = b.cells_cap;
+          ctrl->halt = 1;
+          ctrl->halt_step = ctrl->step;
+          atomicOr(&ctrl->err, (uint32_t)ERRB_OVERFLOW);
+        }
+      }
+    } else {
+      g = b.grids[e];
+      fits = 1;
+    }
   }
   __syncthreads();
+  if (!fits) return;  // block-uniform
   const uint32_t p = blockIdx.x * SLOT_BLOCK + threadIdx.x;
   bool valid = p < b.nslots;
   float x = 0.f, y = 0.f;
@@ -169,9 +221,13 @@ __global__ void __launch_bounds__(SLOT_BLOCK) k_keys(Bufs b, Ctrl* ctrl, int use
   }
 }
 
-void launch_keys(const Bufs& b, Ctrl* ctrl, bool use_status, cudaStream_t st) {
-  if (b.nslots == 0) return;
-  launch_dep(k_keys, dim3((b.nslots + SLOT_BLOCK - 1) / SLOT_BLOCK), dim3(SLOT_BLOCK), st, b, ctrl, use_status ? 1 : 0);
+void launch_keys(const Bufs& b, const PairParams& pp, Ctrl* ctrl, bool use_status, bool own_grid, cudaStream_t st) {
+  if (b.nslots == 0) {
+    if (own_grid) launch_grid(b, pp, ctrl, st);  // the grid and cell count are still needed
+    return;
+  }
+  launch_dep(k_keys, dim3((b.nslots + SLOT_BLOCK - 1) / SLOT_BLOCK), dim3(SLOT_BLOCK), st, b, pp, ctrl,
+             use_status ? 1 : 0, own_grid ? 1 : 0);
 }
 
 // Exclusive scan of the cell counts in two launches over SCAN_BLOCKS fixed chunks:

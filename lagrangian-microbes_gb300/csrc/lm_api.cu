@@ -457,8 +457,9 @@ cudaError_t enqueue_interaction(lm_ctx* c, const StepArgs& a, uint32_t flags, bo
   cudaStream_t st = c->st;
   const Bufs b = bufs(c, (flags & LM_STEP_LOG_PAIRS) != 0);
   if (positions_only) PROF(c, P_BBOX, launch_bbox(b, c->ctrl, use_status, st));
-  PROF(c, P_GRID, launch_grid(b, c->pp, c->ctrl, st));
-  PROF(c, P_KEYS, launch_keys(b, c->ctrl, use_status, st));
+  const bool own_grid = c->n_ens == 1;  // one ensemble: k_keys derives the grid itself
+  if (!own_grid) PROF(c, P_GRID, launch_grid(b, c->pp, c->ctrl, st));
+  PROF(c, P_KEYS, launch_keys(b, c->pp, c->ctrl, use_status, own_grid, st));
   PROF(c, P_CELL_SCAN, launch_cell_scan(b, c->ctrl, st));
   PROF(c, P_SCATTER, launch_scatter(b, c->ctrl, st));
   if (flags & LM_STEP_COUNT_PAIRS) {  // count-only: no lists, no interaction

@@ -243,7 +243,8 @@ void launch_bbox(const Bufs& b, Ctrl* ctrl, bool use_status, cudaStream_t st);
 // K2 binning: per-ensemble grids, counting pass, cell scan, scatter into cell order.
 constexpr int SCAN_BLOCKS = 304;
 void launch_grid(const Bufs& b, const PairParams& pp, Ctrl* ctrl, cudaStream_t st);
-void launch_keys(const Bufs& b, Ctrl* ctrl, bool use_status, cudaStream_t st);
+// own_grid (one ensemble): k_keys computes the grid itself (no launch_grid before it).
+void launch_keys(const Bufs& b, const PairParams& pp, Ctrl* ctrl, bool use_status, bool own_grid, cudaStream_t st);
 void launch_cell_scan(const Bufs& b, Ctrl* ctrl, cudaStream_t st);
 void launch_scatter(const Bufs& b, Ctrl* ctrl, cudaStream_t st);
 
