@@ -368,6 +368,13 @@ def run_batched(local: int, stream):
     sim = EnsembleSimulation(fields, ens, radius=RADIUS, p_rs=ps, p_pr=ps, p_sp=ps, seeds=seeds, device=local)
     sim.set_stream(stream.cuda_stream)
     cell_factor, _ = sim.autotune(0.0, DT, 2)
+    # per-kernel time of two plain steps (CUDA events around each launch)
+    sim.upload_ensembles(ens)
+    sim.ctx.profile_enable(True)
+    sim.step(0.0, DT, 2, step0=0)
+    prof = sim.ctx.profile()
+    sim.ctx.profile_enable(False)
+    kernels_ms = {k: ms / 2 for k, (ms, cnt) in prof.items() if cnt}
     sim.capture(0.0, DT, B_STEPS, step0=0)
     sim.run_graph(1, sync=True)  # warm-up: sizes the long neighbour lists for this workload
     reps = 3
@@ -414,7 +421,8 @@ def run_batched(local: int, stream):
             "plain_per_ensemble": {"value": plain_value, "unit": "microbe-steps/s",
                                    "ms_per_sim_step": plain_ms / B_STEPS,
                                    "form": "one context per ensemble, per-step launches, ensembles one after another"},
-            "batched_over_plain": graph_value / plain_value, "field_generation_s": t_gen}
+            "batched_over_plain": graph_value / plain_value, "field_generation_s": t_gen,
+            "kernels_ms_per_step": kernels_ms}
 
 
 def run_adjoint(fld, local: int):
