@@ -20,10 +20,17 @@
 //     copy, so same-bin lanes mostly hit different words) and are added to 64-bit global counts
 //     at segment changes, every DH_FLUSH items and at the end.
 //
-// The kernel is FP32 / special-function bound: per pair about 120 instructions and no memory
-// traffic beyond the tile loads.
+// The kernel is bound by instruction issue (no memory traffic beyond the tile loads), so most
+// pairs take a shorter route to the same bin: the distance from odd polynomials for sin and asin,
+// a reciprocal square root and the hardware log2 (dh_fast), valid for 1.5 m <= d, asin argument
+// <= 0.25 (d <= ~3,200 km) and |dlon| <= 180 degrees. Its 10 log10 d differs from the reference
+// chain's by a few 1e-5 at most; only when it lies farther than DH_MARGIN = 1e-3 from a bin
+// boundary is its rounding taken, otherwise (and outside that range) the reference chain decides,
+// so every bin is the reference chain's. LM_HIST_EXACT=1 in the environment makes every pair take
+// the reference chain (the tests compare the two).
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <vector>
 
 #include "lm_api.h"
@@ -60,6 +67,54 @@ __device__ __forceinline__ int dh_bin(float la1, float lo1, float c1, float la2,
   return (int)rintf(__fmul_rn(10.0f, log10f(fmaxf(1.0f, d))));
 }
 
+constexpr float DH_MARGIN = 1e-3f;
+constexpr float DH_PI_360 = 8.72664625997164788e-3f;  // pi / 360
+constexpr float DH_TEN_LOG10_2 = 3.01029995663981195f;  // 10 log10(2)
+
+// sin x for |x| <= pi / 2: Taylor series to x^11 (truncation below 6e-8 relative there).
+__device__ __forceinline__ float dh_sin(float x) {
+  const float z = x * x;
+  float p = -2.50521083854417188e-8f;  // -1 / 11!
+  p = fmaf(p, z, 2.75573192239858907e-6f);  // 1 / 9!
+  p = fmaf(p, z, -1.98412698412698413e-4f);  // -1 / 7!
+  p = fmaf(p, z, 8.33333333333333333e-3f);   // 1 / 5!
+  p = fmaf(p, z, -1.66666666666666667e-1f);  // -1 / 3!
+  return fmaf(x * z, p, x);
+}
+
+// asin s for 0 <= s <= 0.25: Taylor series to s^11 (truncation below 1e-9 relative there).
+__device__ __forceinline__ float dh_asin(float s) {
+  const float z = s * s;
+  float p = 2.23721590909090909e-2f;  // 63 / 2816
+  p = fmaf(p, z, 3.03819444444444444e-2f);  // 35 / 1152
+  p = fmaf(p, z, 4.46428571428571429e-2f);  // 5 / 112
+  p = fmaf(p, z, 7.5e-2f);                  // 3 / 40
+  p = fmaf(p, z, 1.66666666666666667e-1f);  // 1 / 6
+  return fmaf(s * z, p, s);
+}
+
+// 10 log10 d of the pair by the short route; false when the pair is outside its range.
+__device__ __forceinline__ bool dh_fast(float la1, float lo1, float c1, float la2, float lo2, float c2, float R,
+                                        float* x) {
+  const float dlat = la2 - la1, dlon = lo2 - lo1;
+  const float d1 = dh_sin(dlat * DH_PI_360), d2 = dh_sin(dlon * DH_PI_360);
+  const float a = fmaf(d1, d1, d2 * d2 * c1 * c2);
+  const float s = a * rsqrtf(a);  // NaN for a = 0: the reference chain takes it
+  const float d = 2.0f * R * dh_asin(s);
+  *x = DH_TEN_LOG10_2 * __log2f(d);
+  return fabsf(dlon) <= 180.0f && s <= 0.25f && d >= 1.5f;
+}
+
+__device__ __forceinline__ int dh_pair_bin(float la1, float lo1, float c1, float la2, float lo2, float c2, float R,
+                                           int exact) {
+  float x;
+  if (!exact && dh_fast(la1, lo1, c1, la2, lo2, c2, R, &x)) {
+    const float k = rintf(x);
+    if (fabsf(x - k) < 0.5f - DH_MARGIN) return (int)k;
+  }
+  return dh_bin(la1, lo1, c1, la2, lo2, c2, R);
+}
+
 __device__ void dh_flush(uint32_t* hist, int nb, unsigned long long* out) {
   __syncthreads();
   for (int b = threadIdx.x; b < nb; b += DH_THREADS) {
@@ -78,7 +133,7 @@ __device__ void dh_flush(uint32_t* hist, int nb, unsigned long long* out) {
 __global__ void __launch_bounds__(DH_THREADS) k_dist_hist(const float* __restrict__ lat, const float* __restrict__ lon,
                                                           const float* __restrict__ cs,
                                                           const DhSeg* __restrict__ segs, int n_seg,
-                                                          unsigned long long n_items, int bins, float R,
+                                                          unsigned long long n_items, int bins, float R, int exact,
                                                           unsigned long long* __restrict__ counts) {
   __shared__ float tla[DH_THREADS], tlo[DH_THREADS], tc[DH_THREADS];
   extern __shared__ uint32_t hist[];  // [warp][bin][copy], bin = bins is the overflow
@@ -121,7 +176,7 @@ __global__ void __launch_bounds__(DH_THREADS) k_dist_hist(const float* __restric
       const uint32_t js = (I == (uint32_t)J) ? threadIdx.x + 1 : 0u;  // j > i on the diagonal
 #pragma unroll 4
       for (uint32_t jj = js; jj < jn; ++jj) {
-        const int b = min(dh_bin(la, lo, c, tla[jj], tlo[jj], tc[jj], R), bins);
+        const int b = min(dh_pair_bin(la, lo, c, tla[jj], tlo[jj], tc[jj], R, exact), bins);
         atomicAdd(mine + b * DH_COPIES, 1u);
       }
     }
@@ -215,7 +270,10 @@ extern "C" int lm_distance_histogram(lm_ctx* c, const float* lat, const float* l
       return r;
     const unsigned long long cap = (unsigned long long)std::max(per_sm, 1) * (unsigned long long)std::max(ctx_sms(c), 1);
     const unsigned blocks = (unsigned)std::min(items, cap);
+    const char* ex = std::getenv("LM_HIST_EXACT");
+    const int exact = (ex && ex[0] == '1') ? 1 : 0;
     k_dist_hist<<<blocks, DH_THREADS, smem, st>>>(dlat.p, dlon.p, dcs.p, dseg.p, n_seg, items, bins, (float)radius_m,
+                                                   exact,
                                                    dcnt.p);
     if ((r = dh_cuda(c, cudaGetLastError()))) return r;
     if ((r = dh_cuda(c, cudaMemcpyAsync(counts, dcnt.p, nb * n_seg * sizeof(unsigned long long),

@@ -122,3 +122,20 @@ def test_large_totals_and_shuffle_invariance(pdh):
     sizes = [int((species == k).sum()) for k in (1, 2, 3)]
     for k, m in zip((1, 2, 3), sizes):
         assert got[k][0].sum() + got[k][1] == m * (m - 1) // 2
+
+
+def test_short_route_gives_the_reference_chain_bins(pdh, monkeypatch):
+    """Most pairs take the short route (polynomial sin/asin, hardware log2) unless they lie near a
+    bin boundary or outside its range; the bins must be exactly those of the reference chain for
+    every pair (LM_HIST_EXACT=1 makes every pair take the reference chain)."""
+    rng = np.random.default_rng(16)
+    cases = [_points(rng, 20_000, box=(25.0, 30.0, 200.0, 205.0)),                      # 2e8 pairs, all short
+             (rng.uniform(-89, 89, 6000).astype(np.float32), rng.uniform(-180, 180, 6000).astype(np.float32)),
+             ((30 + 1e-4 * rng.random(3000)).astype(np.float32), (150 + 1e-4 * rng.random(3000)).astype(np.float32))]
+    for lat, lon in cases:  # a 5-degree patch, the whole globe, a sub-10-m cluster (d around 1-15 m)
+        fast = pdh.pairwise_distance_histogram(lat, lon, 80)
+        monkeypatch.setenv("LM_HIST_EXACT", "1")
+        exact = pdh.pairwise_distance_histogram(lat, lon, 80)
+        monkeypatch.delenv("LM_HIST_EXACT")
+        np.testing.assert_array_equal(fast[0], exact[0])
+        assert fast[1] == exact[1]
