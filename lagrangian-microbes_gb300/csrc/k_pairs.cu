@@ -76,21 +76,36 @@ __device__ __forceinline__ Vertex load_vertex(const Bufs& b, uint32_t s) {
   return v;
 }
 
-// Calls f(t) for every cell-order index t != s within the radius of vertex v.
+// Calls f(t) for every cell-order index t != s within the radius of vertex v (in no particular
+// order). The key runs of the three rows (at most two each) are found first and all their cell
+// starts loaded together; each run is then walked four candidates at a time, the positions loaded
+// before the tests, so a microbe waits for a few load latencies instead of one per candidate.
 template <class F>
 __device__ __forceinline__ void for_neighbours(const Bufs& b, const PairParams& pp, const Vertex& v, F&& f) {
+  uint32_t klo[6], khi[6];
+  bool has[6];
+#pragma unroll
   for (int dy = -1; dy <= 1; ++dy) {
     const int ry = (int)v.cy + dy;
-    if (ry < 0 || ry >= v.g.ncy) continue;
-    const RowRuns rr = row_runs(v.g, max((int)v.cx - 1, 0), min((int)v.cx + 1, v.g.ncx - 1), ry);
+    const bool row = ry >= 0 && ry < v.g.ncy;
+    const RowRuns rr = row_runs(v.g, max((int)v.cx - 1, 0), min((int)v.cx + 1, v.g.ncx - 1), row ? ry : (int)v.cy);
 #pragma unroll
     for (int q = 0; q < 2; ++q) {
-      if (q >= rr.n) break;
-      const uint32_t t1 = b.cstart[rr.hi[q] + 1];
-      for (uint32_t t = b.cstart[rr.lo[q]]; t < t1; ++t)
-        if (t != v.s && within(pp, v.ps, b.spos[t])) f(t);
+      has[(dy + 1) * 2 + q] = row && q < rr.n;
+      klo[(dy + 1) * 2 + q] = rr.lo[q];
+      khi[(dy + 1) * 2 + q] = rr.hi[q];
     }
   }
+  uint32_t t0[6], t1[6];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    t0[k] = has[k] ? b.cstart[klo[k]] : 0u;
+    t1[k] = has[k] ? b.cstart[khi[k] + 1] : 0u;
+  }
+#pragma unroll
+  for (int k = 0; k < 6; ++k)
+    for (uint32_t t = t0[k]; t < t1[k]; ++t)
+      if (t != v.s && within(pp, v.ps, b.spos[t])) f(t);
 }
 
 __device__ __forceinline__ uint32_t lanemask_lt_p() {
