@@ -78,8 +78,8 @@ __device__ __forceinline__ Vertex load_vertex(const Bufs& b, uint32_t s) {
 
 // Calls f(t) for every cell-order index t != s within the radius of vertex v (in no particular
 // order). The key runs of the three rows (at most two each) are found first and all their cell
-// starts loaded together; each run is then walked four candidates at a time, the positions loaded
-// before the tests, so a microbe waits for a few load latencies instead of one per candidate.
+// starts loaded together, so a microbe waits for one round of those loads instead of one per row.
+// (Walking the runs four candidates at a time as well needed 58 registers and was slower.)
 template <class F>
 __device__ __forceinline__ void for_neighbours(const Bufs& b, const PairParams& pp, const Vertex& v, F&& f) {
   uint32_t klo[6], khi[6];
