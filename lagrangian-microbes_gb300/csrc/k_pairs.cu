@@ -262,7 +262,7 @@ __device__ __forceinline__ void count_runs(const Vertex& v, const Bufs& b, uint3
 __global__ void __launch_bounds__(COUNT_THREADS) k_count_pairs(Bufs b, PairParams pp, Ctrl* ctrl) {
   pdl_wait();
   if (ctrl->halt) return;
-  __shared__ float2 tile[COUNT_THREADS];
+  __shared__ __align__(16) float2 tile[COUNT_THREADS];
   __shared__ uint32_t first_key, last_key;
   __shared__ unsigned long long tot;
   const uint32_t n_valid = ctrl->n_valid;
@@ -293,23 +293,40 @@ __global__ void __launch_bounds__(COUNT_THREADS) k_count_pairs(Bufs b, PairParam
         // own cell: partner index tb + k must exceed s
         const uint32_t k0 = q == 0 ? (s + 1 > tb ? min(s + 1 - tb, n_t) : 0u) : 0u;
         if (pp.norm == 2) {
-          // branch-free float32 decision; a tile holding a candidate inside the float32 band
-          // around r^2 is recounted with the exact test (the same decision as within())
-          uint32_t c = 0;
-          bool band = false;
-#pragma unroll 8
-          for (uint32_t k = k0; k < n_t; ++k) {
-            const float2 t = tile[k];
-            const float dx = me.x - t.x, dy = me.y - t.y;
-            const float d2 = __fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy));
-            c += d2 < pp.r2f_lo ? 1u : 0u;
-            band |= d2 >= pp.r2f_lo && d2 <= pp.r2f_hi;
+          // branch-free float32 decision, two candidates per 16-byte shared load: clo counts the
+          // candidates below the float32 band around r^2, chi those not above it; a tile where they
+          // differ holds a candidate inside the band and is recounted with the exact test (the same
+          // decision as within()). d2 is one fused multiply-add: its error is far inside the band.
+          uint32_t clo = 0, chi = 0;
+          const float lo = pp.r2f_lo, hi = pp.r2f_hi;
+          uint32_t k = k0;
+          if ((k & 1u) && k < n_t) {
+            const float dx = me.x - tile[k].x, dy = me.y - tile[k].y;
+            const float d2 = fmaf(dx, dx, dy * dy);
+            clo += d2 < lo ? 1u : 0u;
+            chi += d2 <= hi ? 1u : 0u;
+            ++k;
           }
-          if (band) {
-            c = 0;
-            for (uint32_t k = k0; k < n_t; ++k) c += within(pp, me, tile[k]) ? 1u : 0u;
+          const float4* t4 = reinterpret_cast<const float4*>(tile);
+#pragma unroll 4
+          for (; k + 1 < n_t; k += 2) {
+            const float4 q = t4[k >> 1];
+            const float ax = me.x - q.x, ay = me.y - q.y, bx = me.x - q.z, by = me.y - q.w;
+            const float da = fmaf(ax, ax, ay * ay), db = fmaf(bx, bx, by * by);
+            clo += (da < lo ? 1u : 0u) + (db < lo ? 1u : 0u);
+            chi += (da <= hi ? 1u : 0u) + (db <= hi ? 1u : 0u);
           }
-          cnt += c;
+          if (k < n_t) {
+            const float dx = me.x - tile[k].x, dy = me.y - tile[k].y;
+            const float d2 = fmaf(dx, dx, dy * dy);
+            clo += d2 < lo ? 1u : 0u;
+            chi += d2 <= hi ? 1u : 0u;
+          }
+          if (clo != chi) {
+            clo = 0;
+            for (uint32_t kk = k0; kk < n_t; ++kk) clo += within(pp, me, tile[kk]) ? 1u : 0u;
+          }
+          cnt += clo;
         } else {
           for (uint32_t k = k0; k < n_t; ++k) cnt += within(pp, me, tile[k]) ? 1u : 0u;
         }
