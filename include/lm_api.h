@@ -258,6 +258,15 @@ int lm_adjoint_final_positions(lm_adjoint* adj, double* lon, double* lat);
  * sampled the same pieces. Used to compare gradients with an FP64 run cell path by cell path. */
 int lm_adjoint_cell_signature(lm_adjoint* adj, unsigned long long* sig);
 
+/* ---- failure injection (tests; no reference counterpart) ----
+ * The next lm_step call that interacts (plain launches only, never a captured graph) makes its
+ * first step's interaction kernel wait on a device flag that nothing sets, as a stalled
+ * dependency would, until `seconds` (0 < seconds <= 10) have passed: the kernel then records the
+ * timeout and returns, no pair of that step is applied, and the call returns LM_ERR_TIMEOUT. The
+ * context stays usable; later steps run normally. Failure detection is exercised this way without
+ * any fault on the GPU. */
+int lm_debug_inject_wait(lm_ctx* ctx, double seconds);
+
 /* ---- pairwise distance histogram ----
  * Replaces pairwise_distance_histogram_parallel / pairwise_distance_histogram_1point
  * (sandbox/pairwise_distance_histogram_distributed.jl:56-76) and pairwise_dist_gpu

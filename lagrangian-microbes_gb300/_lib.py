@@ -136,6 +136,7 @@ SIGNATURES = {
     "lm_adjoint_cell_signature": [P, P],
     "lm_adjoint_final_positions": [P, P, P],
     "lm_distance_histogram": [P, P, P, I64, P, I32, I32, F64, P],
+    "lm_debug_inject_wait": [P, F64],
 }
 
 

@@ -353,6 +353,20 @@ __device__ bool rounds_tiled(const Bufs& b, uint32_t step, Ctrl* ctrl, unsigned 
 __global__ void __launch_bounds__(RD_THREADS) k_rounds(Bufs b, StepArgs a, Ctrl* ctrl) {
   pdl_wait();
   if (((volatile uint32_t*)&ctrl->halt)[0]) return;
+  if (a.test_wait_ns) {
+    // injected failure (tests): the wait of a stalled dependency, on a flag that nothing sets,
+    // bounded like every wait of this kernel; the step applies no pair and reports the timeout
+    if (threadIdx.x == 0) {
+      const unsigned long long w0 = globaltimer();
+      while (((volatile uint32_t*)&ctrl->never)[0] == 0u) {
+        if (globaltimer() - w0 > a.test_wait_ns) {
+          atomicOr(&ctrl->err, (uint32_t)ERRB_TIMEOUT);
+          break;
+        }
+      }
+    }
+    return;
+  }
   const uint32_t step = a.use_ctrl_step ? ctrl->step : a.step0;
   const uint32_t cnt = ((volatile uint32_t*)&ctrl->act_n)[0];
   const uint32_t stride = gridDim.x * blockDim.x;

@@ -94,6 +94,7 @@ struct lm_ctx {
   // control block
   Ctrl* ctrl = nullptr;
   Ctrl* hctrl = nullptr;
+  unsigned long long inject_wait_ns = 0;  // lm_debug_inject_wait: the next plain interaction step
   uint32_t* hstage = nullptr;
   size_t hstage_n = 0;
 
@@ -449,6 +450,7 @@ StepArgs step_args(double t, double dt, int64_t step, double kh, bool graph) {
   a.step0 = (uint32_t)step;
   a.use_ctrl_step = graph ? 1 : 0;
   a.kick = kh > 0 ? (float)std::sqrt(6.0 * std::fabs(dt) * kh) : 0.f;
+  a.test_wait_ns = 0;
   return a;
 }
 
@@ -557,7 +559,11 @@ int run_steps(lm_ctx* c, double t, double dt, int64_t n_steps, int64_t step0, ui
   bool redo = false;
   while (s < n_steps) {
     for (int64_t k = s; k < n_steps; ++k) {
-      const StepArgs a = step_args(t + dt * k, dt, step0 + k, kh, false);
+      StepArgs a = step_args(t + dt * k, dt, step0 + k, kh, false);
+      if (c->inject_wait_ns && (flags & LM_STEP_INTERACT)) {  // armed by lm_debug_inject_wait: this step only
+        a.test_wait_ns = c->inject_wait_ns;
+        c->inject_wait_ns = 0;
+      }
       CK(enqueue_step(c, a, flags, !(redo && k == s)));
       if ((r = record_step(c, k, rec_lon, rec_lat, rec_species))) return r;
       if (rec_census)
@@ -1070,6 +1076,13 @@ int lm_query_pairs(lm_ctx* c, int64_t n, const float* lon, const float* lat, int
     pi[k] = (int32_t)(pairs[k] >> 32);
     pj[k] = (int32_t)(pairs[k] & 0xffffffffu);
   }
+  return LM_OK;
+}
+
+int lm_debug_inject_wait(lm_ctx* c, double seconds) {
+  if (!c) return LM_ERR_ARG;
+  if (!(seconds > 0.0 && seconds <= 10.0)) return fail(c, LM_ERR_ARG, "seconds must be in (0, 10]");
+  c->inject_wait_ns = std::max<unsigned long long>(1ull, (unsigned long long)(seconds * 1e9));
   return LM_OK;
 }
 

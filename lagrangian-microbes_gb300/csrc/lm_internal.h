@@ -76,7 +76,7 @@ struct Ctrl {
   int stage_k[3];               // frame brackets of this step's stage times t, t+dt/2, t+dt
   float stage_w[3];
   int stage_ok;                 // 0 when a stage time left the field's time axis
-  uint32_t pad2;
+  uint32_t never;               // a flag nothing sets: the injected failure of the tests waits on it
 };
 
 // Per-ensemble constants (device array, one entry per ensemble).
@@ -160,6 +160,9 @@ struct StepArgs {
   uint32_t step0;     // global step index of t_start
   int use_ctrl_step;  // 1: step index = ctrl->step (graph mode); 0: step index = step0
   float kick;         // sqrt(6 |dt| Kh) in degrees, 0 disables the diffusion kick
+  // failure injection (lm_debug_inject_wait, plain steps only): when nonzero, k_rounds waits on
+  // Ctrl::never, which nothing sets, until this many nanoseconds have passed, and reports a timeout
+  unsigned long long test_wait_ns;
 };
 
 // Everything the per-step kernels need besides the field.
