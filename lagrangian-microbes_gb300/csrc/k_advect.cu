@@ -162,10 +162,11 @@ void launch_bbox(const Bufs& b, Ctrl* ctrl, bool use_status, cudaStream_t st) {
 }
 
 // Per-step bookkeeping: reset the per-step counters and the ensemble boxes (start), advance the
-// device step counter (end).
-__global__ void k_step_begin(Bufs b, FieldView f, StepArgs a, int bracket, Ctrl* ctrl) {
-  pdl_wait();
-  if (ctrl->halt) return;
+// device step counter (end). Within one call the end of a step also does the start of the next
+// (k_step_end with `chain`), which saves a launch per step; the counters are reset by the same
+// thread that has just accumulated them.
+__device__ __forceinline__ void step_begin_body(const Bufs& b, const FieldView& f, const StepArgs& a, int bracket,
+                                                Ctrl* ctrl) {
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   for (uint32_t e = t; e < b.n_ens; e += gridDim.x * blockDim.x) {
     b.ebox[4 * e + 0] = 0xffffffffu;  // min: start at the largest encoding
@@ -200,26 +201,48 @@ __global__ void k_step_begin(Bufs b, FieldView f, StepArgs a, int bracket, Ctrl*
   }
 }
 
-__global__ void k_step_end(Ctrl* ctrl, int interact) {
+__global__ void k_step_begin(Bufs b, FieldView f, StepArgs a, int bracket, Ctrl* ctrl) {
   pdl_wait();
   if (ctrl->halt) return;
-  if (interact) {
-    ctrl->pairs_total += ctrl->n_dir / 2;
-    ctrl->steps_total += 1;
-    ctrl->rounds_total += ctrl->rounds;
-  }
-  ctrl->step += 1;
+  step_begin_body(b, f, a, bracket, ctrl);
 }
 
-void launch_step_begin(const Bufs& b, const FieldView* f, const StepArgs& a, Ctrl* ctrl, cudaStream_t st) {
+// End of a step; with `chain`, also the start of the next one (`an` its arguments).
+__global__ void k_step_end(Bufs b, FieldView f, StepArgs an, int bracket, Ctrl* ctrl, int interact, int chain) {
+  pdl_wait();
+  if (ctrl->halt) return;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (interact) {
+      ctrl->pairs_total += ctrl->n_dir / 2;
+      ctrl->steps_total += 1;
+      ctrl->rounds_total += ctrl->rounds;
+    }
+    ctrl->step += 1;
+  }
+  if (chain) step_begin_body(b, f, an, bracket, ctrl);
+}
+
+static int bookkeeping_grid(const Bufs& b) {
   int grid = (int)((b.n_ens + 255) / 256);
   if (grid < 1) grid = 1;
   if (grid > 64) grid = 64;
+  return grid;
+}
+
+void launch_step_begin(const Bufs& b, const FieldView* f, const StepArgs& a, Ctrl* ctrl, cudaStream_t st) {
   FieldView fv{};
   if (f) fv = *f;
-  launch_dep(k_step_begin, dim3(grid), dim3(256), st, b, fv, a, f ? 1 : 0, ctrl);
+  launch_dep(k_step_begin, dim3(bookkeeping_grid(b)), dim3(256), st, b, fv, a, f ? 1 : 0, ctrl);
 }
-void launch_step_end(Ctrl* ctrl, bool interact, cudaStream_t st) { launch_dep(k_step_end, dim3(1), dim3(1), st, ctrl, interact ? 1 : 0); }
+void launch_step_end(Ctrl* ctrl, bool interact, cudaStream_t st) {
+  launch_dep(k_step_end, dim3(1), dim3(1), st, Bufs{}, FieldView{}, StepArgs{}, 0, ctrl, interact ? 1 : 0, 0);
+}
+void launch_step_turn(const Bufs& b, const FieldView* f, const StepArgs& an, Ctrl* ctrl, bool interact,
+                      cudaStream_t st) {
+  FieldView fv{};
+  if (f) fv = *f;
+  launch_dep(k_step_end, dim3(bookkeeping_grid(b)), dim3(256), st, b, fv, an, f ? 1 : 0, ctrl, interact ? 1 : 0, 1);
+}
 
 // Gathers from the padded slot layout into caller order (map[slot] = caller index or -1).
 template <class T>

@@ -479,18 +479,24 @@ cudaError_t enqueue_interaction(lm_ctx* c, const StepArgs& a, uint32_t flags, bo
   return cudaGetLastError();
 }
 
-// One fused step; `advect` false re-runs only the interaction part of an advected step.
-cudaError_t enqueue_step(lm_ctx* c, const StepArgs& a, uint32_t flags, bool advect) {
+// One fused step; `advect` false re-runs only the interaction part of an advected step. `begun`:
+// the previous step's end already started this one; `next` (the next step of the same call, which
+// advects): this step's end also starts that one.
+cudaError_t enqueue_step(lm_ctx* c, const StepArgs& a, uint32_t flags, bool advect, bool begun = false,
+                         const StepArgs* next = nullptr) {
   const Bufs b = bufs(c, false);
-  PROF(c, P_BOOKKEEPING, launch_step_begin(b, advect ? &c->fv : nullptr, a, c->ctrl, c->st));
+  if (!begun) PROF(c, P_BOOKKEEPING, launch_step_begin(b, advect ? &c->fv : nullptr, a, c->ctrl, c->st));
   if (advect) PROF(c, P_ADVECT, launch_advect(c->fv, a, b, c->ctrl, c->st));
   if (flags & (LM_STEP_INTERACT | LM_STEP_COUNT_PAIRS)) {
     cudaError_t e = enqueue_interaction(c, a, flags, !advect, true);
     if (e != cudaSuccess) return e;
   }
   if (flags & LM_STEP_CENSUS) PROF(c, P_CENSUS, launch_census(b, c->ctrl, c->st));
-  PROF(c, P_BOOKKEEPING,
-       launch_step_end(c->ctrl, (flags & (LM_STEP_INTERACT | LM_STEP_COUNT_PAIRS)) != 0, c->st));
+  const bool counted = (flags & (LM_STEP_INTERACT | LM_STEP_COUNT_PAIRS)) != 0;
+  if (next)
+    PROF(c, P_BOOKKEEPING, launch_step_turn(b, &c->fv, *next, c->ctrl, counted, c->st));
+  else
+    PROF(c, P_BOOKKEEPING, launch_step_end(c->ctrl, counted, c->st));
   return cudaGetLastError();
 }
 
@@ -558,13 +564,18 @@ int run_steps(lm_ctx* c, double t, double dt, int64_t n_steps, int64_t step0, ui
   int64_t s = 0;
   bool redo = false;
   while (s < n_steps) {
+    bool chained = false;  // the previous step's end started step k
     for (int64_t k = s; k < n_steps; ++k) {
       StepArgs a = step_args(t + dt * k, dt, step0 + k, kh, false);
       if (c->inject_wait_ns && (flags & LM_STEP_INTERACT)) {  // armed by lm_debug_inject_wait: this step only
         a.test_wait_ns = c->inject_wait_ns;
         c->inject_wait_ns = 0;
       }
-      CK(enqueue_step(c, a, flags, !(redo && k == s)));
+      // the last step keeps its counters for lm_stats; a per-step census read keeps them per step
+      const bool chain = k + 1 < n_steps && !rec_census;
+      const StepArgs an = step_args(t + dt * (k + 1), dt, step0 + k + 1, kh, false);
+      CK(enqueue_step(c, a, flags, !(redo && k == s), chained, chain ? &an : nullptr));
+      chained = chain;
       if ((r = record_step(c, k, rec_lon, rec_lat, rec_species))) return r;
       if (rec_census)
         CK(cudaMemcpyAsync(c->hstage + 4 * k, c->ctrl->census, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->st));
@@ -610,8 +621,8 @@ int capture(lm_ctx* c) {
   CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
   c->capturing = true;
   for (int k = 0; k < c->g_spg; ++k) {
-    const StepArgs a = step_args(c->g_t_start, c->g_dt, c->g_step0, c->g_kh, true);
-    const cudaError_t le = enqueue_step(c, a, c->g_flags, true);
+    const StepArgs a = step_args(c->g_t_start, c->g_dt, c->g_step0, c->g_kh, true);  // step from the device counter
+    const cudaError_t le = enqueue_step(c, a, c->g_flags, true, k > 0, k + 1 < c->g_spg ? &a : nullptr);
     if (le != cudaSuccess) {
       c->capturing = false;
       cudaGraph_t g = nullptr;

@@ -240,6 +240,9 @@ void launch_interleave(const float* u, const float* v, float2* uv, size_t n, cud
 // step_begin also brackets the stage times of the step in the field's frames when `f` is given.
 void launch_step_begin(const Bufs& b, const FieldView* f, const StepArgs& a, Ctrl* ctrl, cudaStream_t st);
 void launch_step_end(Ctrl* ctrl, bool interact, cudaStream_t st);
+// End of a step and start of the next (arguments `an`) in one launch (steps of one call).
+void launch_step_turn(const Bufs& b, const FieldView* f, const StepArgs& an, Ctrl* ctrl, bool interact,
+                      cudaStream_t st);
 void launch_advect(const FieldView& f, const StepArgs& a, const Bufs& b, Ctrl* ctrl, cudaStream_t st);
 void launch_bbox(const Bufs& b, Ctrl* ctrl, bool use_status, cudaStream_t st);
 
