@@ -36,6 +36,116 @@ __device__ __forceinline__ float grid_dims(const uint32_t* box, float c, float* 
   return ceilf(*ncx / (float)TILE) * ceilf(*ncy / (float)TILE) * (float)(TILE * TILE);
 }
 
+// Key ranges in ensemble index order (batches of more ensembles than the block has threads).
+__device__ __forceinline__ void grid_in_order(const Bufs& b, float c, unsigned long long* carry_sh, uint32_t* wsi) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (uint32_t e0 = 0; e0 < b.n_ens; e0 += GRID_THREADS) {
+    const uint32_t e = e0 + threadIdx.x;
+    float nx = 0.f, ny = 0.f;
+    uint32_t cells = 0;
+    if (e < b.n_ens) cells = (uint32_t)fminf(grid_dims(b.ebox + 4 * e, c, &nx, &ny), 4.0e9f);
+    uint32_t y = cells;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, y, o);
+      if (lane >= o) y += t;
+    }
+    if (lane == 31) wsi[wid] = y;
+    __syncthreads();
+    unsigned long long wp = 0, tot = 0;
+    for (int w = 0; w < GRID_THREADS / 32; ++w) {
+      if (w < wid) wp += wsi[w];
+      tot += wsi[w];
+    }
+    const unsigned long long base = (*carry_sh) + wp + y - cells;
+    if (e < b.n_ens) {
+      EnsGrid g;
+      const uint32_t* box = b.ebox + 4 * e;
+      const bool empty = !(dec_f(box[0]) <= dec_f(box[2]));
+      g.c = c;
+      g.inv_c = 1.f / c;
+      g.x0 = empty ? 0.f : dec_f(box[0]) - c;
+      g.y0 = empty ? 0.f : dec_f(box[1]) - c;
+      g.ncx = (int)nx;
+      g.ncy = (int)ny;
+      g.cell_base = (uint32_t)(base > 0xffffffffull ? 0xffffffffull : base);
+      g.pad = 0;
+      b.grids[e] = g;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) (*carry_sh) += tot;
+    __syncthreads();
+  }
+  for (uint32_t e = threadIdx.x; e < b.n_ens; e += GRID_THREADS) b.eord[e] = e;
+}
+
+// Key ranges ordered by density, densest ensemble first (microbes per bounding-box area, ties by
+// index). The interaction applies batches larger than the blocks' shared memory in groups of
+// ensembles consecutive in key order, and a group lasts as long as its longest dependency chains,
+// which grow with the density: consecutive dense ensembles share groups instead of each slowing a
+// group of sparse ones. Pairs do not depend on the order (every ensemble has its own key range).
+__device__ __forceinline__ void grid_ranked(const Bufs& b, float c, unsigned long long* carry_sh) {
+  __shared__ float dsh[GRID_THREADS];
+  __shared__ uint32_t csh[GRID_THREADS];
+  __shared__ unsigned long long bsh[GRID_THREADS];
+  __shared__ unsigned long long wsum[GRID_THREADS / 32];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const uint32_t E = b.n_ens, e = threadIdx.x;
+  float nx = 0.f, ny = 0.f, dens = -1.f;
+  uint32_t cells = 0;
+  if (e < E) {
+    const uint32_t* box = b.ebox + 4 * e;
+    cells = (uint32_t)fminf(grid_dims(box, c, &nx, &ny), 4.0e9f);
+    const float w = dec_f(box[2]) - dec_f(box[0]), h = dec_f(box[3]) - dec_f(box[1]);
+    dens = (w >= 0.f && h >= 0.f) ? (float)b.ens[e].n / ((w + c) * (h + c)) : 0.f;  // also NaN -> 0
+  }
+  dsh[e] = dens;
+  __syncthreads();
+  uint32_t rk = e;  // threads past E keep their index (no cells)
+  if (e < E) {
+    rk = 0;
+    for (uint32_t f = 0; f < E; ++f) {
+      const float d = dsh[f];
+      rk += (d > dens || (d == dens && f < e)) ? 1u : 0u;
+    }
+    b.eord[rk] = e;
+  }
+  csh[rk] = cells;  // the ranks of [0, E) are a permutation of [0, E)
+  __syncthreads();
+  // exclusive scan of the cells in rank order (thread j holds rank j)
+  const unsigned long long own = csh[threadIdx.x];
+  unsigned long long y = own;
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long t = __shfl_up_sync(0xffffffffu, y, o);
+    if (lane >= o) y += t;
+  }
+  if (lane == 31) wsum[wid] = y;
+  __syncthreads();
+  unsigned long long wp = 0, tot = 0;
+  for (int w = 0; w < GRID_THREADS / 32; ++w) {
+    if (w < wid) wp += wsum[w];
+    tot += wsum[w];
+  }
+  bsh[threadIdx.x] = wp + y - own;
+  __syncthreads();
+  if (e < E) {
+    const unsigned long long base = bsh[rk];
+    EnsGrid g;
+    const uint32_t* box = b.ebox + 4 * e;
+    const bool empty = !(dec_f(box[0]) <= dec_f(box[2]));
+    g.c = c;
+    g.inv_c = 1.f / c;
+    g.x0 = empty ? 0.f : dec_f(box[0]) - c;
+    g.y0 = empty ? 0.f : dec_f(box[1]) - c;
+    g.ncx = (int)nx;
+    g.ncy = (int)ny;
+    g.cell_base = (uint32_t)(base > 0xffffffffull ? 0xffffffffull : base);
+    g.pad = 0;
+    b.grids[e] = g;
+  }
+  if (threadIdx.x == 0) *carry_sh = tot;
+  __syncthreads();
+}
+
 // One block: grid geometry of every ensemble and the global cell numbering. If the cells would
 // exceed the capacity, the cell size grows (pairs stay exact because only c >= r matters).
 __global__ void __launch_bounds__(GRID_THREADS) k_grid(Bufs b, PairParams pp, Ctrl* ctrl) {
@@ -73,41 +183,10 @@ __global__ void __launch_bounds__(GRID_THREADS) k_grid(Bufs b, PairParams pp, Ct
   __shared__ unsigned long long carry;
   if (threadIdx.x == 0) carry = 0;
   __syncthreads();
-  for (uint32_t e0 = 0; e0 < b.n_ens; e0 += GRID_THREADS) {
-    const uint32_t e = e0 + threadIdx.x;
-    float nx = 0.f, ny = 0.f;
-    uint32_t cells = 0;
-    if (e < b.n_ens) cells = (uint32_t)fminf(grid_dims(b.ebox + 4 * e, c, &nx, &ny), 4.0e9f);
-    uint32_t y = cells;
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t t = __shfl_up_sync(0xffffffffu, y, o);
-      if (lane >= o) y += t;
-    }
-    if (lane == 31) wsi[wid] = y;
-    __syncthreads();
-    unsigned long long wp = 0, tot = 0;
-    for (int w = 0; w < GRID_THREADS / 32; ++w) {
-      if (w < wid) wp += wsi[w];
-      tot += wsi[w];
-    }
-    const unsigned long long base = carry + wp + y - cells;
-    if (e < b.n_ens) {
-      EnsGrid g;
-      const uint32_t* box = b.ebox + 4 * e;
-      const bool empty = !(dec_f(box[0]) <= dec_f(box[2]));
-      g.c = c;
-      g.inv_c = 1.f / c;
-      g.x0 = empty ? 0.f : dec_f(box[0]) - c;
-      g.y0 = empty ? 0.f : dec_f(box[1]) - c;
-      g.ncx = (int)nx;
-      g.ncy = (int)ny;
-      g.cell_base = (uint32_t)(base > 0xffffffffull ? 0xffffffffull : base);
-      g.pad = 0;
-      b.grids[e] = g;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) carry += tot;
-    __syncthreads();
+  if (b.n_ens <= GRID_THREADS) {
+    grid_ranked(b, c, &carry);
+  } else {
+    grid_in_order(b, c, &carry, wsi);
   }
   if (threadIdx.x == 0) {
     const unsigned long long total = carry;

@@ -310,14 +310,15 @@ __device__ bool rounds_tiled(const Bufs& b, uint32_t step, Ctrl* ctrl, unsigned 
       ng = 1;
     }
   } else {
-    // ensemble e holds the vertices [cstart[cell_base_e], cstart[cell_base_e+1]); greedy groups
-    // of whole ensembles, each at most `cap` vertices (none when one ensemble alone is larger)
+    // the k-th ensemble in key order, e = eord[k], holds the vertices from cstart[cell_base_e] to
+    // the next one's start; greedy groups of whole ensembles consecutive in that order, each at
+    // most `cap` vertices (none when one ensemble alone is larger)
     extern __shared__ unsigned long long tl_raw[];
     uint32_t* es = reinterpret_cast<uint32_t*>(tl_raw);
     const uint32_t E = b.n_ens;
     const bool fits = E + 1 <= (uint32_t)(TL_SMEM / sizeof(uint32_t));
     if (fits) {
-      for (uint32_t e = threadIdx.x; e < E; e += blockDim.x) es[e] = b.cstart[b.grids[e].cell_base];
+      for (uint32_t e = threadIdx.x; e < E; e += blockDim.x) es[e] = b.cstart[b.grids[b.eord[e]].cell_base];
       if (threadIdx.x == 0) es[E] = n_valid;
     }
     __syncthreads();

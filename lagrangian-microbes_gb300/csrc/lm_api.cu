@@ -71,6 +71,7 @@ struct lm_ctx {
   int8_t* rsp = nullptr;
   uint32_t ens_cap = 0;
   EnsGrid* grids = nullptr;
+  uint32_t* eord = nullptr;
   uint32_t* ebox = nullptr;
   uint32_t* census = nullptr;
 
@@ -270,7 +271,8 @@ int ensure_slots(lm_ctx* c, uint32_t slots, uint32_t n_ens) {
   }
   if (n_ens > c->ens_cap || !c->ens_d) {
     const uint32_t cap = std::max<uint32_t>(n_ens, 1);
-    if ((r = dalloc(c, &c->ens_d, cap)) || (r = dalloc(c, &c->grids, cap)) || (r = dalloc(c, &c->ebox, (size_t)4 * cap)) ||
+    if ((r = dalloc(c, &c->ens_d, cap)) || (r = dalloc(c, &c->grids, cap)) || (r = dalloc(c, &c->eord, cap)) ||
+        (r = dalloc(c, &c->ebox, (size_t)4 * cap)) ||
         (r = dalloc(c, &c->census, (size_t)4 * cap)))
       return r;
     CK(cudaMemsetAsync(c->census, 0, sizeof(uint32_t) * 4 * cap, c->st));
@@ -313,6 +315,10 @@ int layout(lm_ctx* c, uint32_t n_ens, const int64_t* counts) {
   }
   if (slot) CK(cudaMemcpyAsync(c->map_d, c->hmap.data(), slot * sizeof(int32_t), cudaMemcpyHostToDevice, c->st));
   CK(cudaMemcpyAsync(c->block_ens, bens.data(), bens.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, c->st));
+  // key ranges in index order until the first k_grid (which may reorder them; one ensemble never is)
+  std::vector<uint32_t> eord(n_ens);
+  for (uint32_t e = 0; e < n_ens; ++e) eord[e] = e;
+  CK(cudaMemcpyAsync(c->eord, eord.data(), n_ens * sizeof(uint32_t), cudaMemcpyHostToDevice, c->st));
   CK(cudaStreamSynchronize(c->st));
   return LM_OK;
 }
@@ -359,6 +365,7 @@ Bufs bufs(const lm_ctx* c, bool log) {
   b.plat = c->plat;
   b.ebox = c->ebox;
   b.grids = c->grids;
+  b.eord = c->eord;
   b.key = c->key;
   b.rank = c->rank;
   b.ccount = c->ccount;
@@ -704,7 +711,7 @@ int lm_ctx_destroy(lm_ctx* c) {
   void* bufs_[] = {c->uv,     c->xo,    c->yo,     c->plon,   c->plat,   c->species, c->status, c->key,
                    c->rank,   c->sid,   c->skey,   c->sens,   c->deg,    c->slab,    c->off,    c->longv,
                    c->wstate, c->level,  c->act,    c->spos,   c->rlon,    c->rlat,   c->rsp,
-                   c->map_d,  c->block_ens, c->ens_d, c->grids, c->ebox, c->census,  c->ccount, c->cstart,
+                   c->map_d,  c->block_ens, c->ens_d, c->grids, c->eord, c->ebox, c->census,  c->ccount, c->cstart,
                    c->csum,   c->ovf,   c->oprio,  c->ctrl,   c->plog,  c->snap_xo, c->snap_yo, c->snap_sp,
                    c->snap_st};
   for (void* p : bufs_)

@@ -180,6 +180,7 @@ struct Bufs {
   float* plat;
   uint32_t* ebox;     // [E][4] ordered-int encoded min x, min y, max x, max y
   EnsGrid* grids;     // [E]
+  uint32_t* eord;     // [E] the ensembles in the order of their key ranges (cell order)
   uint32_t* key;
   uint32_t* rank;
   uint32_t* ccount;   // [cells_cap + 1]
