@@ -80,8 +80,9 @@ __device__ __forceinline__ Vertex load_vertex(const Bufs& b, uint32_t s) {
 // order). The key runs of the three rows (at most two each) are found first and all their cell
 // starts loaded together, so a microbe waits for one round of those loads instead of one per row.
 // (Walking the runs four candidates at a time as well needed 58 registers and was slower.)
-template <class F>
-__device__ __forceinline__ void for_neighbours(const Bufs& b, const PairParams& pp, const Vertex& v, F&& f) {
+// The cell-order ranges [t0[k], t1[k]) of the (at most six) key runs of v's 3x3 neighbourhood,
+// all cell starts loaded together; missing runs are empty.
+__device__ __forceinline__ void neighbour_runs(const Bufs& b, const Vertex& v, uint32_t* t0, uint32_t* t1) {
   uint32_t klo[6], khi[6];
   bool has[6];
 #pragma unroll
@@ -96,12 +97,17 @@ __device__ __forceinline__ void for_neighbours(const Bufs& b, const PairParams& 
       khi[(dy + 1) * 2 + q] = rr.hi[q];
     }
   }
-  uint32_t t0[6], t1[6];
 #pragma unroll
   for (int k = 0; k < 6; ++k) {
     t0[k] = has[k] ? b.cstart[klo[k]] : 0u;
     t1[k] = has[k] ? b.cstart[khi[k] + 1] : 0u;
   }
+}
+
+template <class F>
+__device__ __forceinline__ void for_neighbours(const Bufs& b, const PairParams& pp, const Vertex& v, F&& f) {
+  uint32_t t0[6], t1[6];
+  neighbour_runs(b, v, t0, t1);
 #pragma unroll
   for (int k = 0; k < 6; ++k)
     for (uint32_t t = t0[k]; t < t1[k]; ++t)
@@ -505,7 +511,9 @@ __global__ void __launch_bounds__(LONG_WARPS * 32) k_sweep_long(Bufs b, PairPara
     return;
   }
   for (uint32_t ib = 0; ib < count; ib += 32) {
-    // lane k holds vertex ib + k of this warp's list
+    // lane k holds vertex ib + k of this warp's list, and loads its cell, position, key runs and
+    // ensemble constants, for all 32 vertices at once (a chain of dependent loads per batch
+    // instead of one per vertex)
     const bool mine = ib + lane < count;
     const uint32_t s_l = mine ? b.longv[gw + (ib + lane) * nw] : 0u;
     const uint32_t d_l = mine ? b.deg[s_l] : 0u;
@@ -516,50 +524,81 @@ __global__ void __launch_bounds__(LONG_WARPS * 32) k_sweep_long(Bufs b, PairPara
     }
     const unsigned long long o_l = run + incl - d_l;
     run += __shfl_sync(0xffffffffu, incl, 31);
+    uint32_t r0[6], r1[6], la_l = 0, base_l = 0, k0_l = 0, k1_l = 0;
+    float px_l = 0.f, py_l = 0.f;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) r0[q] = r1[q] = 0u;
+    if (mine) {
+      const Vertex v = load_vertex(b, s_l);
+      neighbour_runs(b, v, r0, r1);
+      const EnsInfo& info = b.ens[v.e];
+      k0_l = info.seed_lo;
+      k1_l = info.seed_hi;
+      base_l = v.base;
+      la_l = b.sid[s_l] - v.base;
+      px_l = v.ps.x;
+      py_l = v.ps.y;
+    }
     const uint32_t nk = min(32u, count - ib);
     for (uint32_t k = 0; k < nk; ++k) {
       const uint32_t s = __shfl_sync(0xffffffffu, s_l, k);
       const uint32_t d = __shfl_sync(0xffffffffu, d_l, k);
       const unsigned long long o = __shfl_sync(0xffffffffu, o_l, k);
-      const Vertex v = load_vertex(b, s);
-      const EnsInfo& info = b.ens[v.e];
-      const uint32_t la = b.sid[s] - v.base;
+      const uint32_t la = __shfl_sync(0xffffffffu, la_l, k), base = __shfl_sync(0xffffffffu, base_l, k);
+      const uint32_t k0 = __shfl_sync(0xffffffffu, k0_l, k), k1 = __shfl_sync(0xffffffffu, k1_l, k);
+      const float2 ps = make_float2(__shfl_sync(0xffffffffu, px_l, k), __shfl_sync(0xffffffffu, py_l, k));
+      // the six runs as one candidate range: candidate i is in the run q with c[q] <= i < c[q + 1]
+      uint32_t t0[6], c[7];
+      c[0] = 0;
+#pragma unroll
+      for (int q = 0; q < 6; ++q) {
+        t0[q] = __shfl_sync(0xffffffffu, r0[q], k);
+        c[q + 1] = c[q] + (__shfl_sync(0xffffffffu, r1[q], k) - t0[q]);
+      }
       const bool in_smem = d <= LONG_SMEM_MAX;
       uint32_t m = 0;
-      for (int dy = -1; dy <= 1; ++dy) {
-        const int ry = (int)v.cy + dy;
-        if (ry < 0 || ry >= v.g.ncy) continue;
-        const RowRuns rr = row_runs(v.g, max((int)v.cx - 1, 0), min((int)v.cx + 1, v.g.ncx - 1), ry);
+      // two slices of 32 candidates per pass, each candidate's position and id loaded together
+      for (uint32_t tb = 0; tb < c[6]; tb += 64) {
+        uint32_t t[2], id[2];
+        float2 pt[2];
+        bool in[2];
 #pragma unroll
-        for (int q = 0; q < 2; ++q) {
-        if (q >= rr.n) break;
-        const uint32_t t0 = b.cstart[rr.lo[q]], t1 = b.cstart[rr.hi[q] + 1];
-        for (uint32_t tb = t0; tb < t1; tb += 32) {
-          const uint32_t t = tb + lane;
-          const bool ok = t < t1 && t != s && within(pp, v.ps, b.spos[t]);
+        for (int h = 0; h < 2; ++h) {
+          const uint32_t i = tb + 32u * h + lane;
+          uint32_t x = t0[0] + i;
+#pragma unroll
+          for (int q = 1; q < 6; ++q)
+            if (i >= c[q]) x = t0[q] + (i - c[q]);  // the last run starting at or before i (empty runs never win)
+          t[h] = x;
+          in[h] = i < c[6] && x != s;
+          pt[h] = in[h] ? b.spos[x] : ps;
+          id[h] = in[h] ? b.sid[x] : 0u;
+        }
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const bool ok = in[h] && within(pp, ps, pt[h]);
           const uint32_t mask = __ballot_sync(0xffffffffu, ok);
           if (ok) {
             const uint32_t pos = m + __popc(mask & lanemask_lt_p());
             if (pos < d) {
-              const uint32_t lb = b.sid[t] - v.base;
-              const unsigned long long p = pair_prio(min(la, lb), max(la, lb), step, info.seed_lo, info.seed_hi);
+              const uint32_t lb = id[h] - base;
+              const unsigned long long p = pair_prio(min(la, lb), max(la, lb), step, k0, k1);
               if (in_smem) {
                 sh.p[pos] = p;
-                sh.t[pos] = t;
+                sh.t[pos] = t[h];
               } else {
-                b.ovf[o + pos] = t;
+                b.ovf[o + pos] = t[h];
                 b.oprio[o + pos] = p;
               }
             }
           }
           m += __popc(mask);
         }
-        }
       }
       uint32_t first;
       if (in_smem) {
         __syncwarp();
-        long_sort(b, sh, v.base, d, lane);
+        long_sort(b, sh, base, d, lane);
         for (uint32_t i = lane; i < d; i += 32) b.ovf[o + i] = sh.t[sh.ord[i]];
         first = sh.t[sh.ord[0]];
         __syncwarp();  // the next vertex reuses the shared list
