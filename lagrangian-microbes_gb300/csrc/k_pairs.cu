@@ -104,14 +104,24 @@ __device__ __forceinline__ void neighbour_runs(const Bufs& b, const Vertex& v, u
   }
 }
 
+// The six runs are walked as one candidate range (candidate i lies in the run q with
+// c[q] <= i < c[q + 1]), so a warp's loop lasts as long as its longest total, not the sum of its
+// longest run of each row.
 template <class F>
 __device__ __forceinline__ void for_neighbours(const Bufs& b, const PairParams& pp, const Vertex& v, F&& f) {
   uint32_t t0[6], t1[6];
   neighbour_runs(b, v, t0, t1);
+  uint32_t c[7];
+  c[0] = 0;
 #pragma unroll
-  for (int k = 0; k < 6; ++k)
-    for (uint32_t t = t0[k]; t < t1[k]; ++t)
-      if (t != v.s && within(pp, v.ps, b.spos[t])) f(t);
+  for (int q = 0; q < 6; ++q) c[q + 1] = c[q] + (t1[q] - t0[q]);
+  for (uint32_t i = 0; i < c[6]; ++i) {
+    uint32_t t = t0[0] + i;
+#pragma unroll
+    for (int q = 1; q < 6; ++q)
+      if (i >= c[q]) t = t0[q] + (i - c[q]);  // the last run starting at or before i (empty runs never win)
+    if (t != v.s && within(pp, v.ps, b.spos[t])) f(t);
+  }
 }
 
 __device__ __forceinline__ uint32_t lanemask_lt_p() {
