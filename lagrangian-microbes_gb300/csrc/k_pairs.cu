@@ -535,6 +535,7 @@ __global__ void __launch_bounds__(LONG_WARPS * 32) k_sweep_long(Bufs b, PairPara
     const unsigned long long o_l = run + incl - d_l;
     run += __shfl_sync(0xffffffffu, incl, 31);
     uint32_t r0[6], r1[6], la_l = 0, base_l = 0, k0_l = 0, k1_l = 0;
+    int sp_l = 0;
     float px_l = 0.f, py_l = 0.f;
 #pragma unroll
     for (int q = 0; q < 6; ++q) r0[q] = r1[q] = 0u;
@@ -545,7 +546,9 @@ __global__ void __launch_bounds__(LONG_WARPS * 32) k_sweep_long(Bufs b, PairPara
       k0_l = info.seed_lo;
       k1_l = info.seed_hi;
       base_l = v.base;
-      la_l = b.sid[s_l] - v.base;
+      const uint32_t id = b.sid[s_l];
+      la_l = id - v.base;
+      sp_l = b.species[id];
       px_l = v.ps.x;
       py_l = v.ps.y;
     }
@@ -557,6 +560,7 @@ __global__ void __launch_bounds__(LONG_WARPS * 32) k_sweep_long(Bufs b, PairPara
       const uint32_t la = __shfl_sync(0xffffffffu, la_l, k), base = __shfl_sync(0xffffffffu, base_l, k);
       const uint32_t k0 = __shfl_sync(0xffffffffu, k0_l, k), k1 = __shfl_sync(0xffffffffu, k1_l, k);
       const float2 ps = make_float2(__shfl_sync(0xffffffffu, px_l, k), __shfl_sync(0xffffffffu, py_l, k));
+      const int sp = __shfl_sync(0xffffffffu, sp_l, k);
       // the six runs as one candidate range: candidate i is in the run q with c[q] <= i < c[q + 1]
       uint32_t t0[6], c[7];
       c[0] = 0;
@@ -606,7 +610,34 @@ __global__ void __launch_bounds__(LONG_WARPS * 32) k_sweep_long(Bufs b, PairPara
         }
       }
       uint32_t first;
-      if (in_smem) {
+      if (d <= 32) {
+        // one entry per lane, ranked by counting the entries that come before it
+        __syncwarp();
+        const bool has = lane < d;
+        const unsigned long long pi = has ? sh.p[lane] : 0ull;
+        const uint32_t ti = has ? sh.t[lane] : 0u;
+        uint32_t rank = 0;
+        bool tie = false;
+        for (uint32_t j = 0; j < d; ++j) {
+          const unsigned long long pj = __shfl_sync(0xffffffffu, pi, j);
+          rank += pj > pi ? 1u : 0u;
+          tie |= pj == pi && j != lane;
+        }
+        if (__any_sync(0xffffffffu, has && tie)) {
+          // equal priorities go by the partner's local id (the order hash is a bijection of the
+          // pair, so this is not expected within one list)
+          const uint32_t li = has ? b.sid[ti] - base : 0u;
+          for (uint32_t j = 0; j < d; ++j) {
+            const unsigned long long pj = __shfl_sync(0xffffffffu, pi, j);
+            const uint32_t lj = __shfl_sync(0xffffffffu, li, j);
+            rank += (pj == pi && j != lane && lj < li) ? 1u : 0u;
+          }
+        }
+        if (has) b.ovf[o + rank] = ti;
+        const uint32_t r0m = __ballot_sync(0xffffffffu, has && rank == 0u);
+        first = __shfl_sync(0xffffffffu, ti, __ffs(r0m) - 1);
+        __syncwarp();  // the next vertex reuses the shared list
+      } else if (in_smem) {
         __syncwarp();
         long_sort(b, sh, base, d, lane);
         for (uint32_t i = lane; i < d; i += 32) b.ovf[o + i] = sh.t[sh.ord[i]];
@@ -620,7 +651,7 @@ __global__ void __launch_bounds__(LONG_WARPS * 32) k_sweep_long(Bufs b, PairPara
       }
       if (lane == 0) {
         b.off[s] = (uint32_t)o;
-        b.wstate[s] = pack_state(first, 0u, b.species[b.sid[s]]);  // entry 0 of the list
+        b.wstate[s] = pack_state(first, 0u, sp);  // entry 0 of the list
       }
     }
     // every vertex of the batch is active (it has > SLAB pairs): one atomic per batch
