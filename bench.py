@@ -8,7 +8,10 @@ lat 15-40N with hourly frames, RK4 dt = 1 h, interaction radius 0.01 deg (1 km),
 
 One bench step = one CUDA-graph launch of 24 fused steps (one simulated day); K = 30 bench steps
 run the configuration's 720 steps. Between timed bench steps a 512 MiB buffer is written to flush
-the 129 MB L2. Timing uses CUDA events on the stream the library launches on.
+the 129 MB L2. Timing uses CUDA events on the stream the library launches on. Per-kernel times
+(CUDA events around plain launches) are reported for the first simulated day (`kernels`, which the
+roofline uses) and for four steps of the last one (`kernels_last_day`), when the flow has
+clustered the microbes.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -249,6 +252,21 @@ def run_gb300(args):
     step_bytes = 42.0 * n + 16.0 * pairs_per_step + 8.0 * g * 2
     whole = {"bytes_per_step": step_bytes, "gbs": step_bytes * sim_steps / (total_ms / 1e3) / 1e9}
 
+    # ---- the same per-kernel timing in the last simulated day: by then the flow has clustered the
+    # microbes (longer neighbour lists, longer dependency chains, a wider cell grid) ----
+    reset()
+    late_step = (K - 1) * spg
+    if late_step:
+        sim.run_graph(K - 1, sync=True)
+    sim.ctx.profile_enable(True)
+    sim.step(late_step * DT, DT, 4, step0=late_step)
+    prof_late = sim.ctx.profile()
+    st_late = sim.stats()
+    sim.ctx.profile_enable(False)
+    last_day = {"after_steps": late_step, "steps": 4, "long_lists": st_late["long_lists"], "cells": st_late["cells"],
+                "pairs": st_late["pairs"],
+                "us_per_launch": {k: 1e3 * ms / cnt for k, (ms, cnt) in prof_late.items() if cnt}}
+
     # ---- end to end through the public API from host buffers ----
     e2e = None
     if not args.no_e2e:
@@ -282,7 +300,7 @@ def run_gb300(args):
             "pairs_per_step": pairs_per_step,
             "plain": {"value": plain_value, "unit": "microbe-steps/s", "sim_steps": plain_steps,
                       "graph_speedup": value / world / plain_value},
-            "roofline": roofline, "whole_step": whole, "kernels": kernels,
+            "roofline": roofline, "whole_step": whole, "kernels": kernels, "kernels_last_day": last_day,
             "e2e": e2e, "cpu_baseline": cpu, "clocks": clk, "batched": batched, "adjoint": adjoint, "stress": stress,
             "distance_histogram": histogram,
             "gpu_launches": int(round(launches_per_step * K)),
