@@ -405,47 +405,58 @@ __global__ void __launch_bounds__(RS_THREADS) k_rs_hist(const uint32_t* __restri
   for (uint32_t d = threadIdx.x; d < R; d += RS_THREADS) hist[(size_t)d * tiles + blockIdx.x] = h[d];
 }
 
-// Stable scatter of one tile. Items are taken in index order (round r, warp w, lane l), so the rank
-// of an item among equal digits is (tile offset of the digit) + (earlier rounds) + (earlier warps
-// of this round) + (earlier lanes of its warp): the order of equal keys is preserved.
+// Stable scatter of one tile. Warp w takes the tile's w-th run of RS_ITEMS * 32 consecutive items
+// (RS_ITEMS rounds of 32) and ranks each item among the equal digits of its run with match masks and
+// a per-warp digit counter, without block barriers; the block then turns the counters into per-warp
+// digit offsets (the tile's offset of the digit plus the counts of the earlier warps), and each
+// item goes to its warp's offset plus its rank: equal keys keep their order.
 __global__ void __launch_bounds__(RS_THREADS) k_rs_scatter(const uint32_t* __restrict__ kin,
                                                            const uint32_t* __restrict__ vin,
                                                            uint32_t* __restrict__ kout, uint32_t* __restrict__ vout,
                                                            uint32_t m, int shift, int bits,
                                                            const uint32_t* __restrict__ hscan, uint32_t tiles) {
-  __shared__ uint32_t run[RS_RADIX_MAX];
   __shared__ uint32_t wcnt[RS_WARPS][RS_RADIX_MAX];
   const uint32_t R = 1u << bits, mask = R - 1u;
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-  for (uint32_t d = threadIdx.x; d < R; d += RS_THREADS) {
-    run[d] = hscan[(size_t)d * tiles + blockIdx.x];
+  for (uint32_t d = threadIdx.x; d < R; d += RS_THREADS)
     for (int w = 0; w < RS_WARPS; ++w) wcnt[w][d] = 0;
-  }
   __syncthreads();
-  const uint32_t base = blockIdx.x * RS_TILE;
+  const uint32_t base = blockIdx.x * RS_TILE + warp * (RS_ITEMS * 32u);
+  const uint32_t lt = (1u << lane) - 1u;
+  uint32_t kk[RS_ITEMS], rk[RS_ITEMS];
+#pragma unroll
   for (int r = 0; r < RS_ITEMS; ++r) {
-    const uint32_t i = base + (uint32_t)r * RS_THREADS + threadIdx.x;
+    const uint32_t i = base + (uint32_t)r * 32u + lane;
     const bool valid = i < m;
     const uint32_t k = valid ? kin[i] : 0u;
-    const uint32_t v = valid ? (vin ? vin[i] : i) : 0u;
     const uint32_t d = valid ? (k >> shift) & mask : R;
     const uint32_t peers = __match_any_sync(0xffffffffu, d);
-    const uint32_t below = peers & ((1u << lane) - 1u);
-    const bool leader = valid && below == 0;
-    if (leader) wcnt[warp][d] = (uint32_t)__popc(peers);
-    __syncthreads();
-    if (valid) {
-      uint32_t o = run[d] + (uint32_t)__popc(below);
-      for (uint32_t w = 0; w < warp; ++w) o += wcnt[w][d];
-      kout[o] = k;
-      vout[o] = v;
-    }
-    __syncthreads();
-    if (leader) {
-      atomicAdd(&run[d], (uint32_t)__popc(peers));
-      wcnt[warp][d] = 0;
-    }
+    const uint32_t below = peers & lt;
+    const uint32_t c = valid ? wcnt[warp][d] : 0u;  // every peer reads the count before the update
     __syncwarp();
+    if (valid && below == 0) wcnt[warp][d] = c + (uint32_t)__popc(peers);
+    __syncwarp();
+    kk[r] = k;
+    rk[r] = c + (uint32_t)__popc(below);
+  }
+  __syncthreads();
+  for (uint32_t d = threadIdx.x; d < R; d += RS_THREADS) {
+    uint32_t o = hscan[(size_t)d * tiles + blockIdx.x];
+    for (int w = 0; w < RS_WARPS; ++w) {
+      const uint32_t c = wcnt[w][d];
+      wcnt[w][d] = o;
+      o += c;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < RS_ITEMS; ++r) {
+    const uint32_t i = base + (uint32_t)r * 32u + lane;
+    if (i < m) {
+      const uint32_t o = wcnt[warp][(kk[r] >> shift) & mask] + rk[r];
+      kout[o] = kk[r];
+      vout[o] = vin ? vin[i] : i;
+    }
   }
 }
 
