@@ -373,6 +373,35 @@ def test_gpu_batched_beyond_one_tile_pass_equals_single_runs(engine, lm):
     bat.close()
 
 
+def test_gpu_batched_more_ensembles_than_the_ranking_block_equals_single_runs(engine, lm):
+    # 1,100 small dense ensembles: more than the one block that orders key ranges by density handles
+    # (1,024), so the key ranges stay in ensemble order; sampled ensembles against single runs
+    fld = lm.synthetic_psi_field(195.0, 206.0, 20.0, 31.0, 1.0 / 12.0, n_frames=5, frame_seconds=3600.0, seed=9)
+    rng = np.random.default_rng(23)
+    E = 1100
+    ens = []
+    for e in range(E):
+        n = int(rng.integers(30, 200))
+        side = rng.uniform(0.02, 0.1)
+        x0, y0 = rng.uniform(197.0, 204.0), rng.uniform(22.0, 29.0)
+        ens.append((x0 + side * rng.random(n), y0 + side * rng.random(n), rng.integers(1, 4, n).astype(np.int8)))
+    p = rng.uniform(0.5, 0.9, E)
+    seeds = rng.integers(1, 2**62, E)
+    bat = engine.EnsembleSimulation(fld, ens, radius=0.01, p_rs=p, p_pr=p, p_sp=p, seeds=seeds)
+    rec = bat.step(0.0, 3600.0, 3, record=True)
+    assert bat.stats()["pairs"] > 10_000
+    sp_e = bat.split(rec["species"])
+    lon_e = bat.split(rec["lon"])
+    for e in (0, 1, 517, 1023, 1024, 1099):
+        lons, lats, sp0 = ens[e]
+        one = engine.Simulation(fld, lons, lats, sp0, radius=0.01, p_rs=p[e], p_pr=p[e], p_sp=p[e], seed=int(seeds[e]))
+        r1 = one.step(0.0, 3600.0, 3, record=True)
+        np.testing.assert_array_equal(lon_e[e], r1["lon"], err_msg=f"ensemble {e}")
+        np.testing.assert_array_equal(sp_e[e], r1["species"], err_msg=f"ensemble {e}")
+        one.close()
+    bat.close()
+
+
 def test_gpu_batched_graph_equals_plain(engine, lm, orc):
     fields, ens, p, seeds = _batched_setup(lm, orc, E=7, seed=4)
     a = engine.EnsembleSimulation(fields, ens, radius=0.01, p_rs=p, p_pr=p, p_sp=p, seeds=seeds)
