@@ -418,13 +418,17 @@ __device__ void sort_segment(unsigned long long* __restrict__ pr, uint32_t* __re
 }
 
 // Long lists (more than SLAB neighbours): one warp per vertex. The warp reserves the overflow space
-// of 32 vertices at a time (one atomic per batch), gathers each vertex's neighbours with ballots
-// (lanes test 32 candidates of a row run at once) into shared memory, and orders the list there by
-// a bucket sort: the priorities are uniform 64-bit hashes, so 256 buckets on their top 8 bits
-// (descending) hold about d / 256 entries each, and an insertion sort inside each bucket by the
-// exact order (priority descending, partner's local id ascending) finishes it. Lists longer than
-// LONG_SMEM_MAX fall back to a sort in global memory by one lane. Only the sorted partners are
-// kept (the priorities were needed for the order only).
+// of all its vertices with one atomic; for each batch of 32 vertices lane k loads vertex k's cell,
+// position, key runs and ensemble constants, so the dependent loads happen once per batch. For
+// each vertex the warp then walks its six key runs as one candidate range, 64 candidates a pass
+// (position and id loaded together), and gathers the neighbours with ballots into shared memory.
+// The order (priority descending, partner's local id ascending) comes from:
+//   - up to 32 entries: a rank sort in registers, one entry per lane;
+//   - up to LONG_SMEM_MAX: a bucket sort. The priorities are uniform 64-bit hashes, so 256 buckets
+//     on their top 8 bits (descending) hold about d / 256 entries each, and an insertion sort
+//     inside each bucket by the exact order finishes it;
+//   - beyond: a sort in global memory by one lane.
+// Only the sorted partners are kept (the priorities were needed for the order only).
 constexpr int LONG_WARPS = 4;
 constexpr uint32_t LONG_SMEM_MAX = 512;
 constexpr uint32_t LONG_BUCKETS = 256;
