@@ -381,10 +381,9 @@ __global__ void __launch_bounds__(1024) k_cscan_down(Bufs b, Ctrl* ctrl) {
     __syncthreads();
   }
   if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {
-    uint32_t tot = 0;
-    for (int k = 0; k < SCAN_BLOCKS; ++k) tot += b.csum[k];
-    b.cstart[ncells] = tot;
-    ctrl->n_valid = tot;
+    // the last chunk ends the scan: its carry (the chunks before it plus its own) is the total
+    b.cstart[ncells] = carry;
+    ctrl->n_valid = carry;
   }
 }
 
