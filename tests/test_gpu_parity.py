@@ -234,6 +234,33 @@ def test_gpu_diffusion_kick_matches_philox(engine, lm, orc):
     sim.close()
 
 
+def test_gpu_diffusion_kick_statistics(engine, lm):
+    # particle_advecter.py:239-244: lat += U(-1, 1) * sqrt(6 |dt| Kh), then lon likewise. Over many
+    # microbes in a still field the kick has mean 0, variance amp^2 / 3, |kick| <= amp, and the two
+    # draws are uncorrelated (bounds: 5 standard errors).
+    fld = lm.uniform_field(190, 215, 15, 40, 0.5, n_frames=4, u0=0.0, v0=0.0)
+    n = 200_000
+    rng = np.random.default_rng(5)
+    lons = 200 + 5 * rng.random(n)
+    lats = 25 + 5 * rng.random(n)
+    kh = 100 / 1e10
+    sim = engine.Simulation(fld, lons, lats, None, radius=0.0, kh=kh, seed=1234)
+    sim.step(0.0, 3600.0, 1, interact=False)
+    lon, lat, _, _ = sim.state()
+    amp = float(np.sqrt(6 * 3600.0 * kh))
+    for dx in (lat.astype(np.float64) - lats.astype(np.float32).astype(np.float64),
+               lon.astype(np.float64) - lons.astype(np.float32).astype(np.float64)):
+        u = dx / amp
+        assert np.abs(u).max() <= 1.0 + 1e-3  # float32 rounding of the moved position
+        assert abs(u.mean()) < 5 * np.sqrt(1 / 3 / n)
+        # var(U^2) of U(-1, 1) is 4/45; the standard error of the variance estimate is sqrt(4/45/n)
+        assert abs(u.var() - 1 / 3) < 5 * np.sqrt(4 / 45 / n)
+    ulat = (lat.astype(np.float64) - lats.astype(np.float32)) / amp
+    ulon = (lon.astype(np.float64) - lons.astype(np.float32)) / amp
+    assert abs(np.corrcoef(ulat, ulon)[0, 1]) < 5 / np.sqrt(n)
+    sim.close()
+
+
 # ---------------- fused steps and graphs ----------------
 
 def _fused_setup(lm, orc, n=40000, seed=3):

@@ -28,6 +28,22 @@ def test_philox_known_answers(orc):
         assert list(orc.philox4x32_10(ctr, key)) == want
 
 
+def test_oracle_diffusion_draws_are_uniform(orc):
+    # the kick's two draws (lat, then lon) per microbe and step are U(-1, 1): range, mean 0,
+    # variance 1/3, no correlation between them or between neighbouring microbes (5 standard errors)
+    n = 20_000
+    d = np.array([orc.diffusion_draw(p, 7, 99) for p in range(n)], dtype=np.float64)
+    assert np.all(np.abs(d) <= 1.0)
+    for u in (d[:, 0], d[:, 1]):
+        assert abs(u.mean()) < 5 * np.sqrt(1 / 3 / n)
+        assert abs(u.var() - 1 / 3) < 5 * np.sqrt(4 / 45 / n)
+    assert abs(np.corrcoef(d[:, 0], d[:, 1])[0, 1]) < 5 / np.sqrt(n)
+    assert abs(np.corrcoef(d[:-1, 0], d[1:, 0])[0, 1]) < 5 / np.sqrt(n)
+    # another step draws afresh
+    e = np.array([orc.diffusion_draw(p, 8, 99)[0] for p in range(n)], dtype=np.float64)
+    assert abs(np.corrcoef(d[:, 0], e)[0, 1]) < 5 / np.sqrt(n)
+
+
 def test_factorization_matches_reference(lm, orc):
     g = golden("lattice.npz")
     for n, (a, b) in zip(g["ns"], g["factorization"]):
