@@ -127,19 +127,57 @@ class ParticleAdvecter:
             iteration += iters_to_do
         self.iteration += (end_time - start_time) // dt
 
-    def restore_from_disk(self) -> None:
-        """Reload the newest stored positions of every tile (the reference's re-entry restore)."""
-        files = sorted(glob.glob(os.path.join(self.output_dir, "particle_locations_*.pickle")))
+    def newest_stored_positions(self):
+        """The last stored row of every tile from the newest chunk on disk, and the iteration that
+        chunk ends at (the reference's re-entry restore, particle_advecter.py:124-138).
+
+        The reference takes the newest N_procs files by name; when a tile's file of the newest
+        chunk is missing, that mixes positions of different times. Here the newest chunk must hold
+        one readable file per tile with [iterations, particles per tile] positions; anything else
+        raises (FileNotFoundError for missing files, ValueError for unreadable or misshapen ones).
+        """
+        files = glob.glob(os.path.join(self.output_dir, "particle_locations_*.pickle"))
+        if not files:
+            raise FileNotFoundError(f"no particle_locations_*.pickle in {self.output_dir}")
+        chunks = {}
+        for path in files:
+            parts = os.path.basename(path)[: -len(".pickle")].split("_")
+            try:
+                i0, i1, tile_id = int(parts[2]), int(parts[3]), int(parts[4][4:])
+            except (IndexError, ValueError):
+                raise ValueError(f"not a chunk file name: {os.path.basename(path)}") from None
+            chunks.setdefault((i0, i1), {})[tile_id] = path
+        i0, i1 = max(chunks, key=lambda span: (span[1], span[0]))
+        tiles = chunks[(i0, i1)]
+        missing = [t for t in range(self.N_procs) if t not in tiles]
+        if missing:
+            raise FileNotFoundError(f"chunk {i0:05d}-{i1:05d} in {self.output_dir} has no file for tile(s) {missing}")
+        per = self.particles_per_tile
         lons = self._all_lons.copy()
         lats = self._all_lats.copy()
-        per = self.particles_per_tile
-        for path in files[-self.N_procs:]:
-            tile_id = int(os.path.basename(path).split("_")[4][4:6])
-            with open(path, "rb") as f:
-                chunk = pickle.load(f)
-            lons[tile_id * per:(tile_id + 1) * per] = chunk["lon"][-1, :]
-            lats[tile_id * per:(tile_id + 1) * per] = chunk["lat"][-1, :]
+        for tile_id in range(self.N_procs):
+            path = tiles[tile_id]
+            try:
+                with open(path, "rb") as f:
+                    chunk = pickle.load(f)
+                lon, lat = np.asarray(chunk["lon"]), np.asarray(chunk["lat"])
+            except Exception as e:  # truncated or corrupt pickle, or a dict without positions
+                raise ValueError(f"unreadable chunk file {path}: {type(e).__name__}: {e}") from e
+            if lon.ndim != 2 or lon.shape[1] != per or lat.shape != lon.shape or lon.shape[0] < 1:
+                raise ValueError(f"{path}: expected [iterations, {per}] positions, found lon {lon.shape}, "
+                                 f"lat {lat.shape}")
+            lons[tile_id * per:(tile_id + 1) * per] = lon[-1, :]
+            lats[tile_id * per:(tile_id + 1) * per] = lat[-1, :]
+        return lons, lats, i1
+
+    def restore_from_disk(self) -> int:
+        """Continue from the newest stored chunk (e.g. after the process that wrote it was killed):
+        upload its last positions and continue the iteration count where it ends. Returns that
+        iteration."""
+        lons, lats, it = self.newest_stored_positions()
         self._engine().upload_particles(lons, lats, None)
+        self.iteration = it
+        return it
 
     def create_netcdf_file(self, start_time, end_time, dt):
         iters = (end_time - start_time) // dt

@@ -84,3 +84,33 @@ def test_fused_engine_equals_two_phase(lm, orc, small_field, tmp_path):
     np.testing.assert_array_equal(rec["lat"].T, m["latitude"])
     np.testing.assert_array_equal(rec["species"].T, m["species"])
     sim.close()
+
+
+def test_killed_run_resumes_from_its_chunk_files(lm, orc, small_field, tmp_path):
+    # a run stopped after 10 h (its process gone, its chunk files kept) and resumed by a new
+    # ParticleAdvecter from the files ends where an uninterrupted run ends (within float32
+    # rounding of the stored positions, amplified by 10 more hours of flow)
+    import pickle
+    from lagrangian_microbes_gb300.particle_advecter import ParticleAdvecter, _chunk_name, uniform_particle_locations
+    start, dt = datetime(2017, 1, 1), timedelta(hours=1)
+    lons, lats = uniform_particle_locations(N_particles=4000, lat_min=25, lat_max=26, lon_min=200, lon_max=201)
+    mk = lambda d: ParticleAdvecter(lons, lats, N_procs=4, velocity_field=small_field, output_dir=str(tmp_path / d),
+                                    output_chunk_iters=5, Kh=0)
+    whole = mk("whole")
+    whole.time_step(start, start + 10 * dt, dt)
+    whole.time_step(start + 10 * dt, start + 20 * dt, dt)
+    first = mk("resumed")
+    first.time_step(start, start + 10 * dt, dt)
+    del first
+    again = mk("resumed")
+    assert again.restore_from_disk() == 10
+    again.time_step(start + 10 * dt, start + 20 * dt, dt)
+    for tile_id in range(4):
+        chunk = {}
+        for d in ("whole", "resumed"):
+            with open(os.path.join(str(tmp_path / d), _chunk_name(15, 20, tile_id)), "rb") as f:
+                chunk[d] = pickle.load(f)
+        a, b = chunk["whole"], chunk["resumed"]
+        dist = orc.great_circle_m(a["lon"][-1].astype(np.float64), a["lat"][-1].astype(np.float64),
+                                  b["lon"][-1].astype(np.float64), b["lat"][-1].astype(np.float64))
+        assert dist.max() <= 10.0, (tile_id, dist.max())

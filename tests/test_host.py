@@ -110,6 +110,73 @@ def test_particle_advecter_argument_checks(lm, tmp_path):
         distribute_particles_across_tiles(lons, lats, 5)
 
 
+def _write_chunks(pa, spans, rng):
+    import pickle
+    from lagrangian_microbes_gb300.particle_advecter import _chunk_name
+    rows = {}
+    for i0, i1 in spans:
+        for tile_id in range(pa.N_procs):
+            lon = rng.random((i1 - i0, pa.particles_per_tile)).astype(np.float32) + 200
+            lat = rng.random((i1 - i0, pa.particles_per_tile)).astype(np.float32) + 25
+            with open(os.path.join(pa.output_dir, _chunk_name(i0, i1, tile_id)), "wb") as f:
+                pickle.dump({"time": list(range(i0, i1)), "lat": lat, "lon": lon}, f)
+            rows[(i0, i1, tile_id)] = (lon[-1], lat[-1])
+    return rows
+
+
+def test_restore_reads_the_newest_complete_chunk(lm, tmp_path):
+    # the resume path after a killed run (particle_advecter.py:124-138): the last row of every tile
+    # of the newest chunk, and the iteration it ends at
+    from lagrangian_microbes_gb300.particle_advecter import ParticleAdvecter
+    fld = lm.uniform_field(195, 206, 20, 31, 0.25, 4)
+    pa = ParticleAdvecter(np.linspace(200, 201, 12), np.linspace(25, 26, 12), N_procs=3, velocity_field=fld,
+                          output_dir=str(tmp_path))
+    rows = _write_chunks(pa, [(0, 5), (5, 10), (10, 12)], np.random.default_rng(1))
+    lons, lats, it = pa.newest_stored_positions()
+    assert it == 12
+    for t in range(3):
+        np.testing.assert_array_equal(lons[4 * t:4 * t + 4], rows[(10, 12, t)][0])
+        np.testing.assert_array_equal(lats[4 * t:4 * t + 4], rows[(10, 12, t)][1])
+
+
+def test_restore_rejects_missing_corrupt_and_misshapen_checkpoints(lm, tmp_path):
+    import pickle
+    from lagrangian_microbes_gb300.particle_advecter import ParticleAdvecter, _chunk_name
+    fld = lm.uniform_field(195, 206, 20, 31, 0.25, 4)
+    mk = lambda d: ParticleAdvecter(np.linspace(200, 201, 12), np.linspace(25, 26, 12), N_procs=3,
+                                    velocity_field=fld, output_dir=str(tmp_path / d))
+    with pytest.raises(FileNotFoundError):  # nothing stored yet
+        mk("empty").newest_stored_positions()
+    # a tile file of the newest chunk is missing: an error, not the older chunk's row for that tile
+    pa = mk("missing")
+    _write_chunks(pa, [(0, 5), (5, 10)], np.random.default_rng(2))
+    os.remove(os.path.join(pa.output_dir, _chunk_name(5, 10, 1)))
+    with pytest.raises(FileNotFoundError, match=r"tile\(s\) \[1\]"):
+        pa.newest_stored_positions()
+    # a truncated file (a write cut short when the process was killed)
+    pa = mk("truncated")
+    _write_chunks(pa, [(0, 5)], np.random.default_rng(3))
+    path = os.path.join(pa.output_dir, _chunk_name(0, 5, 2))
+    with open(path, "rb") as f:
+        data = f.read()
+    with open(path, "wb") as f:
+        f.write(data[: len(data) // 2])
+    with pytest.raises(ValueError, match="unreadable"):
+        pa.newest_stored_positions()
+    # positions of the wrong shape, and a file that is not a chunk of this run's name pattern
+    pa = mk("shape")
+    _write_chunks(pa, [(0, 5)], np.random.default_rng(4))
+    with open(os.path.join(pa.output_dir, _chunk_name(0, 5, 0)), "wb") as f:
+        pickle.dump({"time": [], "lat": np.zeros((5, 3), np.float32), "lon": np.zeros((5, 3), np.float32)}, f)
+    with pytest.raises(ValueError, match="expected"):
+        pa.newest_stored_positions()
+    pa = mk("name")
+    _write_chunks(pa, [(0, 5)], np.random.default_rng(5))
+    open(os.path.join(pa.output_dir, "particle_locations_x_y_tilez.pickle"), "wb").close()
+    with pytest.raises(ValueError, match="not a chunk file name"):
+        pa.newest_stored_positions()
+
+
 def test_velocity_field_descending_latitude_is_flipped(lm):
     lon = np.array([0.0, 1.0, 2.0])
     lat = np.array([2.0, 1.0])
