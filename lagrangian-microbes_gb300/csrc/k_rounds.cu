@@ -36,7 +36,11 @@
 
 namespace lm {
 
-constexpr int RD_THREADS = 256;
+// 512 threads: two blocks per SM hold 2 x 2,048 vertices in 2 x 96 KB of shared memory. Against
+// four blocks of 256 (the same vertices per SM) a block's range has a shorter edge for its area,
+// so fewer pairs hand off through global memory (at 256 ensembles: 11.6 -> 10.4 ms per step;
+// 1,024 threads were faster there still but slower on the clustered 490k lattice).
+constexpr int RD_THREADS = 512;
 constexpr unsigned long long ROUNDS_TIMEOUT_NS = 2000000000ull;  // 2 s
 
 __device__ __forceinline__ unsigned long long globaltimer() {
@@ -126,7 +130,7 @@ constexpr int POLL_BATCH = 4;  // vertices whose state words one thread loads be
 // ---- tile-local interaction: block-owned vertex ranges with handshakes in shared memory ----
 //
 // Cell keys are tile-major, so a contiguous range of cell-ordered vertices is a compact 2D patch.
-// Block b owns the vertices [b V, b V + V) (V = 256 x up to TL_VPT) and keeps their state words,
+// Block b owns the vertices [b V, b V + V) (V = RD_THREADS x up to TL_VPT) and keeps their state words,
 // slot ids, degrees and list entries in shared memory. A pair whose two microbes the block owns
 // hands off through shared memory (tens of cycles instead of an L2 round trip); a pair that
 // crosses blocks goes through the global state words: the vertex's word is published there while
@@ -188,7 +192,7 @@ __device__ __forceinline__ void rps_pair(const Bufs& b, uint32_t vertex, uint32_
 }
 
 // The pairs among cell-order vertices [g_lo, g_hi) (a group of whole ensembles, so no pair leaves
-// it), at most TL_VMAX per block: each block owns an equal share of whole 256-vertex columns.
+// it), at most TL_VMAX per block: each block owns an equal share of whole RD_THREADS-vertex columns.
 __device__ void tl_group(const Bufs& b, uint32_t step, Ctrl* ctrl, unsigned long long t0, uint32_t g_lo,
                          uint32_t g_hi) {
   extern __shared__ unsigned long long tl_raw[];
