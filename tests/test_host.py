@@ -27,6 +27,33 @@ def test_library_builds_and_exports_every_declared_symbol(lm):
     assert lib.lm_version() == 1
 
 
+def _header_text():
+    with open(os.path.join(REPO, "include", "lm_api.h")) as f:
+        return re.sub(r"/\*.*?\*/", "", f.read(), flags=re.S)
+
+
+def test_python_binding_matches_the_header(lm):
+    # every declared entry is bound with as many arguments as the header declares (no drift
+    # between include/lm_api.h and the ctypes binding)
+    from lagrangian_microbes_gb300 import _lib
+    protos = {}
+    for m in re.finditer(r"^int\s+(lm_\w+)\s*\((.*?)\)\s*;", _header_text(), flags=re.M | re.S):
+        args = m.group(2).strip()
+        protos[m.group(1)] = 0 if args in ("", "void") else len(args.split(","))
+    assert set(protos) == set(_lib.SIGNATURES), sorted(set(protos) ^ set(_lib.SIGNATURES))
+    for name, argtypes in _lib.SIGNATURES.items():
+        assert len(argtypes) == protos[name], name
+
+
+def test_stats_struct_matches_the_header(lm):
+    from lagrangian_microbes_gb300 import _lib
+    body = re.search(r"typedef struct lm_stats \{(.*?)\} lm_stats;", _header_text(), flags=re.S).group(1)
+    fields = re.findall(r"int64_t\s+(\w+)(?:\[(\d+)\])?;", body)
+    assert [(n, int(k or 1)) for n, k in fields] == [
+        (n, getattr(t, "_length_", 1)) for n, t in _lib.Stats._fields_]
+    assert ctypes.sizeof(_lib.Stats) == 8 * sum(int(k or 1) for _, k in fields)
+
+
 def test_library_has_sm103a_code(lm):
     from lagrangian_microbes_gb300 import build
     with open(build.LIB_PATH, "rb") as f:
