@@ -70,6 +70,15 @@ def test_stats_struct_matches_the_header(lm):
     assert ctypes.sizeof(_lib.Stats) == 8 * sum(int(k or 1) for _, k in fields)
 
 
+def test_missing_library_fails_loudly(lm, monkeypatch, tmp_path):
+    # no CPU fallback: without the CUDA library every entry point raises
+    from lagrangian_microbes_gb300 import _lib
+    monkeypatch.setattr(_lib, "_lib", None)
+    monkeypatch.setattr(_lib._build, "LIB_PATH", str(tmp_path / "liblmgb300.so"))
+    with pytest.raises(_lib.LMError, match="missing"):
+        _lib.load(build_if_missing=False)
+
+
 def test_library_has_sm103a_code(lm):
     from lagrangian_microbes_gb300 import build
     with open(build.LIB_PATH, "rb") as f:
