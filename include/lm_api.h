@@ -76,6 +76,9 @@ typedef struct lm_stats {
 } lm_stats;
 
 int lm_version(void);
+/* SM architecture of the library's kernels as the CUDA runtime reports it for the current device
+ * (cudaFuncAttributes::binaryVersion: 103 for sm_103a). LM_ERR_CUDA when no GPU can load them. */
+int lm_kernel_arch(int* sm);
 
 /* Create a context on CUDA device `device` with its own non-blocking stream. */
 int lm_ctx_create(int device, lm_ctx** out);
@@ -204,18 +207,22 @@ int lm_profile_get(lm_ctx* ctx, int kernel, char* name, size_t name_len, double*
 int lm_profile_count(void);
 
 /* Pair counting for callers that cannot allocate device memory (no counterpart in the reference;
- * it has no GPU path). Some callers may not call cudaMalloc/cudaFree at all: code running inside
- * another library's stream capture, hosts that give all device memory to their own pool, plugins
- * whose process forbids allocation after start-up. They pass device pointers: d_lon, d_lat
- * (float32[n]) in, d_degree (int32[n], neighbours of each point) and d_pairs (one uint64, the
- * number of unordered pairs, the size of cKDTree.query_pairs) out, all written on `stream` (a
- * cudaStream_t as an integer, 0 = default stream). Pair semantics are lm_query_pairs'.
+ * it has no GPU path). Some callers may not call cudaMalloc/cudaFree at all: hosts that give all
+ * device memory to their own pool allocator, plugins whose process forbids device allocation after
+ * start-up, latency-bound loops that cannot afford the device-wide synchronisation of cudaFree.
+ * They pass device pointers: d_lon, d_lat (float32[n]) in, d_degree (int32[n], neighbours of each
+ * point) and d_pairs (one uint64, the number of unordered pairs, the size of
+ * cKDTree.query_pairs) out, all written on `stream` (a cudaStream_t as an integer, 0 = default
+ * stream). Pair semantics are lm_query_pairs'.
  * Nothing is allocated: the scratch is a fixed ~1.8 MB array inside the library that every GPU
  * loading it keeps until the process exits, so n is limited to 65536 (larger n: LM_ERR_ARG).
- * The first call on a device looks up that array's device address; make that first call before
- * any stream capture. All calls share the array and it keeps the last call's contents, so calls
- * whose work overlaps on the GPU (other streams, other threads) race: serialise them.
- * Errors: lm_last_error(NULL, ...). */
+ * The first call on a device, with that device current, looks up that array's device address and
+ * loads the function's kernels; make that first call before any stream capture. The address is
+ * kept for the life of the process and belongs to the device's primary context: after
+ * cudaDeviceReset it is stale, so do not call this function again in that process. All calls
+ * share the array and it keeps the last call's contents (each call clears what must start at
+ * zero), so calls whose work overlaps on the GPU (other streams, other threads) race: serialise
+ * them. Errors: lm_last_error(NULL, ...). */
 int lm_count_pairs_noalloc(const float* d_lon, const float* d_lat, int64_t n, double radius, int norm,
                            int32_t* d_degree, unsigned long long* d_pairs, uintptr_t stream);
 

@@ -95,6 +95,7 @@ F64 = ctypes.c_double
 # name -> argtypes (all return int status)
 SIGNATURES = {
     "lm_version": [],
+    "lm_kernel_arch": [ctypes.POINTER(I32)],
     "lm_ctx_create": [I32, ctypes.POINTER(P)],
     "lm_ctx_destroy": [P],
     "lm_last_error": [P, ctypes.c_char_p, ctypes.c_size_t],

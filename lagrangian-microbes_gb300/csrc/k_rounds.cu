@@ -24,7 +24,7 @@
 // always ready, so the loop always progresses; every wait is still bounded (error flag + return
 // after a timeout).
 //
-// When every block can own its share of the vertices in shared memory (up to 1,024 each), the
+// When every block can own its share of the vertices in shared memory (up to 2,048 each), the
 // pairs are applied by the tile-local path (rounds_tiled): handshakes between vertices of one
 // block go through shared memory and only pairs crossing blocks through global memory.
 //
@@ -504,6 +504,8 @@ __global__ void __launch_bounds__(SLOT_BLOCK) k_census(Bufs b, Ctrl* ctrl) {
     atomicAdd(&ctrl->census[threadIdx.x], h[threadIdx.x]);
   }
 }
+
+const void* lm_census_kernel() { return (const void*)k_census; }
 
 void launch_census(const Bufs& b, Ctrl* ctrl, cudaStream_t st) {
   if (b.nslots == 0) return;

@@ -525,23 +525,7 @@ int check_time(lm_ctx* c, double t, double dt, int64_t n_steps) {
   return LM_OK;
 }
 
-void set_pair_params(lm_ctx* c, double r, int norm) {
-  PairParams& pp = c->pp;
-  pp.r = r;
-  pp.r2 = r * r;
-  pp.norm = norm;
-  const double band = 2e-6;
-  if (r > 1e-15 && r < 1e15) {
-    pp.r2f_lo = std::nextafter((float)(pp.r2 * (1 - band)), 0.f);
-    pp.r2f_hi = std::nextafter((float)(pp.r2 * (1 + band)), INFINITY);
-    pp.rf_lo = std::nextafter((float)(r * (1 - band)), 0.f);
-    pp.rf_hi = std::nextafter((float)(r * (1 + band)), INFINITY);
-  } else {  // float32 cannot represent the band: decide every candidate in float64
-    pp.r2f_lo = pp.rf_lo = -1.f;
-    pp.r2f_hi = pp.rf_hi = INFINITY;
-  }
-  pp.cell_factor = (float)c->cell_factor;
-}
+void set_pair_params(lm_ctx* c, double r, int norm) { c->pp = make_pair_params(r, norm, (float)c->cell_factor); }
 
 // Copies of one step's records into caller-order host arrays.
 int record_step(lm_ctx* c, int64_t k, float* rec_lon, float* rec_lat, int8_t* rec_species) {
@@ -668,6 +652,22 @@ int check_ready(lm_ctx* c, uint32_t flags) {
 extern "C" {
 
 int lm_version(void) { return LM_API_VERSION; }
+
+int lm_kernel_arch(int* sm) {
+  if (!sm) {
+    set_thread_error("NULL argument");
+    return LM_ERR_ARG;
+  }
+  cudaFuncAttributes fa;
+  const cudaError_t e = cudaFuncGetAttributes(&fa, (const void*)lm_census_kernel());
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    set_thread_error(cudaGetErrorString(e));
+    return LM_ERR_CUDA;
+  }
+  *sm = fa.binaryVersion;
+  return LM_OK;
+}
 
 int lm_ctx_create(int device, lm_ctx** out) {
   if (!out) return fail(nullptr, LM_ERR_ARG, "out is NULL");

@@ -21,6 +21,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cmath>
 #include <utility>
 
 struct lm_ctx;
@@ -154,6 +155,30 @@ struct PairParams {
   int norm;           // 1, 2 or 0 (= infinity)
 };
 
+// Pair-test parameters of radius r and norm code `norm` (lm_api.h). A float32 pre-test decides
+// every candidate whose distance lies outside a relative band of 2e-6 around r (float32 error
+// < 3e-7 relative); candidates inside the band are re-decided in float64. Radii float32 cannot
+// resolve get an empty float32 range: every candidate is then decided in float64. Shared by every
+// entry point that tests pairs, so all of them draw the same boundary.
+inline PairParams make_pair_params(double r, int norm, float cell_factor) {
+  PairParams pp{};
+  pp.r = r;
+  pp.r2 = r * r;
+  pp.norm = norm;
+  const double band = 2e-6;
+  if (r > 1e-15 && r < 1e15) {
+    pp.r2f_lo = std::nextafter((float)(pp.r2 * (1 - band)), 0.f);
+    pp.r2f_hi = std::nextafter((float)(pp.r2 * (1 + band)), INFINITY);
+    pp.rf_lo = std::nextafter((float)(r * (1 - band)), 0.f);
+    pp.rf_hi = std::nextafter((float)(r * (1 + band)), INFINITY);
+  } else {
+    pp.r2f_lo = pp.rf_lo = -1.f;
+    pp.r2f_hi = pp.rf_hi = INFINITY;
+  }
+  pp.cell_factor = cell_factor;
+  return pp;
+}
+
 struct StepArgs {
   double t_start;     // time of step step0 (seconds, field clock)
   double dt;          // step length (seconds)
@@ -265,6 +290,7 @@ void launch_sweep_long(const Bufs& b, const PairParams& pp, const StepArgs& a, C
 int rounds_grid(int device, int* block);
 cudaError_t launch_rounds(const Bufs& b, const StepArgs& a, Ctrl* ctrl, int grid, int block, cudaStream_t st);
 void launch_census(const Bufs& b, Ctrl* ctrl, cudaStream_t st);
+const void* lm_census_kernel();  // one kernel of the library, for attribute queries
 void launch_unpad(const float* src, float* dst, const int32_t* map, uint32_t nslots, cudaStream_t st);
 void launch_unpad8(const int8_t* src, int8_t* dst, const int32_t* map, uint32_t nslots, cudaStream_t st);
 

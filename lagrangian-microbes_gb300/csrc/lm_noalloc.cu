@@ -1,11 +1,11 @@
 // Fixed-radius pair counting that allocates no memory: lm_count_pairs_noalloc (include/lm_api.h).
 //
-// Who needs it: callers that must not call cudaMalloc or cudaFree, for example code running
-// between the start and end of someone else's CUDA stream capture, a host that has handed all
-// device memory to its own pool, or a plugin whose host process forbids allocation after start-up.
-// They pass device pointers for inputs and outputs; everything else the kernels need lives in
-// NA_SCRATCH below, a file-scope __device__ array that every GPU loading this library holds
-// until the process exits.
+// Who needs it: callers that must not call cudaMalloc or cudaFree, for example a host that has
+// handed all device memory to its own pool allocator, a plugin whose host process forbids device
+// allocation after start-up, or a latency-bound loop that cannot afford the device-wide
+// synchronisation cudaFree implies. They pass device pointers for inputs and outputs; everything
+// else the kernels need lives in NA_SCRATCH below, a file-scope __device__ array that every GPU
+// loading this library holds until the process exits.
 //
 // The counting follows the same pair semantics as lm_query_pairs (cKDTree.query_pairs, inclusive
 // Minkowski-p on float32 lon/lat promoted to float64) in five small launches on the caller's
@@ -265,6 +265,10 @@ int na_fail(int code, const char* msg) {
 
 // Device address of NA_SCRATCH, looked up once per device with that device current. In host code
 // the symbol NA_SCRATCH is only a stand-in, never a device address, so kernels get this pointer.
+// The same first call also loads all five kernels (with lazy module loading a kernel is otherwise
+// loaded at its first launch, and a first call with n = 0 launches only one of them), so every
+// later call only enqueues launches. The address is kept for the life of the process: it belongs
+// to the device's primary context and is not valid after that context is reset (cudaDeviceReset).
 unsigned char* na_scratch_for(int device, int* rc) {
   static std::mutex mu;
   static unsigned char* addr[64] = {};
@@ -276,7 +280,12 @@ unsigned char* na_scratch_for(int device, int* rc) {
   std::lock_guard<std::mutex> lock(mu);
   if (!addr[device]) {
     void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, lm::NA_SCRATCH);
+    cudaError_t e = cudaGetSymbolAddress(&p, lm::NA_SCRATCH);
+    cudaFuncAttributes fa;
+    const void* kernels[] = {(const void*)lm::k_na_prepare, (const void*)lm::k_na_keys, (const void*)lm::k_na_scan,
+                             (const void*)lm::k_na_scatter, (const void*)lm::k_na_count};
+    for (const void* k : kernels)
+      if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k);
     if (e != cudaSuccess) {
       cudaGetLastError();
       *rc = na_fail(LM_ERR_CUDA, cudaGetErrorString(e));
@@ -307,20 +316,7 @@ extern "C" int lm_count_pairs_noalloc(const float* d_lon, const float* d_lat, in
   int rc = LM_OK;
   unsigned char* base = na_scratch_for(device, &rc);
   if (!base) return rc;
-  PairParams pp{};
-  pp.r = radius;
-  pp.r2 = radius * radius;
-  pp.norm = norm;
-  const double band = 2e-6;
-  if (radius > 1e-15 && radius < 1e15) {
-    pp.r2f_lo = std::nextafter((float)(pp.r2 * (1 - band)), 0.f);
-    pp.r2f_hi = std::nextafter((float)(pp.r2 * (1 + band)), INFINITY);
-    pp.rf_lo = std::nextafter((float)(radius * (1 - band)), 0.f);
-    pp.rf_hi = std::nextafter((float)(radius * (1 + band)), INFINITY);
-  } else {
-    pp.r2f_lo = pp.rf_lo = -1.f;
-    pp.r2f_hi = pp.rf_hi = INFINITY;
-  }
+  const PairParams pp = make_pair_params(radius, norm, 1.0f);
   const cudaStream_t st = (cudaStream_t)stream;
   const NaView v = view_of(base);
   const uint32_t un = (uint32_t)n;

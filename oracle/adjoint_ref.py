@@ -50,9 +50,36 @@ class Grid:
         self.dT = float((t_axis[-1] - t_axis[0]) / (self.nt - 1))
 
 
-def _bilinear(F, j, i, a, b):
-    return ((1 - a) * (1 - b) * F[j, i] + a * (1 - b) * F[j, i + 1] + (1 - a) * b * F[j + 1, i]
-            + a * b * F[j + 1, i + 1])
+class _Gather(torch.autograd.Function):
+    """F.flat[q] for a field F [nt][ny][nx]. Its backward adds the incoming gradient at the sampled
+    nodes straight into `sink` (the field's gradient buffer, allocated once per run by advect()),
+    the definition of a gather's adjoint, and returns no tensor for F: torch would otherwise build
+    a dense field-sized gradient for every lookup, and a 720-step run makes ~10^4 of them."""
+
+    @staticmethod
+    def forward(ctx, F, q, sink):
+        ctx.save_for_backward(q)
+        ctx.sink = sink
+        return F.reshape(-1)[q]
+
+    @staticmethod
+    def backward(ctx, g):
+        (q,) = ctx.saved_tensors
+        ctx.sink.view(-1).index_add_(0, q, g)
+        return None, None, None
+
+
+def _node(F, q):
+    sink = getattr(F, "_grad_sink", None)
+    if sink is None or not torch.is_grad_enabled():
+        return F.detach().reshape(-1)[q] if sink is not None else F.reshape(-1)[q]
+    return _Gather.apply(F, q, sink)
+
+
+def _bilinear(F, q, nx, a, b):
+    """Bilinear interpolation in the cell whose south-west node has flat index q."""
+    return ((1 - a) * (1 - b) * _node(F, q) + a * (1 - b) * _node(F, q + 1) + (1 - a) * b * _node(F, q + nx)
+            + a * b * _node(F, q + nx + 1))
 
 
 def velocity(g: Grid, u, v, k: int, w: float, x, y):
@@ -66,11 +93,13 @@ def velocity(g: Grid, u, v, k: int, w: float, x, y):
     j = fyc.detach().floor().long().clamp(max=g.ny - 2)
     a = fxc - i
     b = fyc - j
-    U = _bilinear(u[k], j, i, a, b)
-    V = _bilinear(v[k], j, i, a, b)
+    q = (k * g.ny + j) * g.nx + i
+    U = _bilinear(u, q, g.nx, a, b)
+    V = _bilinear(v, q, g.nx, a, b)
     if w != 0.0:
-        U = (1 - w) * U + w * _bilinear(u[k + 1], j, i, a, b)
-        V = (1 - w) * V + w * _bilinear(v[k + 1], j, i, a, b)
+        q1 = q + g.ny * g.nx
+        U = (1 - w) * U + w * _bilinear(u, q1, g.nx, a, b)
+        V = (1 - w) * V + w * _bilinear(v, q1, g.nx, a, b)
     dlon = U / (M_PER_DEG * torch.cos(y * (math.pi / 180.0)))
     dlat = V / M_PER_DEG
     return dlon, dlat, inside
@@ -100,6 +129,12 @@ def advect(lon_axis, lat_axis, t_axis, u, v, lon0, lat0, t_start: float, dt: flo
            checkpoint_every: int = 32):
     """Differentiable FP64 forward: final (lon, lat) of microbes starting at (lon0, lat0)."""
     g = Grid(lon_axis, lat_axis, t_axis)
+    for F in (u, v):
+        # the field gradient accumulates in F.grad through _Gather (see there); leaves only
+        if F.requires_grad:
+            if F.grad is None:
+                F.grad = torch.zeros_like(F)
+            F._grad_sink = F.grad
     x, y = lon0, lat0
     active = torch.isfinite(x) & torch.isfinite(y)
     for m0 in range(0, n_steps, checkpoint_every):

@@ -15,7 +15,9 @@
  *       finite differences (no reference counterpart: the reference does not differentiate); it
  *       can fold the grid cells of every stage evaluation into a per-particle signature, so that a
  *       difference quotient whose two runs sample different cells (straddling an edge of the
- *       piecewise-bilinear field, where the derivative jumps) is recognised and left out.
+ *       piecewise-bilinear field, where the derivative jumps) is recognised and left out;
+ *       orc_advect_f64d_dir runs it on the field moved along an int8 direction, u + s du, without
+ *       a field-sized float64 copy per difference.
  *   orc_pairs        : cKDTree(X).query_pairs(r, p) (interaction_simulator.py:93-98): all i < j with
  *       Minkowski-p distance <= r on float32 positions promoted to float64; for p = 2 the test is
  *       fl(fl(dx*dx) + fl(dy*dy)) <= fl(r*r) (no FMA; this file must be compiled with
@@ -172,8 +174,8 @@ int64_t orc_advect_f64(const orc_field* f, int64_t n, double* lon, double* lat, 
 
 /* The same FP64 scheme on an FP64 field (finite differences along u, v directions need
  * perturbations far below float32 resolution). Stage brackets as bracket(); one thread per particle. */
-static int vel64d(const orc_field64* f, int k, double w, double x, double y, double* dlon, double* dlat,
-                  uint64_t* sig) {
+static int vel64d(const orc_field64* f, const int8_t* du, const int8_t* dv, double s, int k, double w, double x,
+                  double y, double* dlon, double* dlat, uint64_t* sig) {
   double fx = (x - f->lon0) / f->dlon, fy = (y - f->lat0) / f->dlat;
   if (!(fx >= 0 && fx <= f->nx - 1 && fy >= 0 && fy <= f->ny - 1)) return 0;
   int i = (int)fx, j = (int)fy;
@@ -189,8 +191,14 @@ static int vel64d(const orc_field64* f, int k, double w, double x, double y, dou
     double wt = fr == 0 ? 1.0 - w : w;
     if (wt == 0.0) continue;
     size_t q = base + fr * nxny;
-    u += wt * (w00 * f->u[q] + w01 * f->u[q + 1] + w10 * f->u[q + f->nx] + w11 * f->u[q + f->nx + 1]);
-    v += wt * (w00 * f->v[q] + w01 * f->v[q + 1] + w10 * f->v[q + f->nx] + w11 * f->v[q + f->nx + 1]);
+    double u00 = f->u[q], u01 = f->u[q + 1], u10 = f->u[q + f->nx], u11 = f->u[q + f->nx + 1];
+    double v00 = f->v[q], v01 = f->v[q + 1], v10 = f->v[q + f->nx], v11 = f->v[q + f->nx + 1];
+    if (du) { /* the field moved along an int8 direction: u + s du (finite differences) */
+      u00 += s * du[q], u01 += s * du[q + 1], u10 += s * du[q + f->nx], u11 += s * du[q + f->nx + 1];
+      v00 += s * dv[q], v01 += s * dv[q + 1], v10 += s * dv[q + f->nx], v11 += s * dv[q + f->nx + 1];
+    }
+    u += wt * (w00 * u00 + w01 * u01 + w10 * u10 + w11 * u11);
+    v += wt * (w00 * v00 + w01 * v01 + w10 * v10 + w11 * v11);
   }
   *dlon = u / (1852.0 * 60.0 * cos(y * M_PI / 180.0));
   *dlat = v / (1852.0 * 60.0);
@@ -199,6 +207,12 @@ static int vel64d(const orc_field64* f, int k, double w, double x, double y, dou
 
 int64_t orc_advect_f64d(const orc_field64* f, int64_t n, double* lon, double* lat, uint8_t* status, double t0,
                         double dt, int n_steps, int n_threads, uint64_t* cell_sig) {
+  return orc_advect_f64d_dir(f, NULL, NULL, 0.0, n, lon, lat, status, t0, dt, n_steps, n_threads, cell_sig);
+}
+
+int64_t orc_advect_f64d_dir(const orc_field64* f, const int8_t* du, const int8_t* dv, double s_dir, int64_t n,
+                            double* lon, double* lat, uint8_t* status, double t0, double dt, int n_steps, int n_threads,
+                            uint64_t* cell_sig) {
   const orc_field fk = {NULL, NULL, f->nx, f->ny, f->nt, f->lon0, f->dlon, f->lat0, f->dlat, f->t0, f->dT};
   int64_t bad = 0;
 #ifdef _OPENMP
@@ -219,10 +233,10 @@ int64_t orc_advect_f64d(const orc_field64* f, int64_t n, double* lon, double* la
       double x = lon[p], y = lat[p];
       double k1x, k1y, k2x, k2y, k3x, k3y, k4x, k4y;
       uint64_t sg = cell_sig ? cell_sig[p] : 0;
-      int ok = vel64d(f, k[0], w[0], x, y, &k1x, &k1y, &sg) &&
-               vel64d(f, k[1], w[1], x + 0.5 * dt * k1x, y + 0.5 * dt * k1y, &k2x, &k2y, &sg) &&
-               vel64d(f, k[1], w[1], x + 0.5 * dt * k2x, y + 0.5 * dt * k2y, &k3x, &k3y, &sg) &&
-               vel64d(f, k[2], w[2], x + dt * k3x, y + dt * k3y, &k4x, &k4y, &sg);
+      int ok = vel64d(f, du, dv, s_dir, k[0], w[0], x, y, &k1x, &k1y, &sg) &&
+               vel64d(f, du, dv, s_dir, k[1], w[1], x + 0.5 * dt * k1x, y + 0.5 * dt * k1y, &k2x, &k2y, &sg) &&
+               vel64d(f, du, dv, s_dir, k[1], w[1], x + 0.5 * dt * k2x, y + 0.5 * dt * k2y, &k3x, &k3y, &sg) &&
+               vel64d(f, du, dv, s_dir, k[2], w[2], x + dt * k3x, y + dt * k3y, &k4x, &k4y, &sg);
       if (cell_sig) cell_sig[p] = sg;
       if (ok) {
         lon[p] = x + (k1x + 2 * k2x + 2 * k3x + k4x) * dt / 6.0;

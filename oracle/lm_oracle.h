@@ -33,6 +33,9 @@ int64_t orc_advect_f64(const orc_field* f, int64_t n, double* lon, double* lat, 
                        double dt, int n_steps, double* rec_lon, double* rec_lat);
 int64_t orc_advect_f64d(const orc_field64* f, int64_t n, double* lon, double* lat, uint8_t* status, double t0,
                         double dt, int n_steps, int n_threads, uint64_t* cell_sig);
+int64_t orc_advect_f64d_dir(const orc_field64* f, const int8_t* du, const int8_t* dv, double s, int64_t n, double* lon,
+                            double* lat, uint8_t* status, double t0, double dt, int n_steps, int n_threads,
+                            uint64_t* cell_sig);
 int64_t orc_advect_f32(const orc_field* f, int64_t n, float* lon, float* lat, uint8_t* status, double t0, double dt,
                        int n_steps, int n_threads);
 

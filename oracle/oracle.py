@@ -64,6 +64,7 @@ def lib():
             "orc_advect_f64": (I64, [P, I64, P, P, P, F64, F64, I, P, P]),
             "orc_advect_f32": (I64, [P, I64, P, P, P, F64, F64, I, I]),
             "orc_advect_f64d": (I64, [P, I64, P, P, P, F64, F64, I, I, P]),
+            "orc_advect_f64d_dir": (I64, [P, P, P, F64, I64, P, P, P, F64, F64, I, I, P]),
             "orc_pairs": (I64, [I64, P, P, F64, I, I, P, P, I64]),
             "orc_count_pairs": (I64, [I64, P, P, F64, I, I]),
             "orc_rps_apply": (None, [P, ctypes.c_int32, ctypes.c_int32, U64, U64, U64, U64]),
@@ -173,24 +174,33 @@ def advect_f64(fld, lons, lats, t0: float, dt: float, n_steps: int, record: bool
 
 
 def advect_f64_field64(u, v, lon_axis, lat_axis, t_axis, lons, lats, t0: float, dt: float, n_steps: int,
-                       n_threads: int = 0, cell_signature: bool = False):
+                       n_threads: int = 0, cell_signature: bool = False, du=None, dv=None, s: float = 0.0):
     """FP64 RK4 on a float64 field u, v [nt][ny][nx]: returns (lon, lat, status[, signature]).
 
     The signature (uint64 per particle) folds the grid cell of every stage evaluation; two runs of
-    a particle with equal signatures sampled the same cells, so their difference is smooth."""
+    a particle with equal signatures sampled the same cells, so their difference is smooth.
+    With int8 directions du, dv (the field's shape) the run samples u + s du, v + s dv."""
     u = np.ascontiguousarray(u, dtype=np.float64)
     v = np.ascontiguousarray(v, dtype=np.float64)
     nt, ny, nx = u.shape
-    s = OrcField(u.ctypes.data, v.ctypes.data, nx, ny, nt, float(lon_axis[0]),
-                 float((lon_axis[-1] - lon_axis[0]) / (nx - 1)), float(lat_axis[0]),
-                 float((lat_axis[-1] - lat_axis[0]) / (ny - 1)), float(t_axis[0]),
-                 float((t_axis[-1] - t_axis[0]) / (nt - 1)))
+    fs = OrcField(u.ctypes.data, v.ctypes.data, nx, ny, nt, float(lon_axis[0]),
+                  float((lon_axis[-1] - lon_axis[0]) / (nx - 1)), float(lat_axis[0]),
+                  float((lat_axis[-1] - lat_axis[0]) / (ny - 1)), float(t_axis[0]),
+                  float((t_axis[-1] - t_axis[0]) / (nt - 1)))
     lon = np.array(lons, dtype=np.float64)
     lat = np.array(lats, dtype=np.float64)
     st = np.zeros(lon.size, np.uint8)
     sig = np.zeros(lon.size, np.uint64) if cell_signature else None
-    bad = lib().orc_advect_f64d(ctypes.byref(s), lon.size, _p(lon), _p(lat), _p(st), float(t0), float(dt),
-                                int(n_steps), int(n_threads), _p(sig))
+    if du is None:
+        bad = lib().orc_advect_f64d(ctypes.byref(fs), lon.size, _p(lon), _p(lat), _p(st), float(t0), float(dt),
+                                    int(n_steps), int(n_threads), _p(sig))
+    else:
+        du = np.ascontiguousarray(du, dtype=np.int8)
+        dv = np.ascontiguousarray(dv, dtype=np.int8)
+        if du.shape != u.shape or dv.shape != v.shape:
+            raise ValueError("directions must have the field's shape")
+        bad = lib().orc_advect_f64d_dir(ctypes.byref(fs), _p(du), _p(dv), float(s), lon.size, _p(lon), _p(lat), _p(st),
+                                        float(t0), float(dt), int(n_steps), int(n_threads), _p(sig))
     if bad < 0:
         raise ValueError("time outside the field's time axis")
     return (lon, lat, st, sig) if cell_signature else (lon, lat, st)

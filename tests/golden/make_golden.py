@@ -33,7 +33,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REFERENCE = os.environ.get("LM_REFERENCE_DIR", "/root/reference")
+REFERENCE = os.environ.get("LM_REFERENCE_DIR")
+if not REFERENCE or not os.path.isdir(REFERENCE):
+    raise SystemExit("set LM_REFERENCE_DIR to a checkout of ali-ramadhan/lagrangian-microbes")
 sys.path.insert(0, os.path.join(REPO, "oracle"))
 import oracle  # noqa: E402  (Philox uniforms keyed by (seed, step, i, j))
 

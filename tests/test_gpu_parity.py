@@ -377,7 +377,7 @@ def test_gpu_batched_ensembles_equal_single_runs(engine, lm, orc):
 
 
 def test_gpu_batched_beyond_one_tile_pass_equals_single_runs(engine, lm):
-    # 1.2M microbes in 6 ensembles: more than the blocks' shared memory holds at once (608 x 1024),
+    # 1.2M microbes in 6 ensembles: more than the blocks' shared memory holds at once (304 x 2048),
     # so the interaction runs in groups of whole ensembles; one ensemble is dense (long lists)
     fld = lm.synthetic_psi_field(195.0, 206.0, 20.0, 31.0, 1.0 / 12.0, n_frames=4, frame_seconds=3600.0, seed=4)
     rng = np.random.default_rng(17)

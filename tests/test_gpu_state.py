@@ -69,3 +69,12 @@ def test_autotune_changes_speed_only(lm, orc, small_field):
     for x, y in zip(want, got):
         np.testing.assert_array_equal(x, y)
     sim.close()
+
+
+def test_loaded_kernels_are_sm103a(lm):
+    import ctypes
+
+    from lagrangian_microbes_gb300 import _lib
+    sm = ctypes.c_int(0)
+    assert _lib.load().lm_kernel_arch(ctypes.byref(sm)) == _lib.LM_OK
+    assert sm.value == 103
