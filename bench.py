@@ -182,6 +182,7 @@ def run_gb300(args):
         sim.ctx.call("lm_stats_reset")
 
     reset()
+    depth_first = dependency_depth(sim, 0)
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(K)]
     if world > 1:
@@ -258,6 +259,7 @@ def run_gb300(args):
     late_step = (K - 1) * spg
     if late_step:
         sim.run_graph(K - 1, sync=True)
+    depth_late = dependency_depth(sim, late_step)
     sim.ctx.profile_enable(True)
     sim.step(late_step * DT, DT, 4, step0=late_step)
     prof_late = sim.ctx.profile()
@@ -272,13 +274,15 @@ def run_gb300(args):
     if not args.no_e2e:
         e2e = run_e2e(fld, lons, lats, species, K, spg, local, stream)
 
-    batched = adjoint = stress = histogram = None
+    batched = adjoint = stress = histogram = dropin = None
+    if rank == 0 and not args.no_dropin:
+        dropin = run_dropin(fld, lons, lats, species, local, stream)
     if rank == 0 and not args.no_batched:
         batched = run_batched(local, stream)
     if rank == 0 and not args.no_stress:
         stress = run_stress(fld, local)
     if rank == 0 and not args.no_adjoint:
-        adjoint = run_adjoint(fld, local)
+        adjoint = run_adjoint(local)
     if rank == 0 and not args.no_histogram:
         histogram = run_histogram(lons, lats, species)
 
@@ -301,16 +305,112 @@ def run_gb300(args):
             "plain": {"value": plain_value, "unit": "microbe-steps/s", "sim_steps": plain_steps,
                       "graph_speedup": value / world / plain_value},
             "roofline": roofline, "whole_step": whole, "kernels": kernels, "kernels_last_day": last_day,
-            "e2e": e2e, "cpu_baseline": cpu, "clocks": clk, "batched": batched, "adjoint": adjoint, "stress": stress,
+            "e2e": e2e, "cpu_baseline": cpu, "clocks": clk, "dropin": dropin, "batched": batched, "adjoint": adjoint,
+            "stress": stress,
             "distance_histogram": histogram,
             "gpu_launches": int(round(launches_per_step * K)),
-            "max_rounds": stats["max_rounds"],
-            "mean_rounds": stats["rounds_total"] / max(stats["steps_total"], 1),
+            "dependency_depth": {"first_step": depth_first, f"step_{late_step}": depth_late,
+                                 "what": "longest chain of pairs that share a microbe, in application order "
+                                         "(levels of one logged step, replayed from the same state)"},
+            "cpu_baseline_reference": reference_cpu_timing(),
         }
         print(json.dumps(line), flush=True)
     sim.close()
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+DROPIN_STEPS = 48
+
+
+def run_dropin(fld, lons, lats, species, local: int, stream):
+    """The reference's own two-phase call surface on the 490k workload (rock_paper_scissors_example.py:
+    22-36): ParticleAdvecter.time_step over 48 hourly steps writing per-tile chunk pickles every 24
+    steps, create_netcdf_file, then InteractionSimulator.time_step over the same 48 steps (wall
+    clock, files in a temporary directory). Beside it, the fused engine's plain steps with and
+    without per-step records (positions and species copied to host arrays)."""
+    import shutil
+    import tempfile
+    from datetime import timedelta
+
+    import numpy as np
+    import torch
+
+    import lagrangian_microbes_gb300 as lm
+    from lagrangian_microbes_gb300.engine import Simulation
+    from lagrangian_microbes_gb300.interaction_simulator import InteractionSimulator
+    from lagrangian_microbes_gb300.particle_advecter import ParticleAdvecter
+    n, steps = lons.size, DROPIN_STEPS
+    start, dt = fld.epoch, timedelta(seconds=DT)
+    out = tempfile.mkdtemp(prefix="lm_dropin_")
+    try:
+        t0 = time.perf_counter()
+        pa = ParticleAdvecter(lons, lats, N_procs=4, velocity_field=fld, output_dir=out, output_chunk_iters=24,
+                              seed=SEED, device=local)
+        pa._engine()  # context, field and particle upload
+        t1 = time.perf_counter()
+        pa.time_step(start, start + steps * dt, dt)
+        t2 = time.perf_counter()
+        pa.create_netcdf_file(start, start + steps * dt, dt)
+        t3 = time.perf_counter()
+        rps = lm.rock_paper_scissors(n, P_WIN, P_WIN, P_WIN, seed=SEED)
+        rps[2]["species"][:] = species
+        InteractionSimulator(rps, RADIUS, advection_dir=out, output_dir=out, device=local).time_step(
+            start, start + steps * dt, dt)
+        t4 = time.perf_counter()
+    finally:
+        shutil.rmtree(out, ignore_errors=True)
+    # the fused engine from one state: plain steps without and with records
+    sim = Simulation(fld, lons, lats, species, radius=RADIUS, p_rs=P_WIN, p_pr=P_WIN, p_sp=P_WIN, seed=SEED,
+                     device=local)
+    sim.set_stream(stream.cuda_stream)
+    sim.step(0.0, DT, 2, step0=0)  # warm-up (list capacities, the record ring)
+    sim.upload_particles(lons, lats, species)
+    sim.snapshot()
+    walls = {}
+    for rec in (False, True, False, True):
+        sim.restore()
+        torch.cuda.synchronize()
+        a = time.perf_counter()
+        sim.step(0.0, DT, steps, step0=0, record=rec)
+        torch.cuda.synchronize()
+        walls[rec] = min(walls.get(rec, 1e9), time.perf_counter() - a)
+    sim.close()
+    ms = n * steps
+    return {"workload": "490k lattice, 48 hourly steps through ParticleAdvecter (4 tiles, chunks of 24) + "
+                        "create_netcdf_file + InteractionSimulator (r = 0.01, p = 0.7), files on local disk",
+            "advect": {"value": ms / (t2 - t1), "unit": "microbe-steps/s", "seconds": t2 - t1,
+                       "setup_s": t1 - t0},
+            "netcdf_s": t3 - t2,
+            "interact": {"value": ms / (t4 - t3), "unit": "microbe-steps/s", "seconds": t4 - t3},
+            "two_phase": {"value": ms / (t4 - t1), "unit": "microbe-steps/s (advect + netcdf + interact)"},
+            "fused_plain": {"unrecorded_ms_per_step": 1e3 * walls[False] / steps,
+                            "recorded_ms_per_step": 1e3 * walls[True] / steps,
+                            "recorded_over_unrecorded": walls[True] / walls[False],
+                            "record_bytes_per_step": 9 * n}}
+
+
+def dependency_depth(sim, step: int) -> int:
+    """Levels of the interaction at `step` from the current state (a logged step, then the state
+    is restored): the critical path of the interaction kernel."""
+    sim.snapshot()
+    sim.step(step * DT, DT, 1, step0=step, log_pairs=True)
+    depth = int(sim.stats()["rounds"])
+    sim.restore()
+    return depth
+
+
+def reference_cpu_timing():
+    """The reference's own CPU interaction step (cKDTree + Python loop) on this workload, measured by
+    tests/golden/time_reference_cpu.py where the reference is available (it is not on the GPU host)."""
+    path = os.path.join(REPO, "tests", "golden", "reference_cpu_timing.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+    except (OSError, ValueError):
+        return None
+    d["source"] = "recorded by tests/golden/time_reference_cpu.py on the machine named in 'machine', not on this host"
+    return d
 
 
 def run_e2e(fld, lons, lats, species, K, spg, local, stream):
@@ -338,17 +438,24 @@ def run_e2e(fld, lons, lats, species, K, spg, local, stream):
 
 B_ENSEMBLES = 256
 B_STEPS = 24
+B_TOTAL_STEPS = 240
 B_BOX = (195.0, 215.0, 20.0, 35.0)
 B_WORKLOAD = ("256 ensembles, counts log-uniform in [1e3, 2e5] (rounded to square-ish lattices), patches of 0.5-3 deg side within lon "
               "195-215E lat 20-35N, p ~ U[0.5, 0.9], own seed and own 32-mode psi field each on a shared 1/12 deg "
-              "hourly grid, RK4 dt=1h, r=0.01 deg; the first simulated day (24 of 240 steps)")
+              "hourly grid, RK4 dt=1h, r=0.01 deg; timed on the first and on the last simulated day of the 240 steps")
 
 
-def make_ensembles(n_ens: int, n_frames: int, seed: int = 2025):
+def ensemble_bases(n_ens: int):
+    """The per-ensemble synthetic fields of the batching configuration, before sampling in time
+    (frames are sampled window by window: a 240-step run never holds all 256 x 241 frames)."""
+    from lagrangian_microbes_gb300.fields import psi_basis
+    return [psi_basis(*B_BOX, RES, frame_seconds=DT, seed=SEED + 1 + e) for e in range(n_ens)]
+
+
+def make_ensembles(n_ens: int, n_frames: int, seed: int = 2025, bases=None):
     """The batching configuration: per-ensemble lattices, probabilities, seeds and fields (seeded)."""
     import numpy as np
 
-    import lagrangian_microbes_gb300 as lm
     from lagrangian_microbes_gb300.particle_advecter import uniform_particle_locations
     rng = np.random.default_rng(seed)
     raw = np.exp(rng.uniform(np.log(1e3), np.log(2e5), n_ens))
@@ -367,20 +474,90 @@ def make_ensembles(n_ens: int, n_frames: int, seed: int = 2025):
         lons, lats = uniform_particle_locations(int(counts[e]), lat0[e], lat0[e] + sides[e], lon0[e], lon0[e] + sides[e])
         sp = np.random.default_rng(int(seeds[e])).integers(1, 4, lons.size).astype(np.int8)
         ens.append((lons, lats, sp))
-    fields = [lm.synthetic_psi_field(*B_BOX, RES, n_frames=n_frames, frame_seconds=DT, seed=SEED + 1 + e)
-              for e in range(n_ens)]
+    bases = bases or ensemble_bases(n_ens)
+    fields = [b.frames(0, n_frames) for b in bases]
     return fields, ens, ps, seeds
+
+
+def _oob_ok(fn, *args, **kw):
+    """Run fn; microbes that leave the shared grid are frozen and excluded (the engine reports it
+    once, as OutOfBoundsError, after the call has completed). Returns True when that happened."""
+    from lagrangian_microbes_gb300 import OutOfBoundsError
+    try:
+        fn(*args, **kw)
+        return False
+    except OutOfBoundsError:
+        return True
+
+
+def _time_graph(sim, stream, reps: int = 3) -> float:
+    """Median ms of one graph launch, each from the snapshot taken before (CUDA events)."""
+    import numpy as np
+    import torch
+    times = []
+    for _ in range(reps):
+        sim.restore()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(stream)
+        sim.run_graph(1, sync=False)
+        b.record(stream)
+        torch.cuda.synchronize()
+        times.append(a.elapsed_time(b))
+        _oob_ok(sim.sync)
+    return float(np.median(times))
+
+
+def _time_plain_per_ensemble(bases, ens, ps, seeds, first: int, local: int, state=None) -> float:
+    """Wall ms of B_STEPS plain steps of every ensemble alone (its own context), ensembles one after
+    another, from step `first` (state: the exact state of every ensemble there, or the lattices)."""
+    import numpy as np
+    import torch
+
+    from lagrangian_microbes_gb300.engine import Simulation
+    sims = []
+    edges = np.concatenate([[0], np.cumsum([x[0].size for x in ens])])
+    for e in range(len(ens)):
+        one = Simulation(bases[e].frames(first, B_STEPS + 2), ens[e][0], ens[e][1], ens[e][2], radius=RADIUS,
+                         p_rs=ps[e], p_pr=ps[e], p_sp=ps[e], seed=int(seeds[e]), device=local)
+        if state is not None:
+            a, b = edges[e], edges[e + 1]
+            one.import_state({k: (v[a:b] if k != "step" else v) for k, v in state.items()})
+        one.snapshot()
+        _oob_ok(one.step, first * DT, DT, 1, step0=first)  # warm-up (list capacities), then back
+        one.restore()
+        sims.append(one)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for one in sims:
+        _oob_ok(one.step, first * DT, DT, B_STEPS, step0=first)
+    torch.cuda.synchronize()
+    ms = (time.perf_counter() - t0) * 1e3
+    for one in sims:
+        one.close()
+    return ms
+
+
+def profile_batched(steps: int) -> None:
+    """Plain steps of the batching workload and nothing else: a short program for ncu captures of
+    its kernels (k_advect reads 256 different fields there, which do not fit L2 together)."""
+    from lagrangian_microbes_gb300.engine import EnsembleSimulation
+    fields, ens, ps, seeds = make_ensembles(B_ENSEMBLES, steps + 2)
+    sim = EnsembleSimulation(fields, ens, radius=RADIUS, p_rs=ps, p_pr=ps, p_sp=ps, seeds=seeds)
+    sim.step(0.0, DT, steps, step0=0)
+    sim.sync()
+    sim.close()
 
 
 def run_batched(local: int, stream):
     """Config B: all ensembles in one context (CUDA graph of B_STEPS fused steps) against plain
-    per-step launches of each ensemble alone (its own context), the same simulated steps."""
-    import numpy as np
-    import torch
-
-    from lagrangian_microbes_gb300.engine import EnsembleSimulation, Simulation
-    t_gen = time.perf_counter()
-    fields, ens, ps, seeds = make_ensembles(B_ENSEMBLES, B_STEPS + 2)
+    per-step launches of each ensemble alone (its own context), the same simulated steps: the
+    first simulated day, and the last one (steps 216-239) reached by streaming the fields in
+    one-day windows."""
+    from lagrangian_microbes_gb300.engine import EnsembleSimulation
+    t_start = t_gen = time.perf_counter()
+    bases = ensemble_bases(B_ENSEMBLES)
+    fields, ens, ps, seeds = make_ensembles(B_ENSEMBLES, B_STEPS + 2, bases=bases)
     t_gen = time.perf_counter() - t_gen
     total = int(sum(x[0].size for x in ens))
     sim = EnsembleSimulation(fields, ens, radius=RADIUS, p_rs=ps, p_pr=ps, p_sp=ps, seeds=seeds, device=local)
@@ -393,67 +570,77 @@ def run_batched(local: int, stream):
     prof = sim.ctx.profile()
     sim.ctx.profile_enable(False)
     kernels_ms = {k: ms / 2 for k, (ms, cnt) in prof.items() if cnt}
+    # first simulated day
+    sim.upload_ensembles(ens)
+    sim.set_step(0)
+    sim.snapshot()
     sim.capture(0.0, DT, B_STEPS, step0=0)
     sim.run_graph(1, sync=True)  # warm-up: sizes the long neighbour lists for this workload
-    reps = 3
-    times = []
-    for _ in range(reps):
-        sim.upload_ensembles(ens)
-        sim.set_step(0)
-        sim.ctx.call("lm_stats_reset")
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        a.record(stream)
-        sim.run_graph(1, sync=False)
-        b.record(stream)
-        torch.cuda.synchronize()
-        times.append(a.elapsed_time(b))
-    sim.sync()
+    sim.ctx.call("lm_stats_reset")
+    graph_ms = _time_graph(sim, stream)
     st = sim.stats()
+    plain_ms = _time_plain_per_ensemble(bases, ens, ps, seeds, 0, local)
+    # last simulated day: advance through one-day field windows, then the same two timings
+    late = B_TOTAL_STEPS - B_STEPS
+    sim.restore()
+    for d in range(0, late, B_STEPS):
+        sim.upload_fields([b.frames(d, B_STEPS + 1) for b in bases])
+        _oob_ok(sim.step, d * DT, DT, B_STEPS, step0=d)
+    sim.upload_fields([b.frames(late, B_STEPS + 2) for b in bases])
+    sim.snapshot()
+    sim.ctx.profile_enable(True)
+    _oob_ok(sim.step, late * DT, DT, 2, step0=late)
+    prof_late = sim.ctx.profile()
+    sim.ctx.profile_enable(False)
+    sim.restore()
+    sim.capture(late * DT, DT, B_STEPS, step0=late)
+    _oob_ok(sim.run_graph, 1, sync=True)
+    sim.ctx.call("lm_stats_reset")
+    graph_late_ms = _time_graph(sim, stream)
+    st_late = sim.stats()
+    sim.restore()
+    state = sim.export_state()
+    frozen = int((state["status"] != 0).sum())
     sim.close()
-    graph_ms = float(np.median(times))
-    graph_value = total * B_STEPS / (graph_ms / 1e3)
-    # plain: each ensemble alone through the drop-in engine, per-step launches
-    plain_ms = 0.0
-    sims = []
-    for e in range(B_ENSEMBLES):
-        one = Simulation(fields[e], ens[e][0], ens[e][1], ens[e][2], radius=RADIUS, p_rs=ps[e], p_pr=ps[e],
-                         p_sp=ps[e], seed=int(seeds[e]), device=local)
-        one.step(0.0, DT, 1, step0=0)  # warm-up (list capacities), then from the start again
-        one.upload_particles(ens[e][0], ens[e][1], ens[e][2])
-        sims.append(one)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for e, one in enumerate(sims):
-        one.step(0.0, DT, B_STEPS, step0=0)
-    torch.cuda.synchronize()
-    plain_ms = (time.perf_counter() - t0) * 1e3
-    for one in sims:
-        one.close()
-    plain_value = total * B_STEPS / (plain_ms / 1e3)
+    plain_late_ms = _time_plain_per_ensemble(bases, ens, ps, seeds, late, local, state=state)
+
+    def part(g_ms, p_ms, stats, prof_ms, first):
+        gv = total * B_STEPS / (g_ms / 1e3)
+        pv = total * B_STEPS / (p_ms / 1e3)
+        return {"steps": [first, first + B_STEPS - 1],
+                "pairs_per_step": stats["pairs_total"] / max(stats["steps_total"], 1),
+                "long_lists": stats["long_lists"],
+                "graph": {"value": gv, "unit": "microbe-steps/s", "ms_per_sim_step": g_ms / B_STEPS,
+                          "form": "one context, one CUDA graph of 24 fused steps for all ensembles",
+                          "cell_factor": cell_factor},
+                "plain_per_ensemble": {"value": pv, "unit": "microbe-steps/s", "ms_per_sim_step": p_ms / B_STEPS,
+                                       "form": "one context per ensemble, per-step launches, ensembles one after another"},
+                "batched_over_plain": gv / pv, "kernels_ms_per_step": prof_ms}
+
+    first = part(graph_ms, plain_ms, st, kernels_ms, 0)
+    last = part(graph_late_ms, plain_late_ms, st_late,
+                {k: ms / 2 for k, (ms, cnt) in prof_late.items() if cnt}, late)
     return {"workload": B_WORKLOAD, "ensembles": B_ENSEMBLES, "microbes": total, "sim_steps": B_STEPS,
-            "pairs_per_step": st["pairs_total"] / max(st["steps_total"], 1),
-            "graph": {"value": graph_value, "unit": "microbe-steps/s", "ms_per_sim_step": graph_ms / B_STEPS,
-                      "form": "one context, one CUDA graph of 24 fused steps for all ensembles",
-                      "cell_factor": cell_factor},
-            "plain_per_ensemble": {"value": plain_value, "unit": "microbe-steps/s",
-                                   "ms_per_sim_step": plain_ms / B_STEPS,
-                                   "form": "one context per ensemble, per-step launches, ensembles one after another"},
-            "batched_over_plain": graph_value / plain_value, "field_generation_s": t_gen,
-            "kernels_ms_per_step": kernels_ms}
+            "first_day": first, "last_day": last,
+            "left_the_grid_by_step_216": frozen,  # frozen and excluded from pairing, like every microbe that leaves
+            # the headline of the configuration: both timed days together
+            "graph": {"value": total * 2 * B_STEPS / ((graph_ms + graph_late_ms) / 1e3), "unit": "microbe-steps/s"},
+            "batched_over_plain": (plain_ms + plain_late_ms) / (graph_ms + graph_late_ms),
+            "field_generation_s": t_gen, "seconds": time.perf_counter() - t_start}
 
 
-def run_adjoint(fld, local: int):
+def run_adjoint(local: int):
     """Config D timing: 1M microbes on a 1000x1000 lattice, 720 steps, checkpoints every 32, the
-    mean squared great-circle distance to seeded targets, forward + backward (both precisions)."""
+    mean squared great-circle distance to seeded targets, forward + backward (both precisions). The
+    721-frame field is generated here, whatever the number of bench steps."""
     import numpy as np
     import torch
 
+    import lagrangian_microbes_gb300 as lm
     from lagrangian_microbes_gb300.adjoint import AdjointTape, advect_rk4, mean_squared_distance
     from lagrangian_microbes_gb300.particle_advecter import uniform_particle_locations
     n, steps, k = 1_000_000, 720, 32
-    if fld.u.shape[0] < steps + 1:
-        return {"skipped": f"field has {fld.u.shape[0]} frames, need {steps + 1}"}
+    fld = lm.synthetic_psi_field(*FIELD_BOX, RES, n_frames=steps + 1, frame_seconds=DT, seed=SEED)
     lons, lats = uniform_particle_locations(n, LAT[0], LAT[1], LON[0], LON[1])
     rng = np.random.default_rng(7)
     dev = torch.device("cuda", local)
@@ -464,7 +651,7 @@ def run_adjoint(fld, local: int):
     out = {"workload": "1M microbes, 1000x1000 lattice lon 200-205E lat 25-30N, 720 RK4 steps dt=1h on the 1/12 deg "
                        "hourly field, checkpoints every 32 steps, loss = mean squared great-circle distance to "
                        "targets x0 + N(0, 20 km)", "microbes": n, "sim_steps": steps}
-    for prec in ("f32", "f64"):
+    for prec in ("ds", "f32", "f64"):
         tape = AdjointTape(device=local, precision=prec)
         res = []
         for _ in range(3):
@@ -660,17 +847,22 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-dropin", action="store_true", help="skip the two-phase drop-in measurement")
     ap.add_argument("--no-batched", action="store_true", help="skip the 256-ensemble batching measurement")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint (differentiation) timing")
     ap.add_argument("--no-stress", action="store_true", help="skip the 16M clustered count-only measurement")
     ap.add_argument("--no-histogram", action="store_true", help="skip the pairwise distance histogram measurement")
     ap.add_argument("--profile-run", action="store_true", help="only the warm-up and timed graph launches")
+    ap.add_argument("--profile-batched", type=int, default=0, metavar="STEPS",
+                    help="only STEPS plain steps of the 256-ensemble batching workload (for ncu captures)")
     ap.add_argument("--traffic-json", default=os.path.join(REPO, "profiles", "traffic.json"))
     args = ap.parse_args()
     if args.warmup < 0 or args.steps < 1:
         ap.error("--steps >= 1 and --warmup >= 0")
     if args.impl == "reference":
         run_reference(args)
+    elif args.profile_batched:
+        profile_batched(args.profile_batched)
     else:
         run_gb300(args)
 

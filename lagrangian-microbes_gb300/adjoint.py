@@ -2,8 +2,9 @@
 
 ``advect_rk4(lon0, lat0, u, v, lon_axis, lat_axis, t_axis, t0, dt, n_steps)`` returns the final
 positions of microbes advected from (lon0, lat0) through the gridded velocity (u, v), with the
-arithmetic of the fused engine's advection (the reference's Parcels AdvectionRK4 on a spherical
-RectilinearZGrid, particle_advecter.py:177-187, 220-223; no diffusion kick). Its backward gives
+scheme of the fused engine's advection (the reference's Parcels AdvectionRK4 on a spherical
+RectilinearZGrid, particle_advecter.py:177-187, 220-223; no diffusion kick), positions carried in
+double-float by default (``precision``, see AdjointTape). Its backward gives
 dL/d(lon0, lat0) and dL/d(u, v) for any torch loss on the final positions, computed by the
 hand-written adjoint kernels (k_adjoint.cu) from checkpoints every ``checkpoint_every`` steps; the
 velocity gradient is a deterministic segmented reduction, bit-identical from run to run.
@@ -26,20 +27,22 @@ from . import _lib
 EARTH_RADIUS_M = 6371.228e3
 
 
-PRECISIONS = {"f32": 0, "f64": 1}
+PRECISIONS = {"f32": 0, "f64": 1, "ds": 2}
 
 
 class AdjointTape:
     """One lm_adjoint tape: the recorded forward run and its backward sweep.
 
-    ``precision="f32"`` keeps float32 state with the engine's arithmetic (final positions
-    bit-identical to the fused engine's advection); ``"f64"`` carries float64 state and arithmetic
-    over the float32 field, for long runs where float32 rounding, amplified by the flow, moves
-    trajectories across cell edges of the piecewise-bilinear field. In "f64" mode the final
-    positions come back as float64 tensors.
+    ``precision="ds"`` (the default) carries every position as a double-float pair of float32
+    words, with float32 velocities, Jacobians and adjoint state: over long chaotic runs the
+    trajectory does not accumulate float32 position rounding (which the flow amplifies), at
+    close to float32 cost. ``"f32"`` keeps float32 state with the engine's arithmetic (final
+    positions bit-identical to the fused engine's advection); ``"f64"`` carries float64 state and
+    arithmetic over the float32 field. In "ds" and "f64" modes the final positions come back as
+    float64 tensors (rounded once from the working state).
     """
 
-    def __init__(self, ctx: _lib.Context | None = None, device: int = 0, precision: str = "f32"):
+    def __init__(self, ctx: _lib.Context | None = None, device: int = 0, precision: str = "ds"):
         if precision not in PRECISIONS:
             raise ValueError(f"precision must be one of {sorted(PRECISIONS)}; got {precision!r}")
         self.ctx = ctx or _lib.Context(device)
@@ -81,7 +84,7 @@ class AdjointTape:
             self.ctx.check(rc)
         self.n = n
         self.field_shape = (nt, ny, nx)
-        if self.precision == "f64":  # hand back the float64 state, rounded once
+        if self.precision in ("f64", "ds"):  # hand back the working state, rounded once to float64
             lon = torch.empty(n, dtype=torch.float64, device=lon0.device)
             lat = torch.empty_like(lon)
             self.ctx.check(self._lib.lm_adjoint_final_positions(self._h, lon.data_ptr(), lat.data_ptr()))
@@ -140,7 +143,7 @@ class _AdvectRK4(torch.autograd.Function):
 
 def advect_rk4(lon0, lat0, u, v, lon_axis, lat_axis, t_axis, t0: float, dt: float, n_steps: int,
                checkpoint_every: int = 32, tape: AdjointTape | None = None, allow_out_of_bounds: bool = False,
-               precision: str = "f32"):
+               precision: str = "ds"):
     """Differentiable RK4 advection (float32 CUDA tensors in and out); see the module docstring."""
     tape = tape or AdjointTape(device=lon0.device.index or 0, precision=precision)
     return _AdvectRK4.apply(lon0, lat0, u, v, tape, (lon_axis, lat_axis, t_axis), float(t0), float(dt),

@@ -143,14 +143,10 @@ struct VelJac {
   T inv_mc;                              // d flon / d U = 1 / (M cos lat)
 };
 
+// Velocity and Jacobian in cell (i, j) at bilinear fractions (a, b); `lat` is the absolute latitude.
 template <class T>
-__device__ __forceinline__ bool vel_jac(const FieldView& f, const Geo<T>& g, int k, T w, T xo, T yo, VelJac<T>& r) {
-  const T fx = (xo - g.gx0) * g.inv_dx;
-  const T fy = (yo - g.gy0) * g.inv_dy;
-  if (!(fx >= T(0) && fx <= g.max_fx && fy >= T(0) && fy <= g.max_fy)) return false;
-  const int i = min((int)fx, f.nx - 2);
-  const int j = min((int)fy, f.ny - 2);
-  const T a = fx - (T)i, b = fy - (T)j;
+__device__ __forceinline__ void vel_jac_at(const FieldView& f, int k, T w, int i, int j, T a, T b, T lat, T inv_dx,
+                                           T inv_dy, VelJac<T>& r) {
   const float2* p = f.uv + ((size_t)k * f.ny + j) * f.nx + i;
   float2 q00 = __ldg(p), q01 = __ldg(p + 1), q10 = __ldg(p + f.nx), q11 = __ldg(p + f.nx + 1);
   const T w00 = (T(1) - a) * (T(1) - b), w01 = a * (T(1) - b), w10 = (T(1) - a) * b, w11 = a * b;
@@ -172,7 +168,6 @@ __device__ __forceinline__ bool vel_jac(const FieldView& f, const Geo<T>& g, int
     va = va + w * (((T(1) - b) * ((T)q01.y - (T)q00.y) + b * ((T)q11.y - (T)q10.y)) - va);
     vb = vb + w * (((T(1) - a) * ((T)q10.y - (T)q00.y) + a * ((T)q11.y - (T)q01.y)) - vb);
   }
-  const T lat = g.org_lat + yo;
   const T c = cospi_t(lat * (T(1) / T(180)));
   const T sn = sinpi_t(lat * (T(1) / T(180)));
   const T M = (T)M_PER_DEG;
@@ -180,13 +175,23 @@ __device__ __forceinline__ bool vel_jac(const FieldView& f, const Geo<T>& g, int
   r.flat = v * (T(1) / M);
   r.inv_mc = T(1) / (M * c);
   // d/dlat (1 / cos(lat)) = tan(lat) / cos(lat) * pi / 180 per degree
-  r.dlon_dx = ua * g.inv_dx * r.inv_mc;
-  r.dlon_dy = ub * g.inv_dy * r.inv_mc + r.flon * (sn / c) * (T)0.017453292519943295;
-  r.dlat_dx = va * g.inv_dx * (T(1) / M);
-  r.dlat_dy = vb * g.inv_dy * (T(1) / M);
+  r.dlon_dx = ua * inv_dx * r.inv_mc;
+  r.dlon_dy = ub * inv_dy * r.inv_mc + r.flon * (sn / c) * (T)0.017453292519943295;
+  r.dlat_dx = va * inv_dx * (T(1) / M);
+  r.dlat_dy = vb * inv_dy * (T(1) / M);
   r.cell = (uint32_t)j * (uint32_t)(f.nx - 1) + (uint32_t)i;
   r.a = a;
   r.b = b;
+}
+
+template <class T>
+__device__ __forceinline__ bool vel_jac(const FieldView& f, const Geo<T>& g, int k, T w, T xo, T yo, VelJac<T>& r) {
+  const T fx = (xo - g.gx0) * g.inv_dx;
+  const T fy = (yo - g.gy0) * g.inv_dy;
+  if (!(fx >= T(0) && fx <= g.max_fx && fy >= T(0) && fy <= g.max_fy)) return false;
+  const int i = min((int)fx, f.nx - 2);
+  const int j = min((int)fy, f.ny - 2);
+  vel_jac_at<T>(f, k, w, i, j, fx - (T)i, fy - (T)j, g.org_lat + yo, g.inv_dx, g.inv_dy, r);
   return true;
 }
 
@@ -257,29 +262,16 @@ __global__ void __launch_bounds__(256) k_adj_forward(FieldView f, const AdjStep*
   if (bits) atomicOr(err, bits);
 }
 
-// lambda_{m+1} -> lambda_m, plus 4 records per microbe (key = cell * 4 + stage time, or `sent`).
+// The backward of one RK4 step of microbe p from its four stage Jacobians (every precision):
+// lambda_{m+1} -> lambda_m in lx, ly, plus its 4 records and their keys. `ok` false: the step was
+// frozen (a stage left the grid or the step was non-finite), x_{m+1} = x_m and the adjoint passes
+// through.
 template <class T>
-__global__ void __launch_bounds__(256) k_adj_step(FieldView f, AdjStep s, T dt, uint32_t n, const T* __restrict__ xs,
-                                                  const T* __restrict__ ys, const uint8_t* __restrict__ sts,
-                                                  T* __restrict__ lx, T* __restrict__ ly, float4* __restrict__ rec,
-                                                  uint32_t* __restrict__ key, uint32_t sent, uint32_t* __restrict__ mkey,
-                                                  uint32_t* __restrict__ mcode, uint32_t msent, uint32_t* err) {
-  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= n) return;
-  const Geo<T> g(f);
-  const T x = xs[p], y = ys[p];
-  const T w0 = stage_w<T>(s, 0), w1 = stage_w<T>(s, 1), w2 = stage_w<T>(s, 2);
-  VelJac<T> J1, J2, J3, J4;
-  bool ok = sts[p] == STATUS_OK;
-  ok = ok && vel_jac(f, g, s.k[0], w0, x, y, J1);
-  ok = ok && vel_jac(f, g, s.k[1], w1, x + T(0.5) * dt * J1.flon, y + T(0.5) * dt * J1.flat, J2);
-  ok = ok && vel_jac(f, g, s.k[1], w1, x + T(0.5) * dt * J2.flon, y + T(0.5) * dt * J2.flat, J3);
-  ok = ok && vel_jac(f, g, s.k[2], w2, x + dt * J3.flon, y + dt * J3.flat, J4);
-  if (ok) {  // a non-finite step was frozen by the forward: identity, like a stage off the grid
-    const T nx = x + (J1.flon + T(2) * J2.flon + T(2) * J3.flon + J4.flon) * (dt * (T(1) / T(6)));
-    const T ny = y + (J1.flat + T(2) * J2.flat + T(2) * J3.flat + J4.flat) * (dt * (T(1) / T(6)));
-    ok = isfinite(nx) && isfinite(ny);
-  }
+__device__ __forceinline__ void adj_tail(const FieldView& f, uint32_t p, bool ok, const VelJac<T>& J1,
+                                         const VelJac<T>& J2, const VelJac<T>& J3, const VelJac<T>& J4, T dt,
+                                         T* __restrict__ lx, T* __restrict__ ly, float4* __restrict__ rec,
+                                         uint32_t* __restrict__ key, uint32_t sent, uint32_t* __restrict__ mkey,
+                                         uint32_t* __restrict__ mcode, uint32_t msent, uint32_t* err) {
   if (!ok) {  // frozen this step: x_{m+1} = x_m, the adjoint passes through
     if (mkey)
       mkey[p] = msent;
@@ -330,6 +322,253 @@ __global__ void __launch_bounds__(256) k_adj_step(FieldView f, AdjStep s, T dt, 
   if (!mkey)
     reinterpret_cast<uint4*>(key)[p] =
         make_uint4(4u * J1.cell + 0u, 4u * J2.cell + 1u, 4u * J3.cell + 1u, 4u * J4.cell + 2u);
+}
+
+// lambda_{m+1} -> lambda_m, plus 4 records per microbe (key = cell * 4 + stage time, or `sent`).
+template <class T>
+__global__ void __launch_bounds__(256) k_adj_step(FieldView f, AdjStep s, T dt, uint32_t n, const T* __restrict__ xs,
+                                                  const T* __restrict__ ys, const uint8_t* __restrict__ sts,
+                                                  T* __restrict__ lx, T* __restrict__ ly, float4* __restrict__ rec,
+                                                  uint32_t* __restrict__ key, uint32_t sent, uint32_t* __restrict__ mkey,
+                                                  uint32_t* __restrict__ mcode, uint32_t msent, uint32_t* err) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const Geo<T> g(f);
+  const T x = xs[p], y = ys[p];
+  const T w0 = stage_w<T>(s, 0), w1 = stage_w<T>(s, 1), w2 = stage_w<T>(s, 2);
+  VelJac<T> J1, J2, J3, J4;
+  bool ok = sts[p] == STATUS_OK;
+  ok = ok && vel_jac(f, g, s.k[0], w0, x, y, J1);
+  ok = ok && vel_jac(f, g, s.k[1], w1, x + T(0.5) * dt * J1.flon, y + T(0.5) * dt * J1.flat, J2);
+  ok = ok && vel_jac(f, g, s.k[1], w1, x + T(0.5) * dt * J2.flon, y + T(0.5) * dt * J2.flat, J3);
+  ok = ok && vel_jac(f, g, s.k[2], w2, x + dt * J3.flon, y + dt * J3.flat, J4);
+  if (ok) {  // a non-finite step was frozen by the forward: identity, like a stage off the grid
+    const T nx = x + (J1.flon + T(2) * J2.flon + T(2) * J3.flon + J4.flon) * (dt * (T(1) / T(6)));
+    const T ny = y + (J1.flat + T(2) * J2.flat + T(2) * J3.flat + J4.flat) * (dt * (T(1) / T(6)));
+    ok = isfinite(nx) && isfinite(ny);
+  }
+  adj_tail<T>(f, p, ok, J1, J2, J3, J4, dt, lx, ly, rec, key, sent, mkey, mcode, msent, err);
+}
+
+// ---------------------------------------------------------------- double-float positions
+//
+// The default working precision of the tape (ADJ_DS): each offset is an unevaluated sum of two
+// float32 words, hi + lo (about 48 significant bits), so a 720-step trajectory does not pick up the
+// float32 rounding of the position every step (0.1 m at the field's scale) that the flow then
+// amplifies. Only the position arithmetic is double-float: stage positions, the RK4 update and the
+// position -> (cell, bilinear fraction) mapping. Velocities, Jacobians, the adjoint state and the
+// records stay float32 with the f32 mode's arithmetic (vel_jac_at<float>). Error-free sums and
+// products follow Dekker (1971) and Knuth's two-sum; every operation is rounded explicitly
+// (__fadd_rn & co.) so that no contraction changes it between kernels.
+struct DS {
+  float hi, lo;
+};
+
+__device__ __forceinline__ DS ds_of(double d) {
+  const float h = (float)d;
+  return DS{h, (float)(d - (double)h)};
+}
+__device__ __forceinline__ double ds_value(DS a) { return (double)a.hi + (double)a.lo; }
+__device__ __forceinline__ bool ds_finite(DS a) { return isfinite(a.hi) && isfinite(a.lo); }
+
+// hi + lo of s + t where |s| >= |t| (fast two-sum)
+__device__ __forceinline__ DS ds_renorm(float s, float t) {
+  const float h = __fadd_rn(s, t);
+  return DS{h, __fsub_rn(t, __fsub_rn(h, s))};
+}
+// a + b, b a float32 (two-sum of the high words, then the low word)
+__device__ __forceinline__ DS ds_add(DS a, float b) {
+  const float s = __fadd_rn(a.hi, b);
+  const float bb = __fsub_rn(s, a.hi);
+  const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return ds_renorm(s, __fadd_rn(e, a.lo));
+}
+// a + b for two double-float values
+__device__ __forceinline__ DS ds_add(DS a, DS b) {
+  const float s = __fadd_rn(a.hi, b.hi);
+  const float bb = __fsub_rn(s, a.hi);
+  const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+  return ds_renorm(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
+}
+// a * b (the product of the high words is exact through one fma)
+__device__ __forceinline__ DS ds_mul(DS a, DS b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return ds_renorm(p, e);
+}
+
+// The grid in double-float: fx = (x - gx0) / dx with 1/dx to double-float accuracy (a float32
+// 1/dx alone would shift the sampling point by up to ~0.1 m at the far edge of the grid).
+struct GeoDS {
+  DS mgx0, mgy0, inv_dx, inv_dy;  // -gx0, -gy0 (grid origin minus state origin), 1/dx, 1/dy
+  float max_fx, max_fy, org_lat, inv_dxf, inv_dyf;
+  __device__ explicit GeoDS(const FieldView& f)
+      : mgx0(ds_of(-f.gx0d)), mgy0(ds_of(-f.gy0d)), inv_dx(ds_of(f.inv_dxd)), inv_dy(ds_of(f.inv_dyd)),
+        max_fx(f.max_fx), max_fy(f.max_fy), org_lat(f.org_lat), inv_dxf((float)f.inv_dxd), inv_dyf((float)f.inv_dyd) {}
+};
+
+// Cell index and bilinear fraction of a double-float grid coordinate u in [0, max]; false outside.
+__device__ __forceinline__ bool ds_cell(DS u, float max_u, int n_cells, int& i, float& a) {
+  const bool in = (u.hi > 0.f || (u.hi == 0.f && u.lo >= 0.f)) && (u.hi < max_u || (u.hi == max_u && u.lo <= 0.f));
+  if (!in) return false;
+  float fl = floorf(u.hi);
+  if (fl == u.hi && u.lo < 0.f) fl = __fsub_rn(fl, 1.f);  // hi is an integer and the value lies just below it
+  i = min((int)fl, n_cells - 1);
+  a = __fadd_rn(__fsub_rn(u.hi, (float)i), u.lo);  // u.hi - i is exact (Sterbenz) for i >= 1, and for i = 0
+  return true;
+}
+
+// Velocity and Jacobian at a double-float offset position (float32 arithmetic past the fractions).
+__device__ __forceinline__ bool vel_jac_ds(const FieldView& f, const GeoDS& g, int k, float w, DS xo, DS yo,
+                                           VelJac<float>& r) {
+  int i, j;
+  float a, b;
+  if (!ds_cell(ds_mul(ds_add(xo, g.mgx0), g.inv_dx), g.max_fx, f.nx - 1, i, a)) return false;
+  if (!ds_cell(ds_mul(ds_add(yo, g.mgy0), g.inv_dy), g.max_fy, f.ny - 1, j, b)) return false;
+  vel_jac_at<float>(f, k, w, i, j, a, b, __fadd_rn(g.org_lat, yo.hi), g.inv_dxf, g.inv_dyf, r);
+  return true;
+}
+
+// The increment (k1 + 2 k2 + 2 k3 + k4) dt / 6 of one coordinate, float32.
+__device__ __forceinline__ float rk4_increment(float k1, float k2, float k3, float k4, float dt) {
+  return __fmul_rn(__fadd_rn(__fadd_rn(k1, __fmul_rn(2.f, k2)), __fadd_rn(__fmul_rn(2.f, k3), k4)), dt * (1.0f / 6.0f));
+}
+
+// Stage q (0..3) of one RK4 step from (x, y): its velocity and Jacobian in J[q], given the earlier
+// stages J[0..q-1] (stage positions x + dt/2 k1, x + dt/2 k2, x + dt k3). False outside the grid.
+// The forward, the backward recomputation and the cell signature all evaluate stages through this.
+__device__ __forceinline__ bool ds_stage(const FieldView& f, const GeoDS& g, const AdjStep& s, float dt, DS x, DS y,
+                                         VelJac<float>* J, int q) {
+  if (q == 0) return vel_jac_ds(f, g, s.k[0], s.w[0], x, y, J[0]);
+  const float h = q == 3 ? dt : 0.5f * dt;
+  const int g_ = q == 3 ? 2 : 1;
+  return vel_jac_ds(f, g, s.k[g_], s.w[g_], ds_add(x, __fmul_rn(h, J[q - 1].flon)), ds_add(y, __fmul_rn(h, J[q - 1].flat)),
+                    J[q]);
+}
+
+// One RK4 step from (x, y): the four stages and the new position. False when a stage leaves the grid.
+__device__ __forceinline__ bool rk4_ds(const FieldView& f, const GeoDS& g, const AdjStep& s, float dt, DS x, DS y,
+                                       VelJac<float>* J, DS& nx, DS& ny) {
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+    if (!ds_stage(f, g, s, dt, x, y, J, q)) return false;
+  nx = ds_add(x, rk4_increment(J[0].flon, J[1].flon, J[2].flon, J[3].flon, dt));
+  ny = ds_add(y, rk4_increment(J[0].flat, J[1].flat, J[2].flat, J[3].flat, dt));
+  return true;
+}
+
+__global__ void k_adj_init_ds(FieldView f, uint32_t n, const float* __restrict__ lon, const float* __restrict__ lat,
+                              DS* __restrict__ x, DS* __restrict__ y, uint8_t* __restrict__ st) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const float a = lon[p], b = lat[p];
+  x[p] = ds_of((double)a - (double)f.org_lon);
+  y[p] = ds_of((double)b - (double)f.org_lat);
+  st[p] = (isfinite(a) && isfinite(b)) ? STATUS_OK : STATUS_NAN;
+}
+
+__global__ void k_adj_final_ds(FieldView f, uint32_t n, const DS* __restrict__ x, const DS* __restrict__ y,
+                               float* __restrict__ lon, float* __restrict__ lat, double* __restrict__ lon64,
+                               double* __restrict__ lat64) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const double a = (double)f.org_lon + ds_value(x[p]), b = (double)f.org_lat + ds_value(y[p]);
+  if (lon) {
+    lon[p] = (float)a;
+    lat[p] = (float)b;
+  } else {
+    lon64[p] = a;
+    lat64[p] = b;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_adj_forward_ds(FieldView f, const AdjStep* __restrict__ table, int m0, int m1,
+                                                        float dt, uint32_t n, DS* __restrict__ xs, DS* __restrict__ ys,
+                                                        uint8_t* __restrict__ sts, DS* __restrict__ rec_x,
+                                                        DS* __restrict__ rec_y, uint8_t* __restrict__ rec_st,
+                                                        uint32_t* err) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const GeoDS g(f);
+  DS x = xs[p], y = ys[p];
+  uint8_t st = sts[p];
+  uint32_t bits = 0;
+  for (int m = m0; m < m1; ++m) {
+    if (rec_x) {
+      const size_t o = (size_t)(m - m0) * n + p;
+      rec_x[o] = x;
+      rec_y[o] = y;
+      rec_st[o] = st;
+    }
+    if (st != STATUS_OK) continue;
+    VelJac<float> J[4];
+    DS nx, ny;
+    if (rk4_ds(f, g, table[m], dt, x, y, J, nx, ny)) {
+      if (ds_finite(nx) && ds_finite(ny)) {
+        x = nx;
+        y = ny;
+      } else {
+        st = STATUS_NAN;
+        bits |= ERRB_NAN;
+      }
+    } else {
+      st = (ds_finite(x) && ds_finite(y)) ? STATUS_OOB : STATUS_NAN;
+      bits |= st == STATUS_OOB ? (uint32_t)ERRB_OOB : (uint32_t)ERRB_NAN;
+    }
+  }
+  xs[p] = x;
+  ys[p] = y;
+  sts[p] = st;
+  if (bits) atomicOr(err, bits);
+}
+
+__global__ void __launch_bounds__(256) k_adj_step_ds(FieldView f, AdjStep s, float dt, uint32_t n,
+                                                     const DS* __restrict__ xs, const DS* __restrict__ ys,
+                                                     const uint8_t* __restrict__ sts, float* __restrict__ lx,
+                                                     float* __restrict__ ly, float4* __restrict__ rec,
+                                                     uint32_t* __restrict__ key, uint32_t sent,
+                                                     uint32_t* __restrict__ mkey, uint32_t* __restrict__ mcode,
+                                                     uint32_t msent, uint32_t* err) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const GeoDS g(f);
+  VelJac<float> J[4];
+  DS nx, ny;
+  bool ok = sts[p] == STATUS_OK && rk4_ds(f, g, s, dt, xs[p], ys[p], J, nx, ny);
+  ok = ok && ds_finite(nx) && ds_finite(ny);
+  adj_tail<float>(f, p, ok, J[0], J[1], J[2], J[3], dt, lx, ly, rec, key, sent, mkey, mcode, msent, err);
+}
+
+__global__ void __launch_bounds__(256) k_adj_signature_ds(FieldView f, const AdjStep* __restrict__ table, int n_steps,
+                                                          float dt, uint32_t n, const DS* __restrict__ xs,
+                                                          const DS* __restrict__ ys, const uint8_t* __restrict__ sts,
+                                                          unsigned long long* __restrict__ sig) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const GeoDS g(f);
+  DS x = xs[p], y = ys[p];
+  bool live = sts[p] == STATUS_OK;
+  unsigned long long h = 0;
+  const unsigned long long nx = (unsigned long long)f.nx, cw = (unsigned long long)(f.nx - 1);
+  for (int m = 0; m < n_steps && live; ++m) {
+    const AdjStep s = table[m];
+    VelJac<float> J[4];
+    int q = 0;
+#pragma unroll
+    for (; q < 4; ++q) {  // the stages evaluated, up to one that leaves the grid
+      if (!ds_stage(f, g, s, dt, x, y, J, q)) break;
+      h = (h ^ ((J[q].cell / cw) * nx + J[q].cell % cw)) * 0x100000001B3ull;
+    }
+    if (q < 4) break;
+    const DS x1 = ds_add(x, rk4_increment(J[0].flon, J[1].flon, J[2].flon, J[3].flon, dt));
+    const DS y1 = ds_add(y, rk4_increment(J[0].flat, J[1].flat, J[2].flat, J[3].flat, dt));
+    if (!(ds_finite(x1) && ds_finite(y1))) break;
+    x = x1;
+    y = y1;
+  }
+  sig[p] = h;
 }
 
 // Cell path of every microbe over steps [0, n_steps): the grid cell (j * nx + i) of each stage that
@@ -814,6 +1053,8 @@ void launch_adj_init(const FieldView& f, int prec, uint32_t n, const float* lon,
   if (!n) return;
   if (prec == ADJ_F64)
     k_adj_init<double><<<grid_for(n, 256), 256, 0, st>>>(f, n, lon, lat, (double*)x, (double*)y, status);
+  else if (prec == ADJ_DS)
+    k_adj_init_ds<<<grid_for(n, 256), 256, 0, st>>>(f, n, lon, lat, (DS*)x, (DS*)y, status);
   else
     k_adj_init<float><<<grid_for(n, 256), 256, 0, st>>>(f, n, lon, lat, (float*)x, (float*)y, status);
 }
@@ -823,6 +1064,8 @@ void launch_adj_final(const FieldView& f, int prec, uint32_t n, const void* x, c
   if (!n) return;
   if (prec == ADJ_F64)
     k_adj_final<double><<<grid_for(n, 256), 256, 0, st>>>(f, n, (const double*)x, (const double*)y, lon, lat);
+  else if (prec == ADJ_DS)
+    k_adj_final_ds<<<grid_for(n, 256), 256, 0, st>>>(f, n, (const DS*)x, (const DS*)y, lon, lat, nullptr, nullptr);
   else
     k_adj_final<float><<<grid_for(n, 256), 256, 0, st>>>(f, n, (const float*)x, (const float*)y, lon, lat);
 }
@@ -832,6 +1075,8 @@ void launch_adj_final64(const FieldView& f, int prec, uint32_t n, const void* x,
   if (!n) return;
   if (prec == ADJ_F64)
     k_adj_final64<double><<<grid_for(n, 256), 256, 0, st>>>(f, n, (const double*)x, (const double*)y, lon, lat);
+  else if (prec == ADJ_DS)
+    k_adj_final_ds<<<grid_for(n, 256), 256, 0, st>>>(f, n, (const DS*)x, (const DS*)y, nullptr, nullptr, lon, lat);
   else
     k_adj_final64<float><<<grid_for(n, 256), 256, 0, st>>>(f, n, (const float*)x, (const float*)y, lon, lat);
 }
@@ -859,6 +1104,9 @@ void launch_adj_forward(const FieldView& f, int prec, const AdjStep* table, int 
   if (prec == ADJ_F64)
     k_adj_forward<double><<<grid_for(n, 256), 256, 0, st>>>(f, table, m0, m1, dt, n, (double*)x, (double*)y, status,
                                                             (double*)rec_x, (double*)rec_y, rec_st, err);
+  else if (prec == ADJ_DS)
+    k_adj_forward_ds<<<grid_for(n, 256), 256, 0, st>>>(f, table, m0, m1, (float)dt, n, (DS*)x, (DS*)y, status,
+                                                       (DS*)rec_x, (DS*)rec_y, rec_st, err);
   else
     k_adj_forward<float><<<grid_for(n, 256), 256, 0, st>>>(f, table, m0, m1, (float)dt, n, (float*)x, (float*)y, status,
                                                            (float*)rec_x, (float*)rec_y, rec_st, err);
@@ -872,6 +1120,9 @@ void launch_adj_step(const FieldView& f, int prec, const AdjStep& s, double dt, 
     k_adj_step<double><<<grid_for(n, 256), 256, 0, st>>>(f, s, dt, n, (const double*)x, (const double*)y, status,
                                                          (double*)lx, (double*)ly, rec, key, sent, mkey, mcode, msent,
                                                          err);
+  else if (prec == ADJ_DS)
+    k_adj_step_ds<<<grid_for(n, 256), 256, 0, st>>>(f, s, (float)dt, n, (const DS*)x, (const DS*)y, status,
+                                                    (float*)lx, (float*)ly, rec, key, sent, mkey, mcode, msent, err);
   else
     k_adj_step<float><<<grid_for(n, 256), 256, 0, st>>>(f, s, (float)dt, n, (const float*)x, (const float*)y, status,
                                                         (float*)lx, (float*)ly, rec, key, sent, mkey, mcode, msent,
@@ -902,6 +1153,9 @@ void launch_adj_signature(const FieldView& f, int prec, const AdjStep* table, in
   if (prec == ADJ_F64)
     k_adj_signature<double><<<grid_for(n, 256), 256, 0, st>>>(f, table, n_steps, dt, n, (const double*)x,
                                                               (const double*)y, status, sig);
+  else if (prec == ADJ_DS)
+    k_adj_signature_ds<<<grid_for(n, 256), 256, 0, st>>>(f, table, n_steps, (float)dt, n, (const DS*)x, (const DS*)y,
+                                                         status, sig);
   else
     k_adj_signature<float><<<grid_for(n, 256), 256, 0, st>>>(f, table, n_steps, (float)dt, n, (const float*)x,
                                                              (const float*)y, status, sig);

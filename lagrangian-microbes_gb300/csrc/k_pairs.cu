@@ -54,6 +54,16 @@ __device__ __forceinline__ unsigned long long pair_prio(uint32_t i, uint32_t j, 
   return order_hash(i, j, step, ((unsigned long long)k1 << 32) | k0);
 }
 
+// The three rock-paper-scissors outcomes of pair (local ids la, lb) at `step`, as list-entry bits:
+// the pair's Philox uniform (interactions.py:20's np.random.rand(), keyed by the pair) against the
+// ensemble's forward-win threshold of each matchup (interactions.py:24-35), u53 < t exactly as
+// r < p. Only the entry of the endpoint that applies the pair (the lower cell-order index) gets them.
+__device__ __forceinline__ uint32_t win_bits(const EnsInfo& info, uint32_t la, uint32_t lb, uint32_t step) {
+  const PairDraw d = pair_draw(min(la, lb), max(la, lb), step, info.seed_lo, info.seed_hi);
+  return ((d.u53 < info.t_rs ? 1u : 0u) | (d.u53 < info.t_pr ? 2u : 0u) | (d.u53 < info.t_sp ? 4u : 0u))
+         << ENTRY_WIN_SHIFT;
+}
+
 // a before b: higher priority first, ties by lower partner id (one global order on pairs).
 __device__ __forceinline__ bool before(unsigned long long pa, uint32_t ia, unsigned long long pb, uint32_t ib) {
   return pa > pb || (pa == pb && ia < ib);
@@ -142,6 +152,49 @@ __device__ __forceinline__ void append_active(const Bufs& b, Ctrl* ctrl, bool ac
   }
 }
 
+// The outcome draws of a warp's slab lists, spread evenly over its lanes: lane L needs the draws of
+// the entries in `mask` (bit k: entry k), pair (la, lb[k]) of ensemble `ens`. Drawn one slot per
+// lane in turn, at most 8 x 32 per warp, instead of each lane drawing its own (about half the slots
+// of a lattice list need a draw, and the lanes need them at different slots). The bits are merged
+// into e[k]. Every lane of the warp calls this.
+__device__ __forceinline__ void sweep_draws(const Bufs& b, uint32_t step, uint32_t mask, uint32_t la,
+                                            const uint32_t* lb, uint32_t ens, uint32_t* e) {
+  __shared__ uint32_t q_lb[SLOT_BLOCK / 32][32 * SLAB];    // local id of the partner, per draw
+  __shared__ uint16_t q_src[SLOT_BLOCK / 32][32 * SLAB];   // lane * SLAB + slot of the draw
+  __shared__ uint8_t q_bits[SLOT_BLOCK / 32][32 * SLAB];   // outcome bits, by lane * SLAB + slot
+  __shared__ uint32_t w_la[SLOT_BLOCK / 32][32], w_ens[SLOT_BLOCK / 32][32];
+  const uint32_t lane = threadIdx.x & 31u, w = threadIdx.x >> 5;
+  const uint32_t cnt = __popc(mask);
+  uint32_t incl = cnt;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= (uint32_t)o) incl += y;
+  }
+  const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+  if (total == 0) return;
+  uint32_t pos = incl - cnt;
+#pragma unroll
+  for (int k = 0; k < (int)SLAB; ++k) {
+    if ((mask >> k) & 1u) {
+      q_lb[w][pos] = lb[k];
+      q_src[w][pos] = (uint16_t)(lane * SLAB + k);
+      ++pos;
+    }
+  }
+  w_la[w][lane] = la;
+  w_ens[w][lane] = ens;
+  __syncwarp();
+  for (uint32_t q = lane; q < total; q += 32) {
+    const uint32_t src = q_src[w][q], owner = src / SLAB;
+    const EnsInfo& info = b.ens[w_ens[w][owner]];
+    q_bits[w][src] = (uint8_t)(win_bits(info, w_la[w][owner], q_lb[w][q], step) >> ENTRY_WIN_SHIFT);
+  }
+  __syncwarp();
+#pragma unroll
+  for (int k = 0; k < (int)SLAB; ++k)
+    if ((mask >> k) & 1u) e[k] |= (uint32_t)q_bits[w][lane * SLAB + k] << ENTRY_WIN_SHIFT;
+}
+
 __global__ void __launch_bounds__(SLOT_BLOCK) k_sweep(Bufs b, PairParams pp, StepArgs a, Ctrl* ctrl) {
   pdl_wait();
   if (ctrl->halt) return;
@@ -150,6 +203,10 @@ __global__ void __launch_bounds__(SLOT_BLOCK) k_sweep(Bufs b, PairParams pp, Ste
   const uint32_t s = blockIdx.x * SLOT_BLOCK + threadIdx.x;
   bool active = false, is_long = false;
   uint32_t m = 0;
+  // slab lists awaiting their outcome draws: entries, which ones need a draw, local ids, ensemble
+  uint32_t nbo[SLAB], draw_mask = 0, draw_la = 0, draw_lb[SLAB], draw_info = 0;
+#pragma unroll
+  for (int k = 0; k < (int)SLAB; ++k) nbo[k] = draw_lb[k] = 0;
   if (s < n_valid) {
     const Vertex v = load_vertex(b, s);
     const EnsInfo& info = b.ens[v.e];
@@ -202,15 +259,32 @@ __global__ void __launch_bounds__(SLOT_BLOCK) k_sweep(Bufs b, PairParams pp, Ste
     b.deg[s] = m;
     b.level[s] = 0;
     if (m <= SLAB) {
+      // the outcomes of the pairs this vertex applies (partner above it in cell order), drawn by
+      // the whole warp (sweep_draws) and merged into the entries
+      uint32_t need = 0;
 #pragma unroll
       for (int k = 0; k < (int)SLAB; ++k)
-        if ((uint32_t)k < m) b.slab[(size_t)s * SLAB + k] = nb[k];
-      b.wstate[s] = pack_state(m ? nb[0] : NONE, 0u, b.species[b.sid[s]]);  // entry 0 of the list
+        if ((uint32_t)k < m && nb[k] > s) need |= 1u << k;
+      draw_mask = need;
+      draw_la = la;
+#pragma unroll
+      for (int k = 0; k < (int)SLAB; ++k) {
+        draw_lb[k] = pl[k];
+        nbo[k] = nb[k];
+      }
+      draw_info = v.e;
       active = m > 0;
     } else {
       is_long = true;
       b.wstate[s] = pack_state(NONE, 0u, b.species[b.sid[s]]);  // set by k_sweep_long
     }
+  }
+  sweep_draws(b, step, draw_mask, draw_la, draw_lb, draw_info, nbo);
+  if (s < n_valid && m <= SLAB) {
+#pragma unroll
+    for (int k = 0; k < (int)SLAB; ++k)
+      if ((uint32_t)k < m) b.slab[(size_t)s * SLAB + k] = nbo[k];
+    b.wstate[s] = pack_state(m ? nbo[0] : NONE, 0u, b.species[b.sid[s]]);  // entry 0 of the list
   }
   append_active(b, ctrl, active, s);
   // long lists are finished by k_sweep_long
@@ -368,18 +442,18 @@ void launch_count_pairs(const Bufs& b, const PairParams& pp, Ctrl* ctrl, cudaStr
              ctrl);
 }
 
-// In-place sort of one long list (priorities pr, cell-order neighbours nb) into `before` order.
+// In-place sort of one long list (priorities pr, list entries nb) into `before` order.
 __device__ void sort_segment(unsigned long long* __restrict__ pr, uint32_t* __restrict__ nb,
                              const uint32_t* __restrict__ sid, uint32_t d) {
   if (d <= 64) {
     for (uint32_t x = 1; x < d; ++x) {
       const unsigned long long p = pr[x];
-      const uint32_t t = nb[x], it = sid[t];
+      const uint32_t t = nb[x], it = sid[entry_id(t)];
       uint32_t y = x;
       while (y > 0) {
         const unsigned long long q = pr[y - 1];
         const uint32_t u = nb[y - 1];
-        if (!before(p, it, q, sid[u])) break;
+        if (!before(p, it, q, sid[entry_id(u)])) break;
         pr[y] = q;
         nb[y] = u;
         --y;
@@ -394,8 +468,8 @@ __device__ void sort_segment(unsigned long long* __restrict__ pr, uint32_t* __re
     while (true) {
       uint32_t c = 2 * root + 1;
       if (c >= len) break;
-      if (c + 1 < len && before(pr[c], sid[nb[c]], pr[c + 1], sid[nb[c + 1]])) ++c;
-      if (!before(pr[root], sid[nb[root]], pr[c], sid[nb[c]])) break;
+      if (c + 1 < len && before(pr[c], sid[entry_id(nb[c])], pr[c + 1], sid[entry_id(nb[c + 1])])) ++c;
+      if (!before(pr[root], sid[entry_id(nb[root])], pr[c], sid[entry_id(nb[c])])) break;
       const unsigned long long tp = pr[root];
       pr[root] = pr[c];
       pr[c] = tp;
@@ -435,7 +509,7 @@ constexpr uint32_t LONG_BUCKETS = 256;
 
 struct LongSmem {
   unsigned long long p[LONG_SMEM_MAX];  // pair priority of entry i (gather order)
-  uint32_t t[LONG_SMEM_MAX];            // partner's cell-order index
+  uint32_t t[LONG_SMEM_MAX];            // list entry (partner's cell-order index + outcome bits)
   uint16_t ord[LONG_SMEM_MAX];          // entries in list order
   uint32_t start[LONG_BUCKETS], cur[LONG_BUCKETS];
 };
@@ -444,7 +518,7 @@ struct LongSmem {
 __device__ __forceinline__ bool long_before(const Bufs& b, const LongSmem& sh, uint32_t base, uint32_t x, uint32_t y) {
   const unsigned long long px = sh.p[x], py = sh.p[y];
   if (px != py) return px > py;
-  return b.sid[sh.t[x]] - base < b.sid[sh.t[y]] - base;
+  return b.sid[entry_id(sh.t[x])] - base < b.sid[entry_id(sh.t[y])] - base;
 }
 
 // The bucket sort of entries [0, d) of sh into sh.ord (one warp).
@@ -538,7 +612,7 @@ __global__ void __launch_bounds__(LONG_WARPS * 32) k_sweep_long(Bufs b, PairPara
     }
     const unsigned long long o_l = run + incl - d_l;
     run += __shfl_sync(0xffffffffu, incl, 31);
-    uint32_t r0[6], r1[6], la_l = 0, base_l = 0, k0_l = 0, k1_l = 0;
+    uint32_t r0[6], r1[6], la_l = 0, base_l = 0, k0_l = 0, k1_l = 0, e_l = 0;
     int sp_l = 0;
     float px_l = 0.f, py_l = 0.f;
 #pragma unroll
@@ -549,6 +623,7 @@ __global__ void __launch_bounds__(LONG_WARPS * 32) k_sweep_long(Bufs b, PairPara
       const EnsInfo& info = b.ens[v.e];
       k0_l = info.seed_lo;
       k1_l = info.seed_hi;
+      e_l = v.e;
       base_l = v.base;
       const uint32_t id = b.sid[s_l];
       la_l = id - v.base;
@@ -565,6 +640,7 @@ __global__ void __launch_bounds__(LONG_WARPS * 32) k_sweep_long(Bufs b, PairPara
       const uint32_t k0 = __shfl_sync(0xffffffffu, k0_l, k), k1 = __shfl_sync(0xffffffffu, k1_l, k);
       const float2 ps = make_float2(__shfl_sync(0xffffffffu, px_l, k), __shfl_sync(0xffffffffu, py_l, k));
       const int sp = __shfl_sync(0xffffffffu, sp_l, k);
+      const EnsInfo& info = b.ens[__shfl_sync(0xffffffffu, e_l, k)];
       // the six runs as one candidate range: candidate i is in the run q with c[q] <= i < c[q + 1]
       uint32_t t0[6], c[7];
       c[0] = 0;
@@ -601,11 +677,12 @@ __global__ void __launch_bounds__(LONG_WARPS * 32) k_sweep_long(Bufs b, PairPara
             if (pos < d) {
               const uint32_t lb = id[h] - base;
               const unsigned long long p = pair_prio(min(la, lb), max(la, lb), step, k0, k1);
+              const uint32_t e = t[h] > s ? t[h] | win_bits(info, la, lb, step) : t[h];
               if (in_smem) {
                 sh.p[pos] = p;
-                sh.t[pos] = t[h];
+                sh.t[pos] = e;
               } else {
-                b.ovf[o + pos] = t[h];
+                b.ovf[o + pos] = e;
                 b.oprio[o + pos] = p;
               }
             }
@@ -630,7 +707,7 @@ __global__ void __launch_bounds__(LONG_WARPS * 32) k_sweep_long(Bufs b, PairPara
         if (__any_sync(0xffffffffu, has && tie)) {
           // equal priorities go by the partner's local id (the order hash is a bijection of the
           // pair, so this is not expected within one list)
-          const uint32_t li = has ? b.sid[ti] - base : 0u;
+          const uint32_t li = has ? b.sid[entry_id(ti)] - base : 0u;
           for (uint32_t j = 0; j < d; ++j) {
             const unsigned long long pj = __shfl_sync(0xffffffffu, pi, j);
             const uint32_t lj = __shfl_sync(0xffffffffu, li, j);

@@ -12,7 +12,9 @@
 // any schedule that keeps the priority order at every microbe gives the same species: a pair may
 // be applied as soon as it is the highest-priority unprocessed pair of both its microbes.
 // r is drawn from a Philox block keyed by (ensemble seed, step, i, j) (53-bit uniform), and
-// r < p is evaluated exactly as the integer test u53 < ceil(p * 2^53).
+// r < p is evaluated exactly as the integer test u53 < ceil(p * 2^53). The sweep that builds the
+// lists makes these draws and stores the three outcomes (one per matchup) in the list entry of
+// the pair's applier, so applying a pair here is a table lookup on the two species.
 //
 // All pairs are applied by one persistent cooperative launch without grid barriers. Each vertex v
 // publishes the partner of its highest-priority unprocessed pair (NONE when it has none). A pair
@@ -67,42 +69,37 @@ __device__ __forceinline__ bool beats(int x, int y) {
   return (x == 1 && y == 3) || (x == 2 && y == 1) || (x == 3 && y == 2);
 }
 
-// Partner of vertex s at list position h (NONE past the end); lists are read-only here.
+// List entry of vertex s at position h (NONE past the end); lists are read-only here.
 __device__ __forceinline__ uint32_t next_partner(const Bufs& b, uint32_t s, uint32_t h) {
   const uint32_t d = b.deg[s];
   if (h >= d) return NONE;
   return d <= SLAB ? b.slab[(size_t)s * SLAB + h] : b.ovf[(size_t)b.off[s] + h];
 }
 
+// The species both endpoints hold after a pair of species a and b whose applier's list entry is e
+// (the reference's table, interactions.py:24-35): equal species, or a value outside {1, 2, 3},
+// change nothing; otherwise the matchup's outcome bit says whether the forward winner (the species
+// that beats the other) wins, and the loser takes the winner's species. The rule is symmetric in
+// the two endpoints, so the bit needs no orientation.
+__device__ __forceinline__ int rps_outcome(int a, int b, uint32_t e) {
+  if (a == b || a < 1 || a > 3 || b < 1 || b > 3) return -1;  // no change
+  const int c = (a + b == 4) ? 0 : (a + b == 3) ? 1 : 2;  // {1,3} rock/scissors, {1,2} paper/rock, {2,3}
+  const bool fwd_wins = (e >> (ENTRY_WIN_SHIFT + c)) & 1u;
+  return beats(a, b) == fwd_wins ? a : b;
+}
+
 // Apply pair (s, u), s < u in cell order, whose state words ws, wu name each other. Everything
 // the pair needs that other threads write (both species, both list positions) is inside the two
 // words, so no fence is needed: the next applier of either vertex reads the words this one
 // stores. Returns the pair's level when levels are tracked (pair-log runs), else 0.
-__device__ __forceinline__ uint32_t apply_pair(const Bufs& b, uint32_t step, uint32_t s, uint32_t u,
-                                               unsigned long long ws, unsigned long long wu, Ctrl* ctrl) {
+__device__ __forceinline__ uint32_t apply_pair(const Bufs& b, uint32_t s, uint32_t u, unsigned long long ws,
+                                               unsigned long long wu, Ctrl* ctrl) {
   const uint32_t hs = state_pos(ws), hu = state_pos(wu);
   const uint32_t ns = next_partner(b, s, hs + 1u), nu = next_partner(b, u, hu + 1u);
   const uint32_t pa = b.sid[s], pb = b.sid[u];
-  const bool s_is_i = pa < pb;  // i < j are the pair's slots (local ids are slot - base)
-  const uint32_t pi = s_is_i ? pa : pb, pj = s_is_i ? pb : pa;
-  const int si = state_species(s_is_i ? ws : wu), sj = state_species(s_is_i ? wu : ws);
-  int ni = si, nj = sj;
-  if (si != sj) {
-    const EnsInfo& info = b.ens[b.sens[s]];
-    unsigned long long t = 0;
-    bool valid = true;
-    if ((si == 1 && sj == 3) || (si == 3 && sj == 1)) t = info.t_rs;
-    else if ((si == 2 && sj == 1) || (si == 1 && sj == 2)) t = info.t_pr;
-    else if ((si == 3 && sj == 2) || (si == 2 && sj == 3)) t = info.t_sp;
-    else valid = false;  // species outside {1,2,3}: the reference's table has no case -> no change
-    if (valid) {
-      const PairDraw d = pair_draw(pi - info.base, pj - info.base, step, info.seed_lo, info.seed_hi);
-      const bool fwd_wins = d.u53 < t;
-      if (beats(si, sj) == fwd_wins) nj = si;  // i wins: j takes i's species
-      else ni = sj;                            // j wins
-    }
-  }
-  const int new_s = s_is_i ? ni : nj, new_u = s_is_i ? nj : ni;
+  const int o = rps_outcome(state_species(ws), state_species(wu), state_partner(ws));
+  const int new_s = o < 0 ? state_species(ws) : o, new_u = o < 0 ? state_species(wu) : o;
+  const uint32_t pi = min(pa, pb), pj = max(pa, pb);
   uint32_t level = 0;
   if (b.plog) {  // pair-log runs: levels live outside the state words, so order them with fences
     __threadfence();
@@ -164,33 +161,6 @@ __device__ __forceinline__ uint32_t tl_entry(const Bufs& b, const TileSmem& t, u
   return d <= SLAB ? t.lst[h * TL_VMAX + l] : b.ovf[(size_t)t.lst[l] + h];
 }
 
-// Species of the pair (a, b) after the rock-paper-scissors rule (the reference's table, Philox
-// draw); `vertex` is a's cell-order index, which names the pair's ensemble.
-__device__ __forceinline__ void rps_pair(const Bufs& b, uint32_t vertex, uint32_t step, uint32_t pa, uint32_t pb,
-                                         unsigned long long wa, unsigned long long wb, int* new_a, int* new_b) {
-  const bool a_is_i = pa < pb;
-  const uint32_t pi = a_is_i ? pa : pb, pj = a_is_i ? pb : pa;
-  const int si = state_species(a_is_i ? wa : wb), sj = state_species(a_is_i ? wb : wa);
-  int ni = si, nj = sj;
-  if (si != sj) {
-    const EnsInfo& info = b.ens[b.sens[vertex]];  // the ensemble is read only when a draw may be needed
-    unsigned long long t = 0;
-    bool valid = true;
-    if ((si == 1 && sj == 3) || (si == 3 && sj == 1)) t = info.t_rs;
-    else if ((si == 2 && sj == 1) || (si == 1 && sj == 2)) t = info.t_pr;
-    else if ((si == 3 && sj == 2) || (si == 2 && sj == 3)) t = info.t_sp;
-    else valid = false;  // species outside {1,2,3}: the reference's table has no case -> no change
-    if (valid) {
-      const PairDraw d = pair_draw(pi - info.base, pj - info.base, step, info.seed_lo, info.seed_hi);
-      const bool fwd_wins = d.u53 < t;
-      if (beats(si, sj) == fwd_wins) nj = si;
-      else ni = sj;
-    }
-  }
-  *new_a = a_is_i ? ni : nj;
-  *new_b = a_is_i ? nj : ni;
-}
-
 // The pairs among cell-order vertices [g_lo, g_hi) (a group of whole ensembles, so no pair leaves
 // it), at most TL_VMAX per block: each block owns an equal share of whole RD_THREADS-vertex columns.
 __device__ void tl_group(const Bufs& b, uint32_t step, Ctrl* ctrl, unsigned long long t0, uint32_t g_lo,
@@ -241,11 +211,12 @@ __device__ void tl_group(const Bufs& b, uint32_t step, Ctrl* ctrl, unsigned long
       if (!((live >> k) & 1u)) continue;
       const uint32_t l = threadIdx.x + (uint32_t)k * RD_THREADS, s = lo + l;
       const unsigned long long ws = ld_sh(t.w + l);
-      const uint32_t u = state_partner(ws);
-      if (u == NONE) {
+      const uint32_t ue = state_partner(ws);  // s's current list entry
+      if (ue == NONE) {
         live &= ~(1u << k);
         continue;
       }
+      const uint32_t u = entry_id(ue);
       const bool u_local = u >= lo && u < hi;
       if (s > u) {
         // the owner of u applies; while u is outside the block, take the result from global memory.
@@ -258,38 +229,41 @@ __device__ void tl_group(const Bufs& b, uint32_t step, Ctrl* ctrl, unsigned long
         continue;
       }
       const unsigned long long wu = u_local ? ld_sh(t.w + (u - lo)) : ld_relaxed(b.wstate + u);
-      if (state_partner(wu) != s) continue;
+      if (state_partner(wu) != s) continue;  // u's entry of a pair it does not apply carries no bits
       // apply (s, u): this thread owns the lower endpoint
       const uint32_t hs = state_pos(ws), hu = state_pos(wu);
       const uint32_t ns = tl_entry(b, t, l, hs + 1u);
-      uint32_t nu, pu;
+      uint32_t nu;
       if (u_local) {
         nu = tl_entry(b, t, u - lo, hu + 1u);
-        pu = t.sid[u - lo];
       } else {
         const uint32_t du = b.deg[u];
         nu = hu + 1u < du ? (du <= SLAB ? b.slab[(size_t)u * SLAB + hu + 1u] : b.ovf[(size_t)b.off[u] + hu + 1u]) : NONE;
-        pu = b.sid[u];
       }
-      const uint32_t ps = t.sid[l];
-      int new_s, new_u;
-      rps_pair(b, s, step, ps, pu, ws, wu, &new_s, &new_u);
-      if (nu == NONE) b.species[pu] = (int8_t)new_u;
-      if (ns == NONE) b.species[ps] = (int8_t)new_s;
+      const int o = rps_outcome(state_species(ws), state_species(wu), ue);
+      const int new_s = o < 0 ? state_species(ws) : o, new_u = o < 0 ? state_species(wu) : o;
       const unsigned long long nwu = pack_state(nu, hu + 1u, new_u), nws = pack_state(ns, hs + 1u, new_s);
+      const uint32_t nu_id = entry_id(nu), ns_id = entry_id(ns);
       if (u_local) {
         st_sh(t.w + (u - lo), nwu);
-        if (nu != NONE && (nu < lo || nu >= hi)) st_relaxed(b.wstate + u, nwu);  // u's next pair crosses
+        if (nu != NONE && (nu_id < lo || nu_id >= hi)) st_relaxed(b.wstate + u, nwu);  // u's next pair crosses
       } else {
         st_relaxed(b.wstate + u, nwu);  // u's owner pulls it
       }
       st_sh(t.w + l, nws);
-      if (ns != NONE && (ns < lo || ns >= hi)) st_relaxed(b.wstate + s, nws);  // s's next pair crosses
+      if (ns != NONE && (ns_id < lo || ns_id >= hi)) st_relaxed(b.wstate + s, nws);  // s's next pair crosses
     }
     if (live && ((++polls & 63u) == 0u) && globaltimer() - t0 > ROUNDS_TIMEOUT_NS) {
       atomicOr(&ctrl->err, (uint32_t)ERRB_TIMEOUT);
       break;
     }
+  }
+  // every owned list is done (its word names no partner, and no one writes a vertex's word after
+  // its last pair): the words hold the final species, written back once per vertex
+#pragma unroll
+  for (int k = 0; k < TL_VPT; ++k) {
+    const uint32_t l = threadIdx.x + (uint32_t)k * RD_THREADS;
+    if (l < nloc && t.deg[l]) b.species[t.sid[l]] = (int8_t)state_species(ld_sh(t.w + l));
   }
 }
 
@@ -398,16 +372,16 @@ __global__ void __launch_bounds__(RD_THREADS) k_rounds(Bufs b, StepArgs a, Ctrl*
         ws[k] = (live >> k) & 1u ? ld_relaxed(b.wstate + sv[k]) : (unsigned long long)NONE;
 #pragma unroll
       for (int k = 0; k < POLL_BATCH; ++k) {
-        const uint32_t u = state_partner(ws[k]);
+        const uint32_t u = entry_id(state_partner(ws[k]));
         wu[k] = NONE;
-        if (u == NONE) live &= ~(1u << k);
+        if (state_partner(ws[k]) == NONE) live &= ~(1u << k);
         else if (sv[k] < u) wu[k] = ld_relaxed(b.wstate + u);
       }
 #pragma unroll
       for (int k = 0; k < POLL_BATCH; ++k) {
-        const uint32_t u = state_partner(ws[k]);
-        if (u != NONE && sv[k] < u && state_partner(wu[k]) == sv[k])
-          max_level = max(max_level, apply_pair(b, step, sv[k], u, ws[k], wu[k], ctrl));
+        const uint32_t u = entry_id(state_partner(ws[k]));
+        if (state_partner(ws[k]) != NONE && sv[k] < u && state_partner(wu[k]) == sv[k])
+          max_level = max(max_level, apply_pair(b, sv[k], u, ws[k], wu[k], ctrl));
       }
       if (live && ((++polls & 63u) == 0u) && globaltimer() - t0 > ROUNDS_TIMEOUT_NS) {
         atomicOr(&ctrl->err, (uint32_t)ERRB_TIMEOUT);
@@ -429,18 +403,18 @@ __global__ void __launch_bounds__(RD_THREADS) k_rounds(Bufs b, StepArgs a, Ctrl*
       }
 #pragma unroll
       for (int k = 0; k < POLL_BATCH; ++k) {
-        const uint32_t u = state_partner(ws[k]);
+        const uint32_t u = entry_id(state_partner(ws[k]));
         wu[k] = NONE;
-        if (u != NONE) {
+        if (state_partner(ws[k]) != NONE) {
           pending = true;
           if (sv[k] < u) wu[k] = ld_relaxed(b.wstate + u);
         }
       }
 #pragma unroll
       for (int k = 0; k < POLL_BATCH; ++k) {
-        const uint32_t u = state_partner(ws[k]);
-        if (u != NONE && sv[k] < u && state_partner(wu[k]) == sv[k])
-          max_level = max(max_level, apply_pair(b, step, sv[k], u, ws[k], wu[k], ctrl));
+        const uint32_t u = entry_id(state_partner(ws[k]));
+        if (state_partner(ws[k]) != NONE && sv[k] < u && state_partner(wu[k]) == sv[k])
+          max_level = max(max_level, apply_pair(b, sv[k], u, ws[k], wu[k], ctrl));
       }
     }
     if (pending && ((++polls & 63u) == 0u) && globaltimer() - t0 > ROUNDS_TIMEOUT_NS) {

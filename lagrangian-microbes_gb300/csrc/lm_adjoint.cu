@@ -49,11 +49,12 @@ struct lm_adjoint {
   uint32_t n = 0;
   int n_steps = 0, K = 0, n_ck = 0;
   double dt = 0.0;
-  int prec = ADJ_F32;  // working precision of the recorded run
-  int prec_next = ADJ_F32;
+  int prec = ADJ_DS;  // working precision of the recorded run
+  int prec_next = ADJ_DS;
   DBuf<AdjStep> table;
   std::vector<AdjStep> table_h;
-  DBuf<unsigned char> x, y, ck_x, ck_y, seg_x, seg_y, lx, ly, fin_x, fin_y;  // T-typed, T chosen by `prec`
+  // positions of adj_state_bytes(prec) per element; adjoint state lx, ly of adj_lambda_bytes(prec)
+  DBuf<unsigned char> x, y, ck_x, ck_y, seg_x, seg_y, lx, ly, fin_x, fin_y;
   DBuf<float> csum;
   DBuf<uint8_t> st, ck_st, seg_st;
   DBuf<float4> rec;
@@ -170,9 +171,9 @@ int lm_adjoint_destroy(lm_adjoint* a) {
 
 int lm_adjoint_set_precision(lm_adjoint* a, int precision) {
   if (!a) return LM_ERR_ARG;
-  if (precision != LM_ADJ_F32 && precision != LM_ADJ_F64)
-    return afail(a, LM_ERR_ARG, "precision must be LM_ADJ_F32 or LM_ADJ_F64 (got %d)", precision);
-  a->prec_next = precision == LM_ADJ_F64 ? ADJ_F64 : ADJ_F32;
+  if (precision != LM_ADJ_F32 && precision != LM_ADJ_F64 && precision != LM_ADJ_DS)
+    return afail(a, LM_ERR_ARG, "precision must be LM_ADJ_F32, LM_ADJ_F64 or LM_ADJ_DS (got %d)", precision);
+  a->prec_next = precision == LM_ADJ_F64 ? ADJ_F64 : precision == LM_ADJ_DS ? ADJ_DS : ADJ_F32;
   return LM_OK;
 }
 
@@ -210,7 +211,7 @@ int lm_adjoint_forward(lm_adjoint* a, const float* u, const float* v, int nt, in
   const int n_ck = (n_steps + checkpoint_every - 1) / checkpoint_every;
   const size_t M = (size_t)4 * N;
   const int prec = a->prec_next;
-  const size_t es = prec == ADJ_F64 ? sizeof(double) : sizeof(float);
+  const size_t es = adj_state_bytes(prec);  // lx, ly need no more (adj_lambda_bytes)
   int r;
   if ((r = grow(a, a->uv, fe)) || (r = grow(a, a->table, (size_t)n_steps)) || (r = grow(a, a->x, es * N)) ||
       (r = grow(a, a->y, es * N)) || (r = grow(a, a->st, N)) || (r = grow(a, a->ck_x, es * n_ck * N)) ||
@@ -284,7 +285,7 @@ int lm_adjoint_backward(lm_adjoint* a, const float* g_lon, const float* g_lat, f
   const uint32_t sent = 4u * cells;
   const int kb = key_bits_for(sent);
   const uint32_t M = 4u * N;
-  const size_t es = a->prec == ADJ_F64 ? sizeof(double) : sizeof(float);
+  const size_t es = adj_state_bytes(a->prec);
   const uint32_t cw = (uint32_t)(a->nx - 1), ch = (uint32_t)(a->ny - 1);
   const int kbm = key_bits_for(2u * cells);
   int r;

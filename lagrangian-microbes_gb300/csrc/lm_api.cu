@@ -67,8 +67,6 @@ struct lm_ctx {
   unsigned long long* wstate = nullptr;
   uint32_t* act = nullptr;
   float2* spos = nullptr;
-  float *rlon = nullptr, *rlat = nullptr;  // caller-order staging (E > 1)
-  int8_t* rsp = nullptr;
   uint32_t ens_cap = 0;
   EnsGrid* grids = nullptr;
   uint32_t* eord = nullptr;
@@ -109,6 +107,19 @@ struct lm_ctx {
   // pair log
   uint32_t* plog = nullptr;
   uint32_t plog_cap = 0;
+
+  // step records of lm_step (rec_lon / rec_lat / rec_species): every step's record is packed into
+  // one slot of a device ring (caller order), and copied to the caller's arrays on the copy stream
+  // rec_st REC_SLOTS - 1 steps later, so the copies of step k overlap the kernels of the next steps
+  // instead of holding up the compute stream.
+  static constexpr int REC_SLOTS = 3;
+  cudaStream_t rec_st = nullptr;
+  unsigned char* rec_ring = nullptr;
+  size_t rec_slot = 0;  // bytes per slot: lon [n] float, lat [n] float, species [n] int8
+  cudaEvent_t rec_done[REC_SLOTS] = {}, rec_copied[REC_SLOTS] = {};
+  std::vector<int64_t> rec_pending;  // steps whose records wait in the ring, oldest first
+  float *rec_lon = nullptr, *rec_lat = nullptr;
+  int8_t* rec_sp = nullptr;
 
   int rgrid = 0, rblock = 0;
 
@@ -205,9 +216,19 @@ void prof_collect(lm_ctx* c) {
     prof_end(c, id, pa_);            \
   } while (0)
 
+// Forget the captured graph: its kernels hold the buffers' addresses and the field geometry by
+// value, so it is stale once a buffer is reallocated or a field is uploaded (capture again).
+void drop_graph(lm_ctx* c) {
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  if (c->graph) cudaGraphDestroy(c->graph);
+  c->gexec = nullptr;
+  c->graph = nullptr;
+}
+
 template <class T>
 int dalloc(lm_ctx* c, T** p, size_t count) {
   if (*p) {
+    drop_graph(c);  // a captured graph holds the old address
     cudaFree(*p);
     *p = nullptr;
   }
@@ -260,7 +281,6 @@ int ensure_slots(lm_ctx* c, uint32_t slots, uint32_t n_ens) {
         (r = dalloc(c, &c->slab, (size_t)cap * SLAB)) || (r = dalloc(c, &c->off, cap)) ||
         (r = dalloc(c, &c->longv, cap)) || (r = dalloc(c, &c->wstate, cap)) ||
         (r = dalloc(c, &c->level, cap)) || (r = dalloc(c, &c->act, cap)) || (r = dalloc(c, &c->spos, cap)) ||
-        (r = dalloc(c, &c->rlon, cap)) || (r = dalloc(c, &c->rlat, cap)) || (r = dalloc(c, &c->rsp, cap)) ||
         (r = dalloc(c, &c->map_d, cap)) || (r = dalloc(c, &c->block_ens, nblk)))
       return r;
     c->slot_cap = cap;
@@ -293,7 +313,9 @@ int layout(lm_ctx* c, uint32_t n_ens, const int64_t* counts) {
     base[e] = (uint32_t)slot;
     slot += cnt[e];
     total += cnt[e];
-    if (slot > 0x7fffff00ull) return fail(c, LM_ERR_ARG, "too many particles");
+    if (slot > MAX_SLOTS)
+      return fail(c, LM_ERR_ARG, "too many particles: a context holds at most %llu slots",
+                  (unsigned long long)MAX_SLOTS);
   }
   int r;
   if ((r = ensure_slots(c, (uint32_t)slot, n_ens))) return r;
@@ -527,23 +549,90 @@ int check_time(lm_ctx* c, double t, double dt, int64_t n_steps) {
 
 void set_pair_params(lm_ctx* c, double r, int norm) { c->pp = make_pair_params(r, norm, (float)c->cell_factor); }
 
-// Copies of one step's records into caller-order host arrays.
-int record_step(lm_ctx* c, int64_t k, float* rec_lon, float* rec_lat, int8_t* rec_species) {
+// The record ring: slots sized for the current particle count, the copy stream and the events.
+int ensure_rec_ring(lm_ctx* c) {
+  const size_t n = c->ntotal;
+  const size_t slot = (9 * n + 255) / 256 * 256;
+  if (!c->rec_st) {
+    CK(cudaStreamCreateWithFlags(&c->rec_st, cudaStreamNonBlocking));
+    for (int q = 0; q < lm_ctx::REC_SLOTS; ++q) {
+      CK(cudaEventCreateWithFlags(&c->rec_done[q], cudaEventDisableTiming));
+      CK(cudaEventCreateWithFlags(&c->rec_copied[q], cudaEventDisableTiming));
+    }
+  }
+  if (slot > c->rec_slot) {
+    if (c->rec_ring) {
+      CK(cudaStreamSynchronize(c->rec_st));
+      cudaFree(c->rec_ring);
+      c->rec_ring = nullptr;
+      c->rec_slot = 0;
+    }
+    const cudaError_t e = cudaMalloc(&c->rec_ring, slot * lm_ctx::REC_SLOTS);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return fail(c, LM_ERR_OOM, "cudaMalloc of the %zu-byte record ring failed: %s", slot * lm_ctx::REC_SLOTS,
+                  cudaGetErrorString(e));
+    }
+    c->rec_slot = slot;
+  }
+  return LM_OK;
+}
+
+// Copy the oldest pending record from its ring slot to the caller's arrays (copy stream, after the
+// step that packed it). Copies into pageable memory return once they are done; the compute stream
+// keeps running the steps queued behind that record meanwhile.
+int flush_record(lm_ctx* c) {
+  const int64_t k = c->rec_pending.front();
+  c->rec_pending.erase(c->rec_pending.begin());
+  const int q = (int)(k % lm_ctx::REC_SLOTS);
+  const size_t n = c->ntotal;
+  unsigned char* slot = c->rec_ring + (size_t)q * c->rec_slot;
+  CK(cudaStreamWaitEvent(c->rec_st, c->rec_done[q], 0));
+  if (c->rec_lon) CK(cudaMemcpyAsync(c->rec_lon + k * n, slot, n * 4, cudaMemcpyDeviceToHost, c->rec_st));
+  if (c->rec_lat) CK(cudaMemcpyAsync(c->rec_lat + k * n, slot + n * 4, n * 4, cudaMemcpyDeviceToHost, c->rec_st));
+  if (c->rec_sp) CK(cudaMemcpyAsync(c->rec_sp + k * n, slot + n * 8, n, cudaMemcpyDeviceToHost, c->rec_st));
+  CK(cudaEventRecord(c->rec_copied[q], c->rec_st));
+  return LM_OK;
+}
+
+// Every pending record in the caller's arrays.
+int flush_records(lm_ctx* c) {
+  int r;
+  while (!c->rec_pending.empty())
+    if ((r = flush_record(c))) return r;
+  if (c->rec_st) CK(cudaStreamSynchronize(c->rec_st));
+  return LM_OK;
+}
+
+// One step's record (positions before the kick, species after the step) into a ring slot in
+// caller order; its copy to the host follows REC_SLOTS - 1 steps later (flush_record).
+int record_step(lm_ctx* c, int64_t k) {
   const uint32_t n = c->ntotal;
-  if (!n) return LM_OK;
+  if (!n || !(c->rec_lon || c->rec_lat || c->rec_sp)) return LM_OK;
+  const int q = (int)(k % lm_ctx::REC_SLOTS);
+  unsigned char* slot = c->rec_ring + (size_t)q * c->rec_slot;
+  float* lon = reinterpret_cast<float*>(slot);
+  float* lat = reinterpret_cast<float*>(slot + (size_t)n * 4);
+  int8_t* sp = reinterpret_cast<int8_t*>(slot + (size_t)n * 8);
+  CK(cudaStreamWaitEvent(c->st, c->rec_copied[q], 0));  // the slot's previous copy has read it
   const bool direct = (c->n_ens == 1);
-  if (rec_lon) {
-    if (!direct) launch_unpad(c->plon, c->rlon, c->map_d, c->nslots, c->st);
-    CK(cudaMemcpyAsync(rec_lon + k * n, direct ? c->plon : c->rlon, n * sizeof(float), cudaMemcpyDeviceToHost, c->st));
+  if (c->rec_lon) {
+    if (direct) CK(cudaMemcpyAsync(lon, c->plon, n * 4, cudaMemcpyDeviceToDevice, c->st));
+    else launch_unpad(c->plon, lon, c->map_d, c->nslots, c->st);
   }
-  if (rec_lat) {
-    if (!direct) launch_unpad(c->plat, c->rlat, c->map_d, c->nslots, c->st);
-    CK(cudaMemcpyAsync(rec_lat + k * n, direct ? c->plat : c->rlat, n * sizeof(float), cudaMemcpyDeviceToHost, c->st));
+  if (c->rec_lat) {
+    if (direct) CK(cudaMemcpyAsync(lat, c->plat, n * 4, cudaMemcpyDeviceToDevice, c->st));
+    else launch_unpad(c->plat, lat, c->map_d, c->nslots, c->st);
   }
-  if (rec_species) {
-    if (!direct) launch_unpad8(c->species, c->rsp, c->map_d, c->nslots, c->st);
-    CK(cudaMemcpyAsync(rec_species + k * n, direct ? c->species : c->rsp, n, cudaMemcpyDeviceToHost, c->st));
+  if (c->rec_sp) {
+    if (direct) CK(cudaMemcpyAsync(sp, c->species, n, cudaMemcpyDeviceToDevice, c->st));
+    else launch_unpad8(c->species, sp, c->map_d, c->nslots, c->st);
   }
+  CK(cudaEventRecord(c->rec_done[q], c->st));
+  c->rec_pending.push_back(k);
+  int r;
+  while ((int)c->rec_pending.size() >= lm_ctx::REC_SLOTS)
+    if ((r = flush_record(c))) return r;
   return LM_OK;
 }
 
@@ -552,6 +641,10 @@ int run_steps(lm_ctx* c, double t, double dt, int64_t n_steps, int64_t step0, ui
   int r;
   if ((r = write_ctrl_step(c, step0))) return r;
   if (rec_census && (r = ensure_hstage(c, (size_t)4 * n_steps))) return r;
+  c->rec_lon = rec_lon;
+  c->rec_lat = rec_lat;
+  c->rec_sp = rec_species;
+  if ((rec_lon || rec_lat || rec_species) && (r = ensure_rec_ring(c))) return r;
   int64_t s = 0;
   bool redo = false;
   while (s < n_steps) {
@@ -567,11 +660,12 @@ int run_steps(lm_ctx* c, double t, double dt, int64_t n_steps, int64_t step0, ui
       const StepArgs an = step_args(t + dt * (k + 1), dt, step0 + k + 1, kh, false);
       CK(enqueue_step(c, a, flags, !(redo && k == s), chained, chain ? &an : nullptr));
       chained = chain;
-      if ((r = record_step(c, k, rec_lon, rec_lat, rec_species))) return r;
+      if ((r = record_step(c, k))) return r;
       if (rec_census)
         CK(cudaMemcpyAsync(c->hstage + 4 * k, c->ctrl->census, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->st));
     }
     CK(cudaGetLastError());
+    if ((r = flush_records(c))) return r;  // (a halted step's record is written again by its redo)
     if ((r = read_ctrl(c))) return r;
     if (c->hctrl->halt) {
       const int64_t k = (int64_t)c->hctrl->halt_step - step0;
@@ -605,10 +699,7 @@ int stage_positions(lm_ctx* c, int64_t n, const float* lon, const float* lat) {
 }
 
 int capture(lm_ctx* c) {
-  if (c->gexec) cudaGraphExecDestroy(c->gexec);
-  if (c->graph) cudaGraphDestroy(c->graph);
-  c->gexec = nullptr;
-  c->graph = nullptr;
+  drop_graph(c);
   CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
   c->capturing = true;
   for (int k = 0; k < c->g_spg; ++k) {
@@ -710,7 +801,7 @@ int lm_ctx_destroy(lm_ctx* c) {
   if (c->graph) cudaGraphDestroy(c->graph);
   void* bufs_[] = {c->uv,     c->xo,    c->yo,     c->plon,   c->plat,   c->species, c->status, c->key,
                    c->rank,   c->sid,   c->skey,   c->sens,   c->deg,    c->slab,    c->off,    c->longv,
-                   c->wstate, c->level,  c->act,    c->spos,   c->rlon,    c->rlat,   c->rsp,
+                   c->wstate, c->level,  c->act,    c->spos,
                    c->map_d,  c->block_ens, c->ens_d, c->grids, c->eord, c->ebox, c->census,  c->ccount, c->cstart,
                    c->csum,   c->ovf,   c->oprio,  c->ctrl,   c->plog,  c->snap_xo, c->snap_yo, c->snap_sp,
                    c->snap_st};
@@ -718,6 +809,15 @@ int lm_ctx_destroy(lm_ctx* c) {
     if (p) cudaFree(p);
   if (c->hctrl) cudaFreeHost(c->hctrl);
   if (c->hstage) cudaFreeHost(c->hstage);
+  if (c->rec_st) {
+    cudaStreamSynchronize(c->rec_st);
+    cudaStreamDestroy(c->rec_st);
+  }
+  if (c->rec_ring) cudaFree(c->rec_ring);
+  for (int q = 0; q < lm_ctx::REC_SLOTS; ++q) {
+    if (c->rec_done[q]) cudaEventDestroy(c->rec_done[q]);
+    if (c->rec_copied[q]) cudaEventDestroy(c->rec_copied[q]);
+  }
   for (auto& p : c->pend) {
     cudaEventDestroy(p.a);
     cudaEventDestroy(p.b);
@@ -760,6 +860,7 @@ int lm_field_upload_batch(lm_ctx* c, int n_fields, const float* u, const float* 
   if (!uniform_axis(lat, ny, &dy)) return fail(c, LM_ERR_GRID, "latitude axis is not uniform and ascending");
   if (!uniform_axis(t_sec, nt, &dT)) return fail(c, LM_ERR_GRID, "time axis is not uniform and ascending");
   CK(cudaSetDevice(c->device));
+  drop_graph(c);  // the graph's steps carry the old field geometry and time axis
   const size_t per = (size_t)nt * ny * nx;
   const size_t n = per * (size_t)n_fields;
   int r;
@@ -1081,7 +1182,7 @@ int lm_query_pairs(lm_ctx* c, int64_t n, const float* lon, const float* lat, int
   pairs.reserve((size_t)c->hctrl->n_dir / 2);
   for (uint32_t s = 0; s < nv; ++s)
     for (uint32_t h = 0; h < deg[s]; ++h) {
-      const uint32_t t = deg[s] <= SLAB ? slab[(size_t)s * SLAB + h] : ovf[(size_t)off[s] + h];
+      const uint32_t t = entry_id(deg[s] <= SLAB ? slab[(size_t)s * SLAB + h] : ovf[(size_t)off[s] + h]);
       const uint32_t a_ = ids[s], b_ = ids[t];
       if (a_ < b_) pairs.push_back(((uint64_t)a_ << 32) | b_);
     }
@@ -1210,7 +1311,8 @@ int lm_graph_capture(lm_ctx* c, double t_start, double dt_sec, int64_t step0, in
 
 int lm_graph_run(lm_ctx* c, int n_launches, int sync) {
   if (!c) return LM_ERR_ARG;
-  if (!c->gexec) return fail(c, LM_ERR_STATE, "no captured graph");
+  if (!c->gexec)
+    return fail(c, LM_ERR_STATE, "no captured graph (capture again after a field upload or a change of capacity)");
   if (n_launches < 0) return fail(c, LM_ERR_ARG, "n_launches < 0");
   CK(cudaSetDevice(c->device));
   const int64_t first = c->next_step;

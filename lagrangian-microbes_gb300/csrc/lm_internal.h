@@ -34,6 +34,17 @@ constexpr uint32_t SLAB = 8;           // neighbour-list entries kept in the per
 constexpr uint8_t STATUS_OK = 0, STATUS_OOB = 1, STATUS_NAN = 2, STATUS_PAD = 3;
 constexpr uint32_t MAX_DEGREE = (1u << 24) - 1;  // list positions take 24 bits of the state word
 
+// Neighbour-list entry: the partner's cell-order index in bits 0-28 and, on the entries of the
+// lower endpoint of a pair (the endpoint that applies it), the pair's three rock-paper-scissors
+// outcomes in bits 29-31: bit 29 + c is set when the pair's Philox uniform lies below the
+// forward-win threshold of matchup c (0 rock/scissors, 1 paper/rock, 2 scissors/paper). The draw
+// is made once, in the sweep that builds the list, instead of in the interaction's dependency
+// chain. Indices stay below ENTRY_ID_MASK, so an entry never equals NONE.
+constexpr uint32_t ENTRY_ID_MASK = (1u << 29) - 1;
+constexpr uint32_t ENTRY_WIN_SHIFT = 29;
+constexpr uint64_t MAX_SLOTS = ENTRY_ID_MASK - 1;
+__host__ __device__ inline uint32_t entry_id(uint32_t e) { return e & ENTRY_ID_MASK; }
+
 // Interaction state word of a vertex: its current species, the position of its current pair in
 // its list, and that pair's partner (NONE once the list is done).
 __host__ __device__ inline unsigned long long pack_state(uint32_t partner, uint32_t pos, int species) {
@@ -301,7 +312,12 @@ struct AdjStep {
   float w[3];
   double wd[3];  // the weights in float64 (FP64-trajectory mode)
 };
-enum AdjPrecision { ADJ_F32 = 0, ADJ_F64 = 1 };
+// Working precision of the adjoint tape: ADJ_F32 the engine's float32 arithmetic, ADJ_F64 float64
+// state and arithmetic, ADJ_DS double-float positions with float32 velocities and adjoint state.
+enum AdjPrecision { ADJ_F32 = 0, ADJ_F64 = 1, ADJ_DS = 2 };
+// Bytes of one position coordinate / one adjoint coordinate in each precision.
+inline size_t adj_state_bytes(int prec) { return prec == ADJ_F32 ? 4 : 8; }
+inline size_t adj_lambda_bytes(int prec) { return prec == ADJ_F64 ? 8 : 4; }
 constexpr int RS_BITS_MAX = 10;                      // digit width of one radix pass
 constexpr uint32_t RS_RADIX_MAX = 1u << RS_BITS_MAX;
 
@@ -315,8 +331,9 @@ struct AdjSortBufs {
 
 void launch_adj_stages(const FieldView& f, double t_start, double dt, int n_steps, AdjStep* table, uint32_t* err,
                        cudaStream_t st);
-// Per-microbe kernels in precision `prec` (ADJ_F32: float state, the engine's arithmetic; ADJ_F64:
-// double state and arithmetic); x, y, lx, ly point to arrays of that type.
+// Per-microbe kernels in precision `prec`: x, y point to position arrays of adj_state_bytes(prec)
+// per element (float, double, or a double-float pair), lx, ly to adjoint arrays of
+// adj_lambda_bytes(prec) (float, or double for ADJ_F64).
 void launch_adj_init(const FieldView& f, int prec, uint32_t n, const float* lon, const float* lat, void* x, void* y,
                      uint8_t* status, cudaStream_t st);
 void launch_adj_final(const FieldView& f, int prec, uint32_t n, const void* x, const void* y, float* lon, float* lat,

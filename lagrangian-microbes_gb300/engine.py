@@ -62,6 +62,7 @@ class Simulation:
         self.ctx.call("lm_field_upload", _lib.ptr(fld.u), _lib.ptr(fld.v), nt, ny, nx, _lib.ptr(fld.lon),
                       _lib.ptr(fld.lat), _lib.ptr(fld.times))
         self.field = fld
+        self._graph = None  # a captured graph holds the previous field: capture again
 
     def upload_particles(self, lons, lats, species=None) -> None:
         lons = np.ascontiguousarray(lons, dtype=np.float64).ravel()
@@ -289,6 +290,8 @@ class EnsembleSimulation(Simulation):
         v = np.ascontiguousarray(np.stack([f.v for f in flds])) if len(flds) > 1 else f0.v
         self.ctx.call("lm_field_upload_batch", len(flds), _lib.ptr(u), _lib.ptr(v), nt, ny, nx, _lib.ptr(f0.lon),
                       _lib.ptr(f0.lat), _lib.ptr(f0.times))
+        self.field = f0
+        self._graph = None  # a captured graph holds the previous fields: capture again
 
     def split(self, flat):
         """Split a per-microbe array (last axis) into a list per ensemble."""

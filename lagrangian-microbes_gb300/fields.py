@@ -83,16 +83,43 @@ class PsiModes:
         return (self.amp * self.ky * s).sum(-1), (-self.amp * self.kx * s).sum(-1)
 
 
-def synthetic_psi_field(lon_min: float, lon_max: float, lat_min: float, lat_max: float, resolution: float,
-                        n_frames: int, frame_seconds: float = 3600.0, n_modes: int = 32,
-                        wavelength_km=(50.0, 500.0), rms_speed: float = 0.2, period_days: float = 10.0,
-                        seed: int = 0, epoch: datetime | None = None, with_modes: bool = False):
-    """Seeded streamfunction field sampled on a regular lon/lat grid.
+@dataclass
+class PsiBasis:
+    """A seeded synthetic field before it is sampled in time: every frame is a mix of four basis
+    fields, u(t) = us cos(w t) + uc sin(w t), v(t) = vs cos(w t) + vc sin(w t). ``frames(first, n)``
+    samples frames first .. first + n - 1 (times frame_seconds * k), bit-identical to the same frames
+    of one long sampling, so a long run can stream its field in windows."""
 
-    Wavelengths are log-uniform in ``wavelength_km``, directions and phases uniform; every mode has
-    the same velocity amplitude (psi amplitude proportional to its wavelength). Coordinates are a
-    local tangent plane at the domain centre: x = R cos(lat0) dlon, y = R dlat.
-    """
+    lon: np.ndarray
+    lat: np.ndarray
+    us: np.ndarray
+    uc: np.ndarray
+    vs: np.ndarray
+    vc: np.ndarray
+    omega: float
+    frame_seconds: float
+    epoch: datetime
+    modes: PsiModes
+
+    def frames(self, first: int, n_frames: int) -> VelocityField:
+        ny, nx = self.us.shape
+        times = self.frame_seconds * np.arange(first, first + n_frames, dtype=np.float64)
+        u = np.empty((n_frames, ny, nx), dtype=np.float32)
+        v = np.empty((n_frames, ny, nx), dtype=np.float32)
+        chunk = max(1, int(4e6 // (nx * ny)))
+        for f0 in range(0, n_frames, chunk):
+            f1 = min(n_frames, f0 + chunk)
+            c = np.cos(self.omega * times[f0:f1])[:, None, None]
+            s = np.sin(self.omega * times[f0:f1])[:, None, None]
+            u[f0:f1] = self.us * c + self.uc * s
+            v[f0:f1] = self.vs * c + self.vc * s
+        return VelocityField(lon=self.lon, lat=self.lat, times=times, u=u, v=v, epoch=self.epoch)
+
+
+def psi_basis(lon_min: float, lon_max: float, lat_min: float, lat_max: float, resolution: float,
+              frame_seconds: float = 3600.0, n_modes: int = 32, wavelength_km=(50.0, 500.0), rms_speed: float = 0.2,
+              period_days: float = 10.0, seed: int = 0, epoch: datetime | None = None) -> PsiBasis:
+    """The basis fields of synthetic_psi_field (same arguments, same seed -> same field)."""
     rng = np.random.default_rng(seed)
     nx = int(round((lon_max - lon_min) / resolution)) + 1
     ny = int(round((lat_max - lat_min) / resolution)) + 1
@@ -127,22 +154,25 @@ def synthetic_psi_field(lon_min: float, lon_max: float, lat_min: float, lat_max:
     scale = rms_speed / np.sqrt(np.mean(us * us + vs * vs))
     us *= scale; uc *= scale; vs *= scale; vc *= scale
     omega = 2 * np.pi / (period_days * 86400.0)
+    modes = PsiModes(kx=kx, ky=ky, phase=phase, amp=amp * scale, lon0=lon0, lat0=lat0, omega=omega, radius_m=radius_m)
+    return PsiBasis(lon=lon, lat=lat, us=us, uc=uc, vs=vs, vc=vc, omega=omega, frame_seconds=frame_seconds,
+                    epoch=epoch or datetime(2017, 1, 1), modes=modes)
 
-    times = frame_seconds * np.arange(n_frames, dtype=np.float64)
-    u = np.empty((n_frames, ny, nx), dtype=np.float32)
-    v = np.empty((n_frames, ny, nx), dtype=np.float32)
-    chunk = max(1, int(4e6 // (nx * ny)))
-    for f0 in range(0, n_frames, chunk):
-        f1 = min(n_frames, f0 + chunk)
-        c = np.cos(omega * times[f0:f1])[:, None, None]
-        s = np.sin(omega * times[f0:f1])[:, None, None]
-        u[f0:f1] = us * c + uc * s
-        v[f0:f1] = vs * c + vc * s
-    fld = VelocityField(lon=lon, lat=lat, times=times, u=u, v=v, epoch=epoch or datetime(2017, 1, 1))
-    if with_modes:
-        return fld, PsiModes(kx=kx, ky=ky, phase=phase, amp=amp * scale, lon0=lon0, lat0=lat0, omega=omega,
-                             radius_m=radius_m)
-    return fld
+
+def synthetic_psi_field(lon_min: float, lon_max: float, lat_min: float, lat_max: float, resolution: float,
+                        n_frames: int, frame_seconds: float = 3600.0, n_modes: int = 32,
+                        wavelength_km=(50.0, 500.0), rms_speed: float = 0.2, period_days: float = 10.0,
+                        seed: int = 0, epoch: datetime | None = None, with_modes: bool = False):
+    """Seeded streamfunction field sampled on a regular lon/lat grid.
+
+    Wavelengths are log-uniform in ``wavelength_km``, directions and phases uniform; every mode has
+    the same velocity amplitude (psi amplitude proportional to its wavelength). Coordinates are a
+    local tangent plane at the domain centre: x = R cos(lat0) dlon, y = R dlat.
+    """
+    basis = psi_basis(lon_min, lon_max, lat_min, lat_max, resolution, frame_seconds, n_modes, wavelength_km,
+                      rms_speed, period_days, seed, epoch)
+    fld = basis.frames(0, n_frames)
+    return (fld, basis.modes) if with_modes else fld
 
 
 def uniform_field(lon_min, lon_max, lat_min, lat_max, resolution, n_frames, u0=0.2, v0=0.0,

@@ -19,6 +19,7 @@ import glob
 import logging
 import os
 import pickle
+from concurrent.futures import ThreadPoolExecutor
 from datetime import timedelta
 
 import numpy as np
@@ -107,24 +108,38 @@ class ParticleAdvecter:
                                    seed=self.seed, kh=self.Kh, device=self.device)
         return self._sim
 
+    def _write_chunk(self, out, times, iteration, iters_to_do):
+        """The per-tile pickles of one chunk (particle_advecter.py:246-249's file names and dicts)."""
+        per = self.particles_per_tile
+        for tile_id in range(self.N_procs):
+            chunk = {"time": times, "lat": np.ascontiguousarray(out["lat"][:, tile_id * per:(tile_id + 1) * per]),
+                     "lon": np.ascontiguousarray(out["lon"][:, tile_id * per:(tile_id + 1) * per])}
+            path = os.path.join(self.output_dir, _chunk_name(iteration, iteration + iters_to_do, tile_id))
+            with open(path, "wb") as f:
+                pickle.dump(chunk, f, protocol=pickle.HIGHEST_PROTOCOL)
+
     def time_step(self, start_time, end_time, dt):
+        """Advect for (end_time - start_time) // dt steps, writing a chunk of positions every
+        output_chunk_iters steps. Chunk k is pickled by a writer thread while the GPU computes chunk
+        k + 1 (at most one chunk waits to be written); within a chunk, each step's positions are
+        copied to the host while the next steps compute."""
         sim = self._engine()
         logger.info("Starting time stepping: %s -> %s (dt=%s) on the GPU.", start_time, end_time, dt)
         t = start_time
         iteration = self.iteration
-        per = self.particles_per_tile
-        while t < end_time:
-            iters_to_do = min(self.output_chunk_iters, (end_time - t) // dt)
-            out = sim.step(t, dt, iters_to_do, interact=False, record=True, step0=iteration)
-            times = [t + (n + 1) * dt for n in range(iters_to_do)]
-            for tile_id in range(self.N_procs):
-                chunk = {"time": times, "lat": np.ascontiguousarray(out["lat"][:, tile_id * per:(tile_id + 1) * per]),
-                         "lon": np.ascontiguousarray(out["lon"][:, tile_id * per:(tile_id + 1) * per])}
-                path = os.path.join(self.output_dir, _chunk_name(iteration, iteration + iters_to_do, tile_id))
-                with open(path, "wb") as f:
-                    pickle.dump(chunk, f, protocol=pickle.HIGHEST_PROTOCOL)
-            t = t + iters_to_do * dt
-            iteration += iters_to_do
+        with ThreadPoolExecutor(max_workers=1) as writer:
+            pending = None
+            while t < end_time:
+                iters_to_do = min(self.output_chunk_iters, (end_time - t) // dt)
+                out = sim.step(t, dt, iters_to_do, interact=False, record=True, step0=iteration)
+                times = [t + (n + 1) * dt for n in range(iters_to_do)]
+                if pending is not None:
+                    pending.result()  # raises what the writer raised
+                pending = writer.submit(self._write_chunk, out, times, iteration, iters_to_do)
+                t = t + iters_to_do * dt
+                iteration += iters_to_do
+            if pending is not None:
+                pending.result()
         self.iteration += (end_time - start_time) // dt
 
     def newest_stored_positions(self):

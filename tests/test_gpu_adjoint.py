@@ -1,6 +1,7 @@
 """GPU adjoint of the advection (lm_adjoint_*, k_adjoint.cu) against its FP64 checkers.
 
-* the tape's forward is bit-identical to the fused engine's advection (lm_step, no kick);
+* the tape's forward in "f32" precision is bit-identical to the fused engine's advection (lm_step,
+  no kick); the default "ds" precision carries positions in double-float;
 * dL/d(lon0, lat0) and dL/d(u, v) agree with an FP64 torch autograd of the same scheme
   (oracle/adjoint_ref.py) and with FP64 central finite differences of the C oracle along random
   directions (h = 1e-6 deg for positions, 1e-6 m/s for the field);
@@ -109,7 +110,8 @@ def test_adjoint_forward_bit_identical_to_engine_advection(lm, small_field):
     np.testing.assert_array_equal(y, want_lat)
 
 
-def test_adjoint_matches_fp64_autograd_and_finite_differences(lm, orc, small_field):
+@pytest.mark.parametrize("precision", ["f32", "ds"])
+def test_adjoint_matches_fp64_autograd_and_finite_differences(lm, orc, small_field, precision):
     """Gradients within 1e-4 relative of the FP64 scheme, microbe by microbe on the same cell path.
 
     The map is piecewise smooth: moving a start by 0.1 m moves the FP64 gradient itself by ~1e-4
@@ -119,14 +121,14 @@ def test_adjoint_matches_fp64_autograd_and_finite_differences(lm, orc, small_fie
     f = small_field
     lon, lat, tlon, tlat = _case(f, 3000, 2)
     t0, dt, n_steps = float(f.times[0]), 3600.0, 48
-    _, _, loss32, g, sig = _gpu_grads(f, lon, lat, tlon, tlat, t0, dt, n_steps, 16)
+    _, _, loss32, g, sig = _gpu_grads(f, lon, lat, tlon, tlat, t0, dt, n_steps, 16, precision=precision)
     same = sig == _fp64_signature(orc, f, lon, lat, t0, dt, n_steps)
     assert same.mean() >= 0.97, same.mean()
     loss64, g64 = _fp64_grads(f, lon, lat, tlon, tlat, t0, dt, n_steps)
     assert abs(loss32 - loss64) <= 1e-5 * loss64
     errs = [_rel(a, b) for a, b in zip(g, g64)]
     assert max(errs) < 1e-3, errs  # all microbes, cell-edge crossings included
-    _, _, _, gs, _ = _gpu_grads(f, lon, lat, tlon, tlat, t0, dt, n_steps, 16, weight=same)
+    _, _, _, gs, _ = _gpu_grads(f, lon, lat, tlon, tlat, t0, dt, n_steps, 16, weight=same, precision=precision)
     _, g64s = _fp64_grads(f, lon, lat, tlon, tlat, t0, dt, n_steps, weight=same)
     errs = [_rel(a, b) for a, b in zip(gs, g64s)]
     assert max(errs) < 1e-4, errs
@@ -139,7 +141,7 @@ def test_adjoint_matches_fp64_autograd_and_finite_differences(lm, orc, small_fie
         d = [rng.standard_normal(a.shape) for a in (lon, lat, f.u, f.v)]
         fd, keep = central_difference(orc, f, lon, lat, tlon, tlat, t0, dt, n_steps, d, path=sig)
         dropped = max(dropped, int((~keep).sum()))
-        _, _, _, gk, _ = _gpu_grads(f, lon, lat, tlon, tlat, t0, dt, n_steps, 16, weight=keep)
+        _, _, _, gk, _ = _gpu_grads(f, lon, lat, tlon, tlat, t0, dt, n_steps, 16, weight=keep, precision=precision)
         ads.append(sum(float((gg * dd).sum()) for gg, dd in zip(gk, d)))
         fds.append(fd)
     ads, fds = np.array(ads), np.array(fds)
@@ -148,13 +150,14 @@ def test_adjoint_matches_fp64_autograd_and_finite_differences(lm, orc, small_fie
     assert np.median(np.abs(ads - fds) / np.abs(fds)) < 1e-4
 
 
-def test_adjoint_gradient_is_deterministic_across_runs_and_checkpoint_intervals(lm, small_field):
+@pytest.mark.parametrize("precision", ["f32", "ds"])
+def test_adjoint_gradient_is_deterministic_across_runs_and_checkpoint_intervals(lm, small_field, precision):
     f = small_field
     lon, lat, tlon, tlat = _case(f, 20000, 3)
     t0, dt, n_steps = float(f.times[0]), 3600.0, 30
-    ref = _gpu_grads(f, lon, lat, tlon, tlat, t0, dt, n_steps, 30)
+    ref = _gpu_grads(f, lon, lat, tlon, tlat, t0, dt, n_steps, 30, precision=precision)
     for k in (30, 1, 7):
-        got = _gpu_grads(f, lon, lat, tlon, tlat, t0, dt, n_steps, k)
+        got = _gpu_grads(f, lon, lat, tlon, tlat, t0, dt, n_steps, k, precision=precision)
         np.testing.assert_array_equal(got[0], ref[0])
         for a, b in zip(got[3], ref[3]):
             np.testing.assert_array_equal(a, b)

@@ -13,8 +13,9 @@ compared with
   positions, h = 1e-6 deg; +-1 m/s per node for u and v, h = 1e-6), over the microbes whose +h and
   -h runs and the GPU run sample the same cells.
 
-The scheme being differentiated is the reference's pset.execute(AdvectionRK4)
-(particle_advecter.py:220-223).
+"ds" is the tape's default precision (double-float positions, float32 velocities and adjoint
+state); "f64" carries float64 state. The scheme being differentiated is the reference's
+pset.execute(AdvectionRK4) (particle_advecter.py:220-223).
 """
 
 import numpy as np

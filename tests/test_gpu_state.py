@@ -78,3 +78,29 @@ def test_loaded_kernels_are_sm103a(lm):
     sm = ctypes.c_int(0)
     assert _lib.load().lm_kernel_arch(ctypes.byref(sm)) == _lib.LM_OK
     assert sm.value == 103
+
+
+def test_field_window_upload_keeps_the_state_and_drops_the_graph(lm, orc):
+    """A long run can stream its field in windows of frames: uploading the next window keeps the
+    microbes (same grid, same origin) and forgets the captured graph, whose steps hold the old
+    field; after capturing again the run continues exactly as with the whole field."""
+    from lagrangian_microbes_gb300 import LMError
+    from lagrangian_microbes_gb300.fields import psi_basis
+    basis = psi_basis(190.0, 215.0, 15.0, 40.0, 1.0 / 12.0, seed=3)
+    lons, lats = orc.lattice(20000, 25.0, 26.0, 200.0, 201.0)
+    sp = np.random.default_rng(2).integers(1, 4, lons.size).astype(np.int8)
+    whole = lm.Simulation(basis.frames(0, 14), lons, lats, sp, radius=0.01, p_rs=0.7, p_pr=0.6, p_sp=0.8, seed=5)
+    whole.capture(0.0, 3600.0, 4, step0=0)
+    whole.run_graph(3)
+    win = lm.Simulation(basis.frames(0, 7), lons, lats, sp, radius=0.01, p_rs=0.7, p_pr=0.6, p_sp=0.8, seed=5)
+    win.capture(0.0, 3600.0, 6, step0=0)
+    win.run_graph(1)
+    win.upload_field(basis.frames(6, 7))
+    with pytest.raises(LMError, match="no captured graph"):
+        win.ctx.call("lm_graph_run", 1, 1)
+    win.capture(6 * 3600.0, 3600.0, 6, step0=6)
+    win.run_graph(1)
+    for a, b in zip(whole.state(), win.state()):
+        np.testing.assert_array_equal(a, b)
+    whole.close()
+    win.close()
