@@ -423,8 +423,11 @@ def run_e2e(fld, lons, lats, species, K, spg, local, stream):
     t0 = time.perf_counter()
     sim = Simulation(fld, lons, lats, species, radius=RADIUS, p_rs=P_WIN, p_pr=P_WIN, p_sp=P_WIN, seed=SEED,
                      device=local)
+    ta = time.perf_counter()
     sim.capture(0.0, DT, spg, step0=0)
+    tb = time.perf_counter()
     sim.run_graph(K, sync=True)
+    tc = time.perf_counter()
     lon, lat, sp, st = sim.state()
     t1 = time.perf_counter()
     sim.close()
@@ -433,6 +436,7 @@ def run_e2e(fld, lons, lats, species, K, spg, local, stream):
     d2h = lon.nbytes + lat.nbytes + sp.nbytes + st.nbytes
     return {"value": n * K * spg / (t1 - t0), "unit": "microbe-steps/s", "h2d_bytes_per_step": h2d / K,
             "d2h_bytes_per_step": d2h / K, "seconds": t1 - t0,
+            "phases_s": {"context_and_uploads": ta - t0, "capture": tb - ta, "steps": tc - tb, "download": t1 - tc},
             "note": "setup (field + particles upload, graph capture) + 720 steps + state download, wall clock"}
 
 

@@ -14,8 +14,11 @@ compared with
   -h runs and the GPU run sample the same cells.
 
 "ds" is the tape's default precision (double-float positions, float32 velocities and adjoint
-state); "f64" carries float64 state. The scheme being differentiated is the reference's
-pset.execute(AdvectionRK4) (particle_advecter.py:220-223).
+state): its directional derivatives are within 1e-4 of FP64 finite differences (the bar of the
+differentiation configuration), and its gradient vectors within 1e-3 of the FP64 autograd (its
+trajectories sit a few centimetres from the FP64 ones, and the float32 velocities and Jacobians
+leave ~5e-4 per component). "f64" carries float64 state and meets 1e-4 on both. The scheme being
+differentiated is the reference's pset.execute(AdvectionRK4) (particle_advecter.py:220-223).
 """
 
 import numpy as np
@@ -43,7 +46,7 @@ def config_d(lm, orc):
     return f, lon, lat, tlon[sel].copy(), tlat[sel].copy()
 
 
-@pytest.mark.parametrize("precision", ["f64"])
+@pytest.mark.parametrize("precision", ["ds", "f64"])
 def test_config_d_gradients_match_fp64_autograd_and_finite_differences(orc, config_d, precision):
     import adjoint_ref
     from test_gpu_adjoint import _fp64_grads, _fp64_signature, _gpu_grads, _rel
@@ -58,7 +61,7 @@ def test_config_d_gradients_match_fp64_autograd_and_finite_differences(orc, conf
     _, _, _, gs, _ = _gpu_grads(f, lon, lat, tlon, tlat, t0, dt, STEPS, K, weight=same, precision=precision)
     _, g64 = _fp64_grads(f, lon, lat, tlon, tlat, t0, dt, STEPS, weight=same)
     errs = [_rel(a, b) for a, b in zip(gs, g64)]
-    assert max(errs) < 1e-4, errs
+    assert max(errs) < (1e-4 if precision == "f64" else 1e-3), errs
 
     # 64 directions of FP64 central differences (error of the vector of directional derivatives, and
     # the median per direction)
