@@ -223,9 +223,11 @@ __global__ void __launch_bounds__(SLOT_BLOCK) k_sweep(Bufs b, PairParams pp, Ste
     // phase 1: collect the neighbours (compile-time slots, predicated); the divergent candidate
     // loop does no more than the distance test
     for_neighbours(b, pp, v, [&](uint32_t t) {
+      // shift register: the newest neighbour in slot 0 (the slots are sorted below; entries past
+      // the eighth are collected again by the long-list kernel)
 #pragma unroll
-      for (int k = 0; k < (int)SLAB; ++k)
-        if ((uint32_t)k == m) nb[k] = t;
+      for (int k = (int)SLAB - 1; k > 0; --k) nb[k] = nb[k - 1];
+      nb[0] = t;
       ++m;
     });
     // phase 2: priorities over the slots, a loop whose trip count (the degree) is nearly the same
@@ -241,21 +243,27 @@ __global__ void __launch_bounds__(SLOT_BLOCK) k_sweep(Bufs b, PairParams pp, Ste
         }
       }
     }
-    if (m > 1 && m <= SLAB) {
-      // 19-comparator sorting network for 8 entries; empty slots (priority 0, partner NONE) sort last
+    // sorting network; empty slots (priority 0, partner NONE) sort last. When no list of the warp
+    // has more than 4 entries (most of a lattice), the 5-comparator network of 4 entries suffices.
 #define LM_CX(x, y)                                         \
   if (before(pr[y], pl[y], pr[x], pl[x])) {                  \
     const unsigned long long tp = pr[x]; pr[x] = pr[y]; pr[y] = tp; \
     const uint32_t tn = nb[x]; nb[x] = nb[y]; nb[y] = tn;    \
     const uint32_t tl = pl[x]; pl[x] = pl[y]; pl[y] = tl;    \
   }
+    if (__all_sync(__activemask(), m <= 4)) {
+      if (m > 1) {
+        LM_CX(0, 1) LM_CX(2, 3) LM_CX(0, 2) LM_CX(1, 3) LM_CX(1, 2)
+      }
+    } else if (m > 1 && m <= SLAB) {
+      // 19-comparator network for 8 entries
       LM_CX(0, 2) LM_CX(1, 3) LM_CX(4, 6) LM_CX(5, 7)
       LM_CX(0, 4) LM_CX(1, 5) LM_CX(2, 6) LM_CX(3, 7)
       LM_CX(0, 1) LM_CX(2, 3) LM_CX(4, 5) LM_CX(6, 7)
       LM_CX(2, 4) LM_CX(3, 5) LM_CX(1, 4) LM_CX(3, 6)
       LM_CX(1, 2) LM_CX(3, 4) LM_CX(5, 6)
-#undef LM_CX
     }
+#undef LM_CX
     b.deg[s] = m;
     b.level[s] = 0;
     if (m <= SLAB) {

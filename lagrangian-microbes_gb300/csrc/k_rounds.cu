@@ -38,11 +38,14 @@
 
 namespace lm {
 
-// 512 threads: two blocks per SM hold 2 x 2,048 vertices in 2 x 96 KB of shared memory. Against
-// four blocks of 256 (the same vertices per SM) a block's range has a shorter edge for its area,
-// so fewer pairs hand off through global memory (at 256 ensembles: 11.6 -> 10.4 ms per step;
-// 1,024 threads were faster there still but slower on the clustered 490k lattice).
-constexpr int RD_THREADS = 512;
+// 1,024 threads owning two vertices each: two blocks per SM hold 2 x 2,048 vertices in 2 x 96 KB of
+// shared memory and keep 2,048 threads resident (32 registers each). The kernel is latency bound
+// (dependent shared-memory loads, polls of words written by other threads), so the doubled number
+// of resident warps against blocks of 512 threads owning four vertices each shortens it: 74 -> 66 us
+// per launch on the first day of the 490k run, 107 -> 90 us on its last day. Against blocks of 256
+// (the same vertices per SM) a block's range has a shorter edge for its area, so fewer pairs hand
+// off through global memory.
+constexpr int RD_THREADS = 1024;
 constexpr unsigned long long ROUNDS_TIMEOUT_NS = 2000000000ull;  // 2 s
 
 __device__ __forceinline__ unsigned long long globaltimer() {
@@ -122,7 +125,7 @@ __device__ __forceinline__ uint32_t apply_pair(const Bufs& b, uint32_t s, uint32
   return level;
 }
 
-constexpr int POLL_BATCH = 4;  // vertices whose state words one thread loads before testing them
+constexpr int POLL_BATCH = 2;  // vertices whose state words one thread loads before testing them
 
 // ---- tile-local interaction: block-owned vertex ranges with handshakes in shared memory ----
 //
@@ -136,7 +139,7 @@ constexpr int POLL_BATCH = 4;  // vertices whose state words one thread loads be
 // shared memory. As in the global path, only the applier of a vertex's current pair writes the
 // vertex's word, so no fences are needed.
 static_assert(SLAB == 8, "the tile path copies a slab row as two 16-byte loads");
-constexpr int TL_VPT = 4;                              // vertices per thread at most
+constexpr int TL_VPT = 2;                              // vertices per thread at most
 constexpr uint32_t TL_VMAX = RD_THREADS * TL_VPT;      // vertices per block at most
 constexpr size_t TL_SMEM = TL_VMAX * (8 + 4 + 4 + 4 * SLAB);  // words, slot ids, degrees, lists
 
@@ -329,7 +332,7 @@ __device__ bool rounds_tiled(const Bufs& b, uint32_t step, Ctrl* ctrl, unsigned 
   return true;
 }
 
-__global__ void __launch_bounds__(RD_THREADS) k_rounds(Bufs b, StepArgs a, Ctrl* ctrl) {
+__global__ void __launch_bounds__(RD_THREADS, 2) k_rounds(Bufs b, StepArgs a, Ctrl* ctrl) {
   pdl_wait();
   if (((volatile uint32_t*)&ctrl->halt)[0]) return;
   if (a.test_wait_ns) {

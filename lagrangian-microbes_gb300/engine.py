@@ -152,18 +152,24 @@ class Simulation:
 
     # ---- stepping ----
     def step(self, t0, dt, n_steps: int, interact: bool = True, census: bool = False, log_pairs: bool = False,
-             record: bool = False, step0: int | None = None, count_pairs: bool = False):
+             record: bool = False, step0: int | None = None, count_pairs: bool = False, out: dict | None = None):
         """Run n_steps plain steps from field time t0. Returns a dict of the requested records.
 
         ``count_pairs`` replaces the interaction by a count of the pairs within the radius (no lists):
-        the count of the last step is ``stats()["pairs"]``, their sum ``stats()["pairs_total"]``."""
+        the count of the last step is ``stats()["pairs"]``, their sum ``stats()["pairs_total"]``.
+        ``out`` (with ``record``) supplies the record arrays: {"lon", "lat", "species"} of at least
+        [n_steps, N] (float32, float32, int8; C order). Reusing them from call to call saves the
+        page faults of fresh host memory, which cost ~10x the copies themselves."""
         n = self.n
         interact = interact and not count_pairs
         flags = STEP_ADVECT | (STEP_INTERACT if interact else 0) | (STEP_CENSUS if census else 0)
         flags |= STEP_COUNT_PAIRS if count_pairs else 0
         flags |= STEP_LOG_PAIRS if log_pairs else 0
         rec_lon = rec_lat = rec_sp = rec_c = None
-        if record:
+        if record and out is not None:
+            rec_lon, rec_lat, rec_sp = (_record_view(out, k, dt_, n_steps, n) for k, dt_ in
+                                        (("lon", np.float32), ("lat", np.float32), ("species", np.int8)))
+        elif record:
             rec_lon = np.empty((n_steps, n), np.float32)
             rec_lat = np.empty((n_steps, n), np.float32)
             rec_sp = np.empty((n_steps, n), np.int8)
@@ -236,6 +242,14 @@ class Simulation:
 
     def close(self) -> None:
         self.ctx.close()
+
+
+def _record_view(out: dict, key: str, dtype, n_steps: int, n: int) -> np.ndarray:
+    """The first n_steps rows of a caller-supplied record array, checked."""
+    a = out[key]
+    if a.dtype != dtype or a.ndim != 2 or a.shape[0] < n_steps or a.shape[1] != n or not a.flags["C_CONTIGUOUS"]:
+        raise ValueError(f"out[{key!r}] must be a C-contiguous {np.dtype(dtype).name} array of at least [{n_steps}, {n}]")
+    return a[:n_steps]
 
 
 class EnsembleSimulation(Simulation):

@@ -101,6 +101,7 @@ class ParticleAdvecter:
         self.seed = int(seed)
         self.device = device
         self._sim = None
+        self._records = None
 
     def _engine(self) -> Simulation:
         if self._sim is None:
@@ -127,11 +128,20 @@ class ParticleAdvecter:
         logger.info("Starting time stepping: %s -> %s (dt=%s) on the GPU.", start_time, end_time, dt)
         t = start_time
         iteration = self.iteration
+        # two record buffers, reused from chunk to chunk: the GPU fills one while the writer pickles
+        # the other (fresh host memory would be page-faulted in by every chunk's copies)
+        if self._records is None:
+            shape = (self.output_chunk_iters, self.N_particles)
+            self._records = [{"lon": np.zeros(shape, np.float32), "lat": np.zeros(shape, np.float32),
+                              "species": np.zeros(shape, np.int8)} for _ in range(2)]
+        chunk = 0
         with ThreadPoolExecutor(max_workers=1) as writer:
             pending = None
             while t < end_time:
                 iters_to_do = min(self.output_chunk_iters, (end_time - t) // dt)
-                out = sim.step(t, dt, iters_to_do, interact=False, record=True, step0=iteration)
+                out = sim.step(t, dt, iters_to_do, interact=False, record=True, step0=iteration,
+                               out=self._records[chunk % 2])
+                chunk += 1
                 times = [t + (n + 1) * dt for n in range(iters_to_do)]
                 if pending is not None:
                     pending.result()  # raises what the writer raised
