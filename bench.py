@@ -170,7 +170,8 @@ def run_gb300(args):
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     sim.set_stream(stream.cuda_stream)
-    cell_factor, tune = sim.autotune(0.0, DT, 3)  # binning cell size; results do not depend on it
+    tuned = sim.autotune_all(0.0, DT, 3)  # cell size and launch shapes; results do not depend on them
+    cell_factor = tuned["cell_factor"]
     sim.capture(0.0, DT, spg, step0=0)
     sim.run_graph(W, sync=True)  # warm-up (also grows neighbour lists if needed)
 
@@ -300,7 +301,7 @@ def run_gb300(args):
             "config": {"workload": WORKLOAD, "microbes": n, "sim_steps_per_bench_step": spg,
                        "sim_steps_timed": sim_steps, "parallelism": f"replicas x{world}",
                        "l2": "512 MiB buffer written between timed bench steps", "form": "cuda-graph, 24 steps/launch",
-                       "cell_factor": cell_factor, "autotune_s": tune},
+                       "tuning": {k: v for k, v in tuned.items() if k != "seconds"}, "autotune_s": tuned["seconds"]},
             "pairs_per_step": pairs_per_step,
             "plain": {"value": plain_value, "unit": "microbe-steps/s", "sim_steps": plain_steps,
                       "graph_speedup": value / world / plain_value},
@@ -571,7 +572,8 @@ def run_batched(local: int, stream):
     total = int(sum(x[0].size for x in ens))
     sim = EnsembleSimulation(fields, ens, radius=RADIUS, p_rs=ps, p_pr=ps, p_sp=ps, seeds=seeds, device=local)
     sim.set_stream(stream.cuda_stream)
-    cell_factor, _ = sim.autotune(0.0, DT, 2)
+    tuned = sim.autotune_all(0.0, DT, 2)
+    cell_factor = tuned["cell_factor"]
     # per-kernel time of two plain steps (CUDA events around each launch)
     sim.upload_ensembles(ens)
     sim.ctx.profile_enable(True)
@@ -621,7 +623,7 @@ def run_batched(local: int, stream):
                 "long_lists": stats["long_lists"],
                 "graph": {"value": gv, "unit": "microbe-steps/s", "ms_per_sim_step": g_ms / B_STEPS,
                           "form": "one context, one CUDA graph of 24 fused steps for all ensembles",
-                          "cell_factor": cell_factor},
+                          "tuning": {k: v for k, v in tuned.items() if k != "seconds"}},
                 "plain_per_ensemble": {"value": pv, "unit": "microbe-steps/s", "ms_per_sim_step": p_ms / B_STEPS,
                                        "form": "one context per ensemble, per-step launches, ensembles one after another"},
                 "batched_over_plain": gv / pv, "kernels_ms_per_step": prof_ms}

@@ -148,6 +148,17 @@ int lm_set_ensemble_params(lm_ctx* ctx, int n_ens, const double* p_rs, const dou
                            const uint64_t* seeds);
 /* Binning cell size in units of the radius (default 1.004; any value >= 1.004 gives the same pairs). */
 int lm_set_cell_factor(lm_ctx* ctx, double factor);
+/* Launch shapes of the step kernels, chosen by an autotuner (Simulation.autotune): no knob changes
+ * any result, only the speed. LM_TUNE_ROUNDS_THREADS: interaction blocks of 1024 threads owning two
+ * vertices each (default) or 512 owning four; LM_TUNE_LONG_BLOCKS_PER_SM: blocks per SM of the
+ * long-neighbour-list kernel (1..32, default 6); LM_TUNE_ADVECT_THREADS: advection threads per
+ * block, 128 or 256 (default). Setting a knob forgets the captured graph (capture again). No
+ * counterpart in the reference (its parallelism is joblib tiles, particle_advecter.py:143-148). */
+#define LM_TUNE_ROUNDS_THREADS 1
+#define LM_TUNE_LONG_BLOCKS_PER_SM 2
+#define LM_TUNE_ADVECT_THREADS 3
+int lm_set_tuning(lm_ctx* ctx, int knob, int value);
+int lm_get_tuning(lm_ctx* ctx, int knob, int* value);
 
 /* n_steps fused steps starting at field time t_sec with global step index step0. Each step:
  * advect (flags & LM_STEP_ADVECT), then bin + pair + interact (flags & LM_STEP_INTERACT) on the

@@ -33,6 +33,10 @@ STEP_CENSUS = 4
 STEP_LOG_PAIRS = 8
 STEP_COUNT_PAIRS = 16
 
+TUNE_ROUNDS_THREADS = 1
+TUNE_LONG_BLOCKS_PER_SM = 2
+TUNE_ADVECT_THREADS = 3
+
 NORM_INF = 0
 NORM_L1 = 1
 NORM_L2 = 2
@@ -106,6 +110,8 @@ SIGNATURES = {
     "lm_ensembles_upload": [P, I32, P, P, P, P],
     "lm_set_ensemble_params": [P, I32, P, P, P, P],
     "lm_set_cell_factor": [P, F64],
+    "lm_set_tuning": [P, I32, I32],
+    "lm_get_tuning": [P, I32, ctypes.POINTER(I32)],
     "lm_census_get": [P, P, I64],
     "lm_particles_upload": [P, I64, P, P, P],
     "lm_particles_download": [P, P, P, P, P],

@@ -32,9 +32,10 @@ void launch_interleave(const float* u, const float* v, float2* uv, size_t n, cud
   k_interleave<<<grid, 256, 0, st>>>(u, v, uv, n);
 }
 
-// Block-level bounding box of valid positions, merged into the ensemble's box.
+// Block-level bounding box of valid positions, merged into the ensemble's box (blocks of B threads).
+template <int B = SLOT_BLOCK>
 __device__ __forceinline__ void block_bbox(bool valid, float x, float y, uint32_t* ebox_e) {
-  __shared__ float red[4][SLOT_BLOCK / 32];
+  __shared__ float red[4][B / 32];
   float mnx = valid ? x : INFINITY, mny = valid ? y : INFINITY;
   float mxx = valid ? x : -INFINITY, mxy = valid ? y : -INFINITY;
   for (int o = 16; o > 0; o >>= 1) {
@@ -52,7 +53,7 @@ __device__ __forceinline__ void block_bbox(bool valid, float x, float y, uint32_
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    for (int k = 1; k < (int)(SLOT_BLOCK / 32); ++k) {
+    for (int k = 1; k < B / 32; ++k) {
       mnx = fminf(mnx, red[0][k]);
       mny = fminf(mny, red[1][k]);
       mxx = fmaxf(mxx, red[2][k]);
@@ -67,7 +68,10 @@ __device__ __forceinline__ void block_bbox(bool valid, float x, float y, uint32_
   }
 }
 
-__global__ void __launch_bounds__(SLOT_BLOCK) k_advect(FieldView f, StepArgs a, Bufs b, Ctrl* ctrl) {
+// Blocks of B = 128 or 256 threads (a tuning knob, lm_set_tuning): B divides the 256-slot blocks of
+// the slot layout, so every block still lies inside one ensemble.
+template <int B>
+__global__ void __launch_bounds__(B) k_advect(FieldView f, StepArgs a, Bufs b, Ctrl* ctrl) {
   pdl_wait();
   __shared__ Stage sh[3];
   __shared__ uint32_t sh_step;
@@ -82,12 +86,12 @@ __global__ void __launch_bounds__(SLOT_BLOCK) k_advect(FieldView f, StepArgs a, 
     }
     sh_step = a.use_ctrl_step ? ctrl->step : a.step0;
     sh_skip = ctrl->halt != 0 || !ctrl->stage_ok;
-    sh_e = b.block_ens[blockIdx.x];
+    sh_e = b.block_ens[(blockIdx.x * (uint32_t)B) / SLOT_BLOCK];
     sh_ens = b.ens[sh_e];
   }
   __syncthreads();
   if (sh_skip) return;
-  const uint32_t p = blockIdx.x * SLOT_BLOCK + threadIdx.x;
+  const uint32_t p = blockIdx.x * (uint32_t)B + threadIdx.x;
   const float2* uv = f.uv + sh_ens.field_off;
 
   uint32_t st = (p < b.nslots) ? b.status[p] : STATUS_PAD;
@@ -131,12 +135,15 @@ __global__ void __launch_bounds__(SLOT_BLOCK) k_advect(FieldView f, StepArgs a, 
     b.xo[p] = x;
     b.yo[p] = y;
   }
-  block_bbox(st == STATUS_OK, ax, ay, b.ebox + 4 * sh_e);
+  block_bbox<B>(st == STATUS_OK, ax, ay, b.ebox + 4 * sh_e);
 }
 
-void launch_advect(const FieldView& f, const StepArgs& a, const Bufs& b, Ctrl* ctrl, cudaStream_t st) {
+void launch_advect(const FieldView& f, const StepArgs& a, const Bufs& b, Ctrl* ctrl, int threads, cudaStream_t st) {
   if (b.nslots == 0) return;
-  launch_dep(k_advect, dim3((b.nslots + SLOT_BLOCK - 1) / SLOT_BLOCK), dim3(SLOT_BLOCK), st, f, a, b, ctrl);
+  if (threads == 128)
+    launch_dep(k_advect<128>, dim3((b.nslots + 127) / 128), dim3(128), st, f, a, b, ctrl);
+  else
+    launch_dep(k_advect<SLOT_BLOCK>, dim3((b.nslots + SLOT_BLOCK - 1) / SLOT_BLOCK), dim3(SLOT_BLOCK), st, f, a, b, ctrl);
 }
 
 // Bounding boxes from the recorded positions (two-phase interaction path and step re-runs).

@@ -682,20 +682,33 @@ __global__ void __launch_bounds__(LONG_WARPS * 32) k_sweep_long(Bufs b, PairPara
           const uint32_t mask = __ballot_sync(0xffffffffu, ok);
           if (ok) {
             const uint32_t pos = m + __popc(mask & lanemask_lt_p());
-            if (pos < d) {
-              const uint32_t lb = id[h] - base;
-              const unsigned long long p = pair_prio(min(la, lb), max(la, lb), step, k0, k1);
-              const uint32_t e = t[h] > s ? t[h] | win_bits(info, la, lb, step) : t[h];
+            if (pos < d) {  // the partner and its local id; priority and draw follow below
               if (in_smem) {
-                sh.p[pos] = p;
-                sh.t[pos] = e;
+                sh.p[pos] = id[h] - base;
+                sh.t[pos] = t[h];
               } else {
-                b.ovf[o + pos] = e;
-                b.oprio[o + pos] = p;
+                b.ovf[o + pos] = t[h];
+                b.oprio[o + pos] = id[h] - base;
               }
             }
           }
           m += __popc(mask);
+        }
+      }
+      // priorities and outcome draws of the d entries, one entry per lane (in the gather only the
+      // lanes that found a neighbour would work, about a third of them)
+      __syncwarp();
+      for (uint32_t i = lane; i < d; i += 32) {
+        const uint32_t tt = in_smem ? sh.t[i] : b.ovf[o + i];
+        const uint32_t lb = (uint32_t)(in_smem ? sh.p[i] : b.oprio[o + i]);
+        const unsigned long long p = pair_prio(min(la, lb), max(la, lb), step, k0, k1);
+        const uint32_t e = tt > s ? tt | win_bits(info, la, lb, step) : tt;
+        if (in_smem) {
+          sh.p[i] = p;
+          sh.t[i] = e;
+        } else {
+          b.ovf[o + i] = e;
+          b.oprio[o + i] = p;
         }
       }
       uint32_t first;
@@ -752,8 +765,9 @@ __global__ void __launch_bounds__(LONG_WARPS * 32) k_sweep_long(Bufs b, PairPara
 }
 
 void launch_sweep_long(const Bufs& b, const PairParams& pp, const StepArgs& a, Ctrl* ctrl, int sms,
-                       cudaStream_t st) {
-  launch_dep(k_sweep_long, dim3(sms * 6), dim3(LONG_WARPS * 32), st, b, pp, a, ctrl);  // 6 x 36 KB per SM
+                       int blocks_per_sm, cudaStream_t st) {
+  // at most 6 blocks of 36 KB fit an SM's shared memory; more queue behind them
+  launch_dep(k_sweep_long, dim3(sms * blocks_per_sm), dim3(LONG_WARPS * 32), st, b, pp, a, ctrl);
 }
 
 }  // namespace lm

@@ -38,14 +38,15 @@
 
 namespace lm {
 
-// 1,024 threads owning two vertices each: two blocks per SM hold 2 x 2,048 vertices in 2 x 96 KB of
-// shared memory and keep 2,048 threads resident (32 registers each). The kernel is latency bound
-// (dependent shared-memory loads, polls of words written by other threads), so the doubled number
-// of resident warps against blocks of 512 threads owning four vertices each shortens it: 74 -> 66 us
-// per launch on the first day of the 490k run, 107 -> 90 us on its last day. Against blocks of 256
-// (the same vertices per SM) a block's range has a shorter edge for its area, so fewer pairs hand
-// off through global memory.
-constexpr int RD_THREADS = 1024;
+// Blocks of 1,024 threads owning two vertices each (the default) or of 512 owning four: two blocks per
+// SM hold 2 x 2,048 vertices in 2 x 96 KB of shared memory. With 1,024 threads the SM keeps 2,048
+// threads resident (32 registers each); the kernel is latency bound (dependent shared-memory loads,
+// polls of words written by other threads), and the doubled number of resident warps shortened it
+// from 74 to 66 us per launch on the first day of the 490k run and from 107 to 90 us on its last
+// day. The block size is a tuning knob (lm_set_tuning); against blocks of 256 (the same vertices
+// per SM) a block's range has a shorter edge for its area, so fewer pairs hand off through global
+// memory.
+constexpr int RD_THREADS_DEFAULT = 1024;
 constexpr unsigned long long ROUNDS_TIMEOUT_NS = 2000000000ull;  // 2 s
 
 __device__ __forceinline__ unsigned long long globaltimer() {
@@ -130,7 +131,7 @@ constexpr int POLL_BATCH = 2;  // vertices whose state words one thread loads be
 // ---- tile-local interaction: block-owned vertex ranges with handshakes in shared memory ----
 //
 // Cell keys are tile-major, so a contiguous range of cell-ordered vertices is a compact 2D patch.
-// Block b owns the vertices [b V, b V + V) (V = RD_THREADS x up to TL_VPT) and keeps their state words,
+// Block b owns the vertices [b V, b V + V) (V <= TL_VMAX, whole columns of the block's threads) and keeps their state words,
 // slot ids, degrees and list entries in shared memory. A pair whose two microbes the block owns
 // hands off through shared memory (tens of cycles instead of an L2 round trip); a pair that
 // crosses blocks goes through the global state words: the vertex's word is published there while
@@ -139,8 +140,7 @@ constexpr int POLL_BATCH = 2;  // vertices whose state words one thread loads be
 // shared memory. As in the global path, only the applier of a vertex's current pair writes the
 // vertex's word, so no fences are needed.
 static_assert(SLAB == 8, "the tile path copies a slab row as two 16-byte loads");
-constexpr int TL_VPT = 2;                              // vertices per thread at most
-constexpr uint32_t TL_VMAX = RD_THREADS * TL_VPT;      // vertices per block at most
+constexpr uint32_t TL_VMAX = 2048;                     // vertices per block at most
 constexpr size_t TL_SMEM = TL_VMAX * (8 + 4 + 4 + 4 * SLAB);  // words, slot ids, degrees, lists
 
 __device__ __forceinline__ unsigned long long ld_sh(const unsigned long long* p) {
@@ -166,8 +166,10 @@ __device__ __forceinline__ uint32_t tl_entry(const Bufs& b, const TileSmem& t, u
 
 // The pairs among cell-order vertices [g_lo, g_hi) (a group of whole ensembles, so no pair leaves
 // it), at most TL_VMAX per block: each block owns an equal share of whole RD_THREADS-vertex columns.
+template <int RD_THREADS>
 __device__ void tl_group(const Bufs& b, uint32_t step, Ctrl* ctrl, unsigned long long t0, uint32_t g_lo,
                          uint32_t g_hi) {
+  constexpr int TL_VPT = (int)TL_VMAX / RD_THREADS;  // vertices per thread at most
   extern __shared__ unsigned long long tl_raw[];
   TileSmem t;
   t.w = tl_raw;
@@ -278,6 +280,7 @@ __device__ void tl_group(const Bufs& b, uint32_t step, Ctrl* ctrl, unsigned long
 constexpr int TL_GROUPS_MAX = 64;
 
 // Returns false (nothing done) when the step does not fit the tile path (grid-uniform).
+template <int RD_THREADS>
 __device__ bool rounds_tiled(const Bufs& b, uint32_t step, Ctrl* ctrl, unsigned long long t0) {
   const uint32_t n_valid = ((volatile uint32_t*)&ctrl->n_valid)[0];
   if (b.plog) return false;
@@ -326,12 +329,13 @@ __device__ bool rounds_tiled(const Bufs& b, uint32_t step, Ctrl* ctrl, unsigned 
   const int groups = ng;
   if (groups <= 0) return false;
   for (int g = 0; g < groups; ++g) {
-    tl_group(b, step, ctrl, t0, gb[g], gb[g + 1]);
+    tl_group<RD_THREADS>(b, step, ctrl, t0, gb[g], gb[g + 1]);
     __syncthreads();  // the block's shared lists are reused by the next group
   }
   return true;
 }
 
+template <int RD_THREADS>
 __global__ void __launch_bounds__(RD_THREADS, 2) k_rounds(Bufs b, StepArgs a, Ctrl* ctrl) {
   pdl_wait();
   if (((volatile uint32_t*)&ctrl->halt)[0]) return;
@@ -355,7 +359,7 @@ __global__ void __launch_bounds__(RD_THREADS, 2) k_rounds(Bufs b, StepArgs a, Ct
   const uint32_t first = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t max_level = 0;
   const unsigned long long t0 = globaltimer();
-  if (rounds_tiled(b, step, ctrl, t0)) return;  // levels are tracked only in pair-log runs
+  if (rounds_tiled<RD_THREADS>(b, step, ctrl, t0)) return;  // levels are tracked only in pair-log runs
   uint32_t polls = 0;
   if (cnt <= (uint32_t)POLL_BATCH * stride) {
     // every thread owns at most POLL_BATCH vertices: keep their ids in registers and stop polling
@@ -432,14 +436,24 @@ __global__ void __launch_bounds__(RD_THREADS, 2) k_rounds(Bufs b, StepArgs a, Ct
   }
 }
 
-int rounds_grid(int device, int* block) {
-  int sms = 0, per_sm = 0;
+// Blocks per SM of the interaction kernel with `threads` per block (512 or 1,024).
+template <int T>
+static int rounds_per_sm(int device) {
+  int per_sm = 0;
+  cudaFuncSetAttribute(k_rounds<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TL_SMEM);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rounds<T>, T, TL_SMEM);
+  (void)device;
+  return per_sm;
+}
+
+int rounds_grid(int device, int threads, int* block) {
+  int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-  cudaFuncSetAttribute(k_rounds, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TL_SMEM);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rounds, RD_THREADS, TL_SMEM);
+  if (threads != 512) threads = RD_THREADS_DEFAULT;
+  int per_sm = threads == 512 ? rounds_per_sm<512>(device) : rounds_per_sm<1024>(device);
   if (per_sm < 1) per_sm = 1;
   if (per_sm > 4) per_sm = 4;
-  *block = RD_THREADS;
+  *block = threads;
   return sms * per_sm;
 }
 
@@ -454,7 +468,8 @@ cudaError_t launch_rounds(const Bufs& b, const StepArgs& a, Ctrl* ctrl, int grid
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, k_rounds, b, a, ctrl);
+  if (block == 512) return cudaLaunchKernelEx(&cfg, k_rounds<512>, b, a, ctrl);
+  return cudaLaunchKernelEx(&cfg, k_rounds<1024>, b, a, ctrl);
 }
 
 // Species counts after the step, per ensemble and in total ([0] collects values outside 1..3).

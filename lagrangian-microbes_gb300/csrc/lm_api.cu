@@ -122,6 +122,10 @@ struct lm_ctx {
   int8_t* rec_sp = nullptr;
 
   int rgrid = 0, rblock = 0;
+  // tuning knobs (lm_set_tuning): block sizes and grid shapes that change speed, never results
+  int tune_rounds_threads = 1024;  // interaction blocks: 1,024 threads x 2 vertices or 512 x 4
+  int tune_long_per_sm = 6;        // long-list blocks per SM
+  int tune_advect_threads = 256;   // advection threads per block (128 or 256)
 
   // graph
   cudaGraph_t graph = nullptr;
@@ -498,7 +502,7 @@ cudaError_t enqueue_interaction(lm_ctx* c, const StepArgs& a, uint32_t flags, bo
     return cudaGetLastError();
   }
   PROF(c, P_SWEEP, launch_sweep(b, c->pp, a, c->ctrl, st));
-  PROF(c, P_SWEEP_LONG, launch_sweep_long(b, c->pp, a, c->ctrl, c->sms, st));
+  PROF(c, P_SWEEP_LONG, launch_sweep_long(b, c->pp, a, c->ctrl, c->sms, c->tune_long_per_sm, st));
   if (flags & LM_STEP_INTERACT) {
     cudaEvent_t pa = prof_begin(c);
     cudaError_t e = launch_rounds(b, a, c->ctrl, c->rgrid, c->rblock, st);
@@ -515,7 +519,7 @@ cudaError_t enqueue_step(lm_ctx* c, const StepArgs& a, uint32_t flags, bool adve
                          const StepArgs* next = nullptr) {
   const Bufs b = bufs(c, false);
   if (!begun) PROF(c, P_BOOKKEEPING, launch_step_begin(b, advect ? &c->fv : nullptr, a, c->ctrl, c->st));
-  if (advect) PROF(c, P_ADVECT, launch_advect(c->fv, a, b, c->ctrl, c->st));
+  if (advect) PROF(c, P_ADVECT, launch_advect(c->fv, a, b, c->ctrl, c->tune_advect_threads, c->st));
   if (flags & (LM_STEP_INTERACT | LM_STEP_COUNT_PAIRS)) {
     cudaError_t e = enqueue_interaction(c, a, flags, !advect, true);
     if (e != cudaSuccess) return e;
@@ -787,7 +791,7 @@ int lm_ctx_create(int device, lm_ctx** out) {
   if ((e = cudaMemsetAsync(c->ctrl, 0, sizeof(Ctrl), c->st)) != cudaSuccess ||
       (e = cudaStreamSynchronize(c->st)) != cudaSuccess)
     return bail(fail(c, LM_ERR_CUDA, "ctrl init: %s", cudaGetErrorString(e)));
-  c->rgrid = rounds_grid(device, &c->rblock);
+  c->rgrid = rounds_grid(device, c->tune_rounds_threads, &c->rblock);
   set_pair_params(c, 0.0, LM_NORM_L2);
   *out = c;
   return LM_OK;
@@ -1116,6 +1120,41 @@ int lm_set_ensemble_params(lm_ctx* c, int n_ens, const double* p_rs, const doubl
   c->p_sp.assign(p_sp, p_sp + n_ens);
   c->seeds.assign(seeds, seeds + n_ens);
   return upload_ens(c);
+}
+
+int lm_set_tuning(lm_ctx* c, int knob, int value) {
+  if (!c) return LM_ERR_ARG;
+  switch (knob) {
+    case LM_TUNE_ROUNDS_THREADS:
+      if (value != 512 && value != 1024) return fail(c, LM_ERR_ARG, "interaction block size must be 512 or 1024");
+      c->tune_rounds_threads = value;
+      CK(cudaSetDevice(c->device));
+      c->rgrid = rounds_grid(c->device, value, &c->rblock);
+      break;
+    case LM_TUNE_LONG_BLOCKS_PER_SM:
+      if (value < 1 || value > 32) return fail(c, LM_ERR_ARG, "long-list blocks per SM must be in [1, 32]");
+      c->tune_long_per_sm = value;
+      break;
+    case LM_TUNE_ADVECT_THREADS:
+      if (value != 128 && value != 256) return fail(c, LM_ERR_ARG, "advection block size must be 128 or 256");
+      c->tune_advect_threads = value;
+      break;
+    default:
+      return fail(c, LM_ERR_ARG, "unknown tuning knob %d", knob);
+  }
+  drop_graph(c);  // a captured graph keeps the launch shapes it was captured with
+  return LM_OK;
+}
+
+int lm_get_tuning(lm_ctx* c, int knob, int* value) {
+  if (!c || !value) return LM_ERR_ARG;
+  switch (knob) {
+    case LM_TUNE_ROUNDS_THREADS: *value = c->tune_rounds_threads; break;
+    case LM_TUNE_LONG_BLOCKS_PER_SM: *value = c->tune_long_per_sm; break;
+    case LM_TUNE_ADVECT_THREADS: *value = c->tune_advect_threads; break;
+    default: return fail(c, LM_ERR_ARG, "unknown tuning knob %d", knob);
+  }
+  return LM_OK;
 }
 
 int lm_set_cell_factor(lm_ctx* c, double factor) {

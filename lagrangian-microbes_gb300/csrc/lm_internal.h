@@ -280,7 +280,8 @@ void launch_step_end(Ctrl* ctrl, bool interact, cudaStream_t st);
 // End of a step and start of the next (arguments `an`) in one launch (steps of one call).
 void launch_step_turn(const Bufs& b, const FieldView* f, const StepArgs& an, Ctrl* ctrl, bool interact,
                       cudaStream_t st);
-void launch_advect(const FieldView& f, const StepArgs& a, const Bufs& b, Ctrl* ctrl, cudaStream_t st);
+// threads: 128 or 256 per block (tuning)
+void launch_advect(const FieldView& f, const StepArgs& a, const Bufs& b, Ctrl* ctrl, int threads, cudaStream_t st);
 void launch_bbox(const Bufs& b, Ctrl* ctrl, bool use_status, cudaStream_t st);
 
 // K2 binning: per-ensemble grids, counting pass, cell scan, scatter into cell order.
@@ -294,11 +295,13 @@ void launch_scatter(const Bufs& b, Ctrl* ctrl, cudaStream_t st);
 // K3 neighbour lists.
 void launch_sweep(const Bufs& b, const PairParams& pp, const StepArgs& a, Ctrl* ctrl, cudaStream_t st);
 void launch_count_pairs(const Bufs& b, const PairParams& pp, Ctrl* ctrl, cudaStream_t st);
+// blocks_per_sm: grid of sms x blocks_per_sm blocks of LONG_WARPS warps (tuning)
 void launch_sweep_long(const Bufs& b, const PairParams& pp, const StepArgs& a, Ctrl* ctrl, int sms,
-                       cudaStream_t st);
+                       int blocks_per_sm, cudaStream_t st);
 
 // K4/K5 interaction dataflow (cooperative persistent kernel).
-int rounds_grid(int device, int* block);
+// Grid of the cooperative launch with `threads` (512 or 1,024) per block; *block receives the block size.
+int rounds_grid(int device, int threads, int* block);
 cudaError_t launch_rounds(const Bufs& b, const StepArgs& a, Ctrl* ctrl, int grid, int block, cudaStream_t st);
 void launch_census(const Bufs& b, Ctrl* ctrl, cudaStream_t st);
 const void* lm_census_kernel();  // one kernel of the library, for attribute queries

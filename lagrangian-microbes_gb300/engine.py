@@ -138,6 +138,54 @@ class Simulation:
         self._graph = None
         return best, times
 
+    TUNING_KNOBS = {"rounds_threads": (_lib.TUNE_ROUNDS_THREADS, (1024, 512)),
+                    "long_blocks_per_sm": (_lib.TUNE_LONG_BLOCKS_PER_SM, (6, 3, 12)),
+                    "advect_threads": (_lib.TUNE_ADVECT_THREADS, (256, 128))}
+
+    def set_tuning(self, knob: str, value: int) -> None:
+        """Set a launch-shape knob (TUNING_KNOBS); results never depend on it, only the speed."""
+        self.ctx.call("lm_set_tuning", self.TUNING_KNOBS[knob][0], int(value))
+        self._graph = None
+
+    def tuning(self) -> dict:
+        out = {}
+        for name, (code, _) in self.TUNING_KNOBS.items():
+            v = ctypes.c_int(0)
+            self.ctx.call("lm_get_tuning", code, ctypes.byref(v))
+            out[name] = v.value
+        return out
+
+    def autotune_all(self, t0, dt, n_steps: int = 3, factors=(1.004, 1.25, 1.5, 2.0), count_pairs: bool = False):
+        """The binning cell size (autotune), then each launch-shape knob in turn (block size of the
+        interaction and advection kernels, long-list blocks per SM), each value timed over n_steps
+        from the current state; the state is returned to where it started. Returns the chosen
+        settings with the seconds of every candidate."""
+        import time as _time
+        best_f, ftimes = self.autotune(t0, dt, n_steps, factors, count_pairs)
+        s0 = self.step_index
+        self.snapshot()
+        chosen = {"cell_factor": best_f}
+        seconds = {"cell_factor": {str(k): v for k, v in ftimes.items()}}
+        for name, (_, values) in self.TUNING_KNOBS.items():
+            times = {}
+            for v in values:
+                self.set_tuning(name, v)
+                self.restore()
+                self.step(t0, dt, 1, step0=s0, count_pairs=count_pairs)  # sizes buffers for this shape
+                self.restore()
+                t = _time.perf_counter()
+                self.step(t0, dt, n_steps, step0=s0, count_pairs=count_pairs)
+                self.sync()
+                times[v] = _time.perf_counter() - t
+            best = min(times, key=times.get)
+            self.set_tuning(name, best)
+            chosen[name] = best
+            seconds[name] = {str(k): v for k, v in times.items()}
+        self.restore()
+        self._graph = None
+        chosen["seconds"] = seconds
+        return chosen
+
     def set_stream(self, stream_handle: int) -> None:
         """Run on an external CUDA stream (e.g. torch.cuda.current_stream().cuda_stream)."""
         self.ctx.call("lm_ctx_set_stream", int(stream_handle))

@@ -104,3 +104,30 @@ def test_field_window_upload_keeps_the_state_and_drops_the_graph(lm, orc):
         np.testing.assert_array_equal(a, b)
     whole.close()
     win.close()
+
+
+def test_launch_shape_knobs_change_speed_only(lm, orc, small_field):
+    """Every value of every tuning knob gives the same trajectory and species, bit for bit; the
+    full autotuner returns to the state it started from."""
+    t0 = float(small_field.times[0])
+    ref, _ = _sim(lm, orc, small_field)
+    ref.step(t0, 3600.0, 5, step0=0)
+    want = ref.state()
+    ref.close()
+    for name, (_, values) in lm.Simulation.TUNING_KNOBS.items():
+        for v in values:
+            sim, _ = _sim(lm, orc, small_field)
+            sim.set_tuning(name, v)
+            assert sim.tuning()[name] == v
+            sim.step(t0, 3600.0, 5, step0=0)
+            for x, y in zip(want, sim.state()):
+                np.testing.assert_array_equal(x, y, err_msg=f"{name}={v}")
+            sim.close()
+    sim, _ = _sim(lm, orc, small_field)
+    chosen = sim.autotune_all(t0, 3600.0, n_steps=1, factors=(1.004, 2.0))
+    assert set(chosen) >= {"cell_factor", *lm.Simulation.TUNING_KNOBS}
+    assert sim.step_index == 0
+    sim.step(t0, 3600.0, 5, step0=0)
+    for x, y in zip(want, sim.state()):
+        np.testing.assert_array_equal(x, y)
+    sim.close()
