@@ -39,6 +39,7 @@ struct lm_ctx {
   // field
   float2* uv = nullptr;
   size_t uv_n = 0;
+  float* stage_uv = nullptr;  // field upload staging: u and v chunks before interleaving
   size_t field_elems = 0;  // nt * ny * nx
   int n_fields = 0;
   FieldView fv{};
@@ -818,6 +819,7 @@ int lm_ctx_destroy(lm_ctx* c) {
     cudaStreamDestroy(c->rec_st);
   }
   if (c->rec_ring) cudaFree(c->rec_ring);
+  if (c->stage_uv) cudaFree(c->stage_uv);
   for (int q = 0; q < lm_ctx::REC_SLOTS; ++q) {
     if (c->rec_done[q]) cudaEventDestroy(c->rec_done[q]);
     if (c->rec_copied[q]) cudaEventDestroy(c->rec_copied[q]);
@@ -872,19 +874,25 @@ int lm_field_upload_batch(lm_ctx* c, int n_fields, const float* u, const float* 
     if ((r = dalloc(c, &c->uv, n))) return r;
     c->uv_n = n;
   }
-  // stage u and v through a bounded temporary device buffer, one chunk of frames at a time
-  const size_t chunk = std::min<size_t>(n, (size_t)64 << 20);
-  float* tmp = nullptr;
-  if ((r = dalloc(c, &tmp, 2 * chunk))) return r;
+  // stage u and v through the context's staging buffer (allocated once, 2 x 16M floats), one chunk
+  // of values at a time: no field-sized temporary is allocated and freed per upload
+  const size_t chunk = (size_t)16 << 20;
+  if (!c->stage_uv) {
+    const cudaError_t e = cudaMalloc(&c->stage_uv, 2 * chunk * sizeof(float));
+    if (e != cudaSuccess) {
+      c->stage_uv = nullptr;
+      cudaGetLastError();
+      return fail(c, LM_ERR_OOM, "cudaMalloc of the field staging buffer failed: %s", cudaGetErrorString(e));
+    }
+  }
   for (size_t o = 0; o < n; o += chunk) {
     const size_t m = std::min(chunk, n - o);
-    CK(cudaMemcpyAsync(tmp, u + o, m * sizeof(float), cudaMemcpyDefault, c->st));
-    CK(cudaMemcpyAsync(tmp + chunk, v + o, m * sizeof(float), cudaMemcpyDefault, c->st));
-    launch_interleave(tmp, tmp + chunk, c->uv + o, m, c->st);
+    CK(cudaMemcpyAsync(c->stage_uv, u + o, m * sizeof(float), cudaMemcpyDefault, c->st));
+    CK(cudaMemcpyAsync(c->stage_uv + chunk, v + o, m * sizeof(float), cudaMemcpyDefault, c->st));
+    launch_interleave(c->stage_uv, c->stage_uv + chunk, c->uv + o, m, c->st);
   }
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(c->st));
-  cudaFree(tmp);
   c->n_fields = n_fields;
   c->field_elems = per;
   c->lon0 = lon[0];

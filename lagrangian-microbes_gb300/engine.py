@@ -115,24 +115,46 @@ class Simulation:
                       _lib.ptr(arr("species", np.int8)), _lib.ptr(arr("status", np.uint8)), int(state["step"]))
         self.step_index = int(state["step"])
 
-    def autotune(self, t0, dt, n_steps: int = 3, factors=(1.004, 1.25, 1.5, 2.0), count_pairs: bool = False):
-        """Pick the binning cell size (in units of the radius) that runs n_steps fastest from the
-        current state, then return to that state. The pair sets, and so all results, are the same
-        for every cell size; only the speed changes. Capture graphs after tuning. Returns
-        (best factor, {factor: seconds})."""
+    def _time_from_snapshot(self, t0, dt, n_steps, s0, count_pairs, reps):
+        """Seconds of n_steps from the snapshot (best of reps, device work included), after one
+        untimed step that sizes the buffers for the current settings."""
         import time as _time
+        self.restore()
+        self.step(t0, dt, 1, step0=s0, count_pairs=count_pairs)
+        self.sync()
+        best = float("inf")
+        for _ in range(reps):
+            self.restore()
+            t = _time.perf_counter()
+            self.step(t0, dt, n_steps, step0=s0, count_pairs=count_pairs)
+            self.sync()
+            best = min(best, _time.perf_counter() - t)
+        return best
+
+    @staticmethod
+    def _pick(times: dict, margin: float):
+        """The first candidate (the incumbent) unless another is faster by more than margin."""
+        keys = list(times)
+        best = keys[0]
+        for k in keys[1:]:
+            if times[k] < times[best] * (1.0 - margin):
+                best = k
+        return best
+
+    def autotune(self, t0, dt, n_steps: int = 3, factors=(1.004, 1.25, 1.5, 2.0), count_pairs: bool = False,
+                 reps: int = 2, margin: float = 0.03):
+        """Pick the binning cell size (in units of the radius) that runs n_steps fastest from the
+        current state, then return to that state. The first factor is kept unless another is faster
+        by more than `margin` (timings of a few steps differ by a few per cent from run to run). The
+        pair sets, and so all results, are the same for every cell size; only the speed changes.
+        Capture graphs after tuning. Returns (best factor, {factor: seconds})."""
         s0 = self.step_index
         self.snapshot()
         times = {}
         for f in factors:
             self.set_cell_factor(f)
-            self.restore()
-            self.step(t0, dt, 1, step0=s0, count_pairs=count_pairs)  # sizes the lists for this cell size
-            self.restore()
-            t = _time.perf_counter()
-            self.step(t0, dt, n_steps, step0=s0, count_pairs=count_pairs)
-            times[f] = _time.perf_counter() - t
-        best = min(times, key=times.get)
+            times[f] = self._time_from_snapshot(t0, dt, n_steps, s0, count_pairs, reps)
+        best = self._pick(times, margin)
         self.set_cell_factor(best)
         self.restore()
         self._graph = None
@@ -155,13 +177,15 @@ class Simulation:
             out[name] = v.value
         return out
 
-    def autotune_all(self, t0, dt, n_steps: int = 3, factors=(1.004, 1.25, 1.5, 2.0), count_pairs: bool = False):
+    def autotune_all(self, t0, dt, n_steps: int = 3, factors=(1.004, 1.25, 1.5, 2.0), count_pairs: bool = False,
+                     reps: int = 2, margin: float = 0.03):
         """The binning cell size (autotune), then each launch-shape knob in turn (block size of the
         interaction and advection kernels, long-list blocks per SM), each value timed over n_steps
-        from the current state; the state is returned to where it started. Returns the chosen
-        settings with the seconds of every candidate."""
-        import time as _time
-        best_f, ftimes = self.autotune(t0, dt, n_steps, factors, count_pairs)
+        from the current state (best of reps); a knob keeps its first value unless another is faster
+        by more than `margin`. The state is returned to where it started. Returns the chosen settings
+        with the seconds of every candidate. Tune from a state like the one the run spends its time
+        in: the long-list and interaction knobs matter once the flow has clustered the microbes."""
+        best_f, ftimes = self.autotune(t0, dt, n_steps, factors, count_pairs, reps, margin)
         s0 = self.step_index
         self.snapshot()
         chosen = {"cell_factor": best_f}
@@ -170,14 +194,8 @@ class Simulation:
             times = {}
             for v in values:
                 self.set_tuning(name, v)
-                self.restore()
-                self.step(t0, dt, 1, step0=s0, count_pairs=count_pairs)  # sizes buffers for this shape
-                self.restore()
-                t = _time.perf_counter()
-                self.step(t0, dt, n_steps, step0=s0, count_pairs=count_pairs)
-                self.sync()
-                times[v] = _time.perf_counter() - t
-            best = min(times, key=times.get)
+                times[v] = self._time_from_snapshot(t0, dt, n_steps, s0, count_pairs, reps)
+            best = self._pick(times, margin)
             self.set_tuning(name, best)
             chosen[name] = best
             seconds[name] = {str(k): v for k, v in times.items()}
