@@ -281,8 +281,7 @@ constexpr int TL_GROUPS_MAX = 64;
 
 // Returns false (nothing done) when the step does not fit the tile path (grid-uniform).
 template <int RD_THREADS>
-__device__ bool rounds_tiled(const Bufs& b, uint32_t step, Ctrl* ctrl, unsigned long long t0) {
-  const uint32_t n_valid = ((volatile uint32_t*)&ctrl->n_valid)[0];
+__device__ bool rounds_tiled(const Bufs& b, uint32_t step, Ctrl* ctrl, unsigned long long t0, uint32_t n_valid) {
   if (b.plog) return false;
   const uint32_t cap = gridDim.x * TL_VMAX;
   __shared__ uint32_t gb[TL_GROUPS_MAX + 1];
@@ -338,7 +337,18 @@ __device__ bool rounds_tiled(const Bufs& b, uint32_t step, Ctrl* ctrl, unsigned 
 template <int RD_THREADS>
 __global__ void __launch_bounds__(RD_THREADS, 2) k_rounds(Bufs b, StepArgs a, Ctrl* ctrl) {
   pdl_wait();
-  if (((volatile uint32_t*)&ctrl->halt)[0]) return;
+  // the control words, read by one thread per block: every thread of the 300-odd blocks loading
+  // the same L2 line (the loads are volatile, so L1 does not merge them) queued ~10^4 requests on
+  // one L2 slice and delayed the start of the pairs by 4-10 us
+  __shared__ uint32_t cw[4];
+  if (threadIdx.x == 0) {
+    cw[0] = ((volatile uint32_t*)&ctrl->halt)[0];
+    cw[1] = ((volatile uint32_t*)&ctrl->act_n)[0];
+    cw[2] = ((volatile uint32_t*)&ctrl->n_valid)[0];
+    cw[3] = a.use_ctrl_step ? ((volatile uint32_t*)&ctrl->step)[0] : a.step0;
+  }
+  __syncthreads();
+  if (cw[0]) return;
   if (a.test_wait_ns) {
     // injected failure (tests): the wait of a stalled dependency, on a flag that nothing sets,
     // bounded like every wait of this kernel; the step applies no pair and reports the timeout
@@ -353,13 +363,13 @@ __global__ void __launch_bounds__(RD_THREADS, 2) k_rounds(Bufs b, StepArgs a, Ct
     }
     return;
   }
-  const uint32_t step = a.use_ctrl_step ? ctrl->step : a.step0;
-  const uint32_t cnt = ((volatile uint32_t*)&ctrl->act_n)[0];
+  const uint32_t step = cw[3];
+  const uint32_t cnt = cw[1];
   const uint32_t stride = gridDim.x * blockDim.x;
   const uint32_t first = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t max_level = 0;
   const unsigned long long t0 = globaltimer();
-  if (rounds_tiled<RD_THREADS>(b, step, ctrl, t0)) return;  // levels are tracked only in pair-log runs
+  if (rounds_tiled<RD_THREADS>(b, step, ctrl, t0, cw[2])) return;  // levels are tracked only in pair-log runs
   uint32_t polls = 0;
   if (cnt <= (uint32_t)POLL_BATCH * stride) {
     // every thread owns at most POLL_BATCH vertices: keep their ids in registers and stop polling
