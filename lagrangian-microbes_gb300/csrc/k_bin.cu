@@ -311,11 +311,33 @@ void launch_keys(const Bufs& b, const PairParams& pp, Ctrl* ctrl, bool use_statu
 
 // Exclusive scan of the cell counts in two launches over SCAN_BLOCKS fixed chunks:
 // (1) chunk sums, (2) per-chunk scan with the prefix of the chunk sums. The counts are zeroed
-// as they are consumed, ready for the next counting pass.
+// as they are consumed, ready for the next counting pass. Each thread takes 4 consecutive cells
+// (one 16-byte word: chunks are whole multiples of 4 cells, and the count and start arrays are
+// separate 256-byte aligned allocations), so a pass of a 1,024-thread block covers 4,096 cells and
+// the scan of a sparse multi-ensemble grid (tens of millions of cells) is bound by bandwidth
+// rather than by the block's barriers.
+constexpr uint32_t SCAN_CPT = 4;
+
 __device__ __forceinline__ void chunk_of(uint32_t ncells, uint32_t* c0, uint32_t* c1) {
-  const uint32_t per = (ncells + SCAN_BLOCKS - 1) / SCAN_BLOCKS;
+  const uint32_t per = ((ncells + SCAN_BLOCKS - 1) / SCAN_BLOCKS + (SCAN_CPT - 1)) & ~(SCAN_CPT - 1);
   *c0 = min(ncells, blockIdx.x * per);
   *c1 = min(ncells, *c0 + per);
+}
+
+// Cells i .. i + 3 of [.., c1) (zero past c1); i is a multiple of 4.
+__device__ __forceinline__ uint4 load_cells(const uint32_t* a, uint32_t i, uint32_t c1) {
+  if (i + SCAN_CPT <= c1) return *reinterpret_cast<const uint4*>(a + i);
+  return make_uint4(i < c1 ? a[i] : 0u, i + 1 < c1 ? a[i + 1] : 0u, i + 2 < c1 ? a[i + 2] : 0u, 0u);
+}
+
+__device__ __forceinline__ void store_cells(uint32_t* a, uint32_t i, uint32_t c1, uint4 v) {
+  if (i + SCAN_CPT <= c1) {
+    *reinterpret_cast<uint4*>(a + i) = v;
+    return;
+  }
+  if (i < c1) a[i] = v.x;
+  if (i + 1 < c1) a[i + 1] = v.y;
+  if (i + 2 < c1) a[i + 2] = v.z;
 }
 
 __device__ __forceinline__ uint32_t block_sum(uint32_t v) {
@@ -335,7 +357,10 @@ __global__ void __launch_bounds__(1024) k_cscan_reduce(Bufs b, Ctrl* ctrl) {
   uint32_t c0, c1;
   chunk_of(ctrl->ncells, &c0, &c1);
   uint32_t s = 0;
-  for (uint32_t i = c0 + threadIdx.x; i < c1; i += blockDim.x) s += b.ccount[i];
+  for (uint32_t i = c0 + threadIdx.x * SCAN_CPT; i < c1; i += blockDim.x * SCAN_CPT) {
+    const uint4 x = load_cells(b.ccount, i, c1);
+    s += x.x + x.y + x.z + x.w;
+  }
   s = block_sum(s);
   if (threadIdx.x == 0) b.csum[blockIdx.x] = s;
 }
@@ -354,11 +379,12 @@ __global__ void __launch_bounds__(1024) k_cscan_down(Bufs b, Ctrl* ctrl) {
   pre = block_sum(pre);
   if (threadIdx.x == 0) carry = pre;
   __syncthreads();
-  for (uint32_t start = c0; start < c1; start += blockDim.x) {
-    const uint32_t i = start + threadIdx.x;
-    const uint32_t x = (i < c1) ? b.ccount[i] : 0u;
-    if (i < c1) b.ccount[i] = 0u;
-    uint32_t y = x;
+  for (uint32_t start = c0; start < c1; start += blockDim.x * SCAN_CPT) {
+    const uint32_t i = start + threadIdx.x * SCAN_CPT;
+    const uint4 x = load_cells(b.ccount, i, c1);
+    store_cells(b.ccount, i, c1, make_uint4(0u, 0u, 0u, 0u));
+    const uint32_t t1 = x.x, t2 = t1 + x.y, t3 = t2 + x.z, t4 = t3 + x.w;  // inclusive, in the thread
+    uint32_t y = t4;
     for (int o = 1; o < 32; o <<= 1) {
       const uint32_t t = __shfl_up_sync(0xffffffffu, y, o);
       if (lane >= o) y += t;
@@ -374,10 +400,10 @@ __global__ void __launch_bounds__(1024) k_cscan_down(Bufs b, Ctrl* ctrl) {
       ws[lane] = w;
     }
     __syncthreads();
-    const uint32_t c = carry + (wid ? ws[wid - 1] : 0u);
-    if (i < c1) b.cstart[i] = c + y - x;
+    const uint32_t c = carry + (wid ? ws[wid - 1] : 0u) + y - t4;  // start of the thread's first cell
+    store_cells(b.cstart, i, c1, make_uint4(c, c + t1, c + t2, c + t3));
     __syncthreads();
-    if (threadIdx.x == blockDim.x - 1) carry = c + y;
+    if (threadIdx.x == blockDim.x - 1) carry = c + t4;
     __syncthreads();
   }
   if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) {

@@ -752,7 +752,7 @@ __global__ void __launch_bounds__(LONG_WARPS * 32) k_sweep_long(Bufs b, PairPara
         first = b.ovf[o];
       }
       if (lane == 0) {
-        b.off[s] = (uint32_t)o;
+        b.slab[(size_t)s * SLAB] = (uint32_t)o;  // a long list's overflow offset, in its unused slab row
         b.wstate[s] = pack_state(first, 0u, sp);  // entry 0 of the list
       }
     }

@@ -77,7 +77,7 @@ __device__ __forceinline__ bool beats(int x, int y) {
 __device__ __forceinline__ uint32_t next_partner(const Bufs& b, uint32_t s, uint32_t h) {
   const uint32_t d = b.deg[s];
   if (h >= d) return NONE;
-  return d <= SLAB ? b.slab[(size_t)s * SLAB + h] : b.ovf[(size_t)b.off[s] + h];
+  return d <= SLAB ? b.slab[(size_t)s * SLAB + h] : b.ovf[(size_t)b.slab[(size_t)s * SLAB] + h];
 }
 
 // The species both endpoints hold after a pair of species a and b whose applier's list entry is e
@@ -183,26 +183,23 @@ __device__ void tl_group(const Bufs& b, uint32_t step, Ctrl* ctrl, unsigned long
   const uint32_t hi = min(g_hi, lo + V);
   const uint32_t nloc = hi - lo;
   // every load of the set-up is independent: the whole slab row (two 16-byte loads; entries past
-  // the degree are never read) and the overflow offset, for all of the thread's vertices at once
+  // the degree are never read; slot 0 of a long list is its overflow offset), for all of the
+  // thread's vertices at once
 #pragma unroll
   for (int k = 0; k < TL_VPT; ++k) {
     const uint32_t l = threadIdx.x + (uint32_t)k * RD_THREADS;
     if (l < nloc) {
       const uint32_t s = lo + l;
       const unsigned long long w0 = ld_relaxed(b.wstate + s);  // written by the sweep, which published every first pair
-      const uint32_t sid = b.sid[s], d = b.deg[s], off = b.off[s];
+      const uint32_t sid = b.sid[s], d = b.deg[s];
       const uint4* row = reinterpret_cast<const uint4*>(b.slab + (size_t)s * SLAB);
       const uint4 r0 = row[0], r1 = row[1];
       t.w[l] = w0;
       t.sid[l] = sid;
       t.deg[l] = d;
-      if (d <= SLAB) {
-        t.lst[0 * TL_VMAX + l] = r0.x, t.lst[1 * TL_VMAX + l] = r0.y, t.lst[2 * TL_VMAX + l] = r0.z;
-        t.lst[3 * TL_VMAX + l] = r0.w, t.lst[4 * TL_VMAX + l] = r1.x, t.lst[5 * TL_VMAX + l] = r1.y;
-        t.lst[6 * TL_VMAX + l] = r1.z, t.lst[7 * TL_VMAX + l] = r1.w;
-      } else {
-        t.lst[l] = off;
-      }
+      t.lst[0 * TL_VMAX + l] = r0.x, t.lst[1 * TL_VMAX + l] = r0.y, t.lst[2 * TL_VMAX + l] = r0.z;
+      t.lst[3 * TL_VMAX + l] = r0.w, t.lst[4 * TL_VMAX + l] = r1.x, t.lst[5 * TL_VMAX + l] = r1.y;
+      t.lst[6 * TL_VMAX + l] = r1.z, t.lst[7 * TL_VMAX + l] = r1.w;
     }
   }
   __syncthreads();
@@ -243,7 +240,7 @@ __device__ void tl_group(const Bufs& b, uint32_t step, Ctrl* ctrl, unsigned long
         nu = tl_entry(b, t, u - lo, hu + 1u);
       } else {
         const uint32_t du = b.deg[u];
-        nu = hu + 1u < du ? (du <= SLAB ? b.slab[(size_t)u * SLAB + hu + 1u] : b.ovf[(size_t)b.off[u] + hu + 1u]) : NONE;
+        nu = hu + 1u < du ? (du <= SLAB ? b.slab[(size_t)u * SLAB + hu + 1u] : b.ovf[(size_t)b.slab[(size_t)u * SLAB] + hu + 1u]) : NONE;
       }
       const int o = rps_outcome(state_species(ws), state_species(wu), ue);
       const int new_s = o < 0 ? state_species(ws) : o, new_u = o < 0 ? state_species(wu) : o;

@@ -64,7 +64,7 @@ struct lm_ctx {
   int8_t* species = nullptr;
   uint8_t* status = nullptr;
   uint32_t *key = nullptr, *rank = nullptr, *sid = nullptr, *skey = nullptr, *sens = nullptr, *deg = nullptr;
-  uint32_t *slab = nullptr, *off = nullptr, *longv = nullptr, *level = nullptr;
+  uint32_t *slab = nullptr, *longv = nullptr, *level = nullptr;
   unsigned long long* wstate = nullptr;
   uint32_t* act = nullptr;
   float2* spos = nullptr;
@@ -283,7 +283,7 @@ int ensure_slots(lm_ctx* c, uint32_t slots, uint32_t n_ens) {
         (r = dalloc(c, &c->plat, cap)) || (r = dalloc(c, &c->species, cap)) || (r = dalloc(c, &c->status, cap)) ||
         (r = dalloc(c, &c->key, cap)) || (r = dalloc(c, &c->rank, cap)) || (r = dalloc(c, &c->sid, cap)) ||
         (r = dalloc(c, &c->skey, cap)) || (r = dalloc(c, &c->sens, cap)) || (r = dalloc(c, &c->deg, cap)) ||
-        (r = dalloc(c, &c->slab, (size_t)cap * SLAB)) || (r = dalloc(c, &c->off, cap)) ||
+        (r = dalloc(c, &c->slab, (size_t)cap * SLAB)) ||
         (r = dalloc(c, &c->longv, cap)) || (r = dalloc(c, &c->wstate, cap)) ||
         (r = dalloc(c, &c->level, cap)) || (r = dalloc(c, &c->act, cap)) || (r = dalloc(c, &c->spos, cap)) ||
         (r = dalloc(c, &c->map_d, cap)) || (r = dalloc(c, &c->block_ens, nblk)))
@@ -404,7 +404,6 @@ Bufs bufs(const lm_ctx* c, bool log) {
   b.spos = c->spos;
   b.deg = c->deg;
   b.slab = c->slab;
-  b.off = c->off;
   b.ovf = c->ovf;
   b.oprio = c->oprio;
   b.longv = c->longv;
@@ -805,7 +804,7 @@ int lm_ctx_destroy(lm_ctx* c) {
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
   if (c->graph) cudaGraphDestroy(c->graph);
   void* bufs_[] = {c->uv,     c->xo,    c->yo,     c->plon,   c->plat,   c->species, c->status, c->key,
-                   c->rank,   c->sid,   c->skey,   c->sens,   c->deg,    c->slab,    c->off,    c->longv,
+                   c->rank,   c->sid,   c->skey,   c->sens,   c->deg,    c->slab,    c->longv,
                    c->wstate, c->level,  c->act,    c->spos,
                    c->map_d,  c->block_ens, c->ens_d, c->grids, c->eord, c->ebox, c->census,  c->ccount, c->cstart,
                    c->csum,   c->ovf,   c->oprio,  c->ctrl,   c->plog,  c->snap_xo, c->snap_yo, c->snap_sp,
@@ -1216,10 +1215,9 @@ int lm_query_pairs(lm_ctx* c, int64_t n, const float* lon, const float* lat, int
   if ((r = clear_err_bits(c, ERRB_NAN))) return r;  // non-finite query points are never paired
   const uint32_t nv = c->hctrl->n_valid;
   const size_t novf = (size_t)c->hctrl->ovf_used;
-  std::vector<uint32_t> deg(nv), off(nv), ids(nv), slab((size_t)nv * SLAB), ovf(novf);
+  std::vector<uint32_t> deg(nv), ids(nv), slab((size_t)nv * SLAB), ovf(novf);
   if (nv) {
     CK(cudaMemcpyAsync(deg.data(), c->deg, nv * 4, cudaMemcpyDeviceToHost, c->st));
-    CK(cudaMemcpyAsync(off.data(), c->off, nv * 4, cudaMemcpyDeviceToHost, c->st));
     CK(cudaMemcpyAsync(ids.data(), c->sid, nv * 4, cudaMemcpyDeviceToHost, c->st));
     CK(cudaMemcpyAsync(slab.data(), c->slab, (size_t)nv * SLAB * 4, cudaMemcpyDeviceToHost, c->st));
   }
@@ -1229,7 +1227,7 @@ int lm_query_pairs(lm_ctx* c, int64_t n, const float* lon, const float* lat, int
   pairs.reserve((size_t)c->hctrl->n_dir / 2);
   for (uint32_t s = 0; s < nv; ++s)
     for (uint32_t h = 0; h < deg[s]; ++h) {
-      const uint32_t t = entry_id(deg[s] <= SLAB ? slab[(size_t)s * SLAB + h] : ovf[(size_t)off[s] + h]);
+      const uint32_t t = entry_id(deg[s] <= SLAB ? slab[(size_t)s * SLAB + h] : ovf[(size_t)slab[(size_t)s * SLAB] + h]);
       const uint32_t a_ = ids[s], b_ = ids[t];
       if (a_ < b_) pairs.push_back(((uint64_t)a_ << 32) | b_);
     }

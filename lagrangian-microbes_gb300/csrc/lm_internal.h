@@ -13,8 +13,9 @@
 //              uint32 key[S], rank[S]     (cell key, rank inside the cell from the counting pass)
 //              uint32 ccount[C+1], cstart[C+1]  (cell counts / exclusive starts, C = cell capacity)
 //              uint32 sid[S], skey[S], sens[S]; float2 spos[S]  (particles in cell order)
-//              uint32 deg[S], slab[S][SLAB]     (neighbour lists up to SLAB, sorted by priority)
-//              uint32 off[S], ovf[cap]; uint64 oprio[cap]  (longer lists, allocated per step)
+//              uint32 deg[S], slab[S][SLAB]     (neighbour lists up to SLAB, sorted by priority;
+//                                                a longer list's overflow offset in slot 0)
+//              uint32 ovf[cap]; uint64 oprio[cap]  (longer lists, allocated per step)
 //              uint64 wstate[S] = species << 56 | list position << 32 | partner;
 //              uint32 level[S] (pair-log runs only), act[S]   (interaction dataflow)
 #pragma once
@@ -227,8 +228,7 @@ struct Bufs {
   uint32_t* sens;
   float2* spos;
   uint32_t* deg;
-  uint32_t* slab;     // [S][SLAB]
-  uint32_t* off;
+  uint32_t* slab;     // [S][SLAB]; slot 0 of a list longer than SLAB holds its offset in ovf
   uint32_t* ovf;
   unsigned long long* oprio;
   uint32_t* longv;    // vertices with lists longer than SLAB
