@@ -195,7 +195,7 @@ __device__ __forceinline__ void sweep_draws(const Bufs& b, uint32_t step, uint32
     if ((mask >> k) & 1u) e[k] |= (uint32_t)q_bits[w][lane * SLAB + k] << ENTRY_WIN_SHIFT;
 }
 
-__global__ void __launch_bounds__(SLOT_BLOCK) k_sweep(Bufs b, PairParams pp, StepArgs a, Ctrl* ctrl) {
+__global__ void __launch_bounds__(SLOT_BLOCK, 5) k_sweep(Bufs b, PairParams pp, StepArgs a, Ctrl* ctrl) {
   pdl_wait();
   if (ctrl->halt) return;
   const uint32_t n_valid = ctrl->n_valid;
