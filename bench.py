@@ -47,6 +47,16 @@ TUNE_DAY = 3  # the autotuner times steps from the state after this many simulat
 WORKLOAD = "490k microbes, 700x700 lattice lon 200-205E lat 25-30N, 1/12 deg hourly psi field, RK4 dt=1h, r=0.01 deg, p=0.7"
 
 
+METRIC = "microbe-steps/s (advect+interact), batched+graphed vs plain, 1 GB300, <=10 m err"
+DTYPE = "f32 (positions), f64 (pair-boundary refine), int8 (species)"
+
+
+def bench_config(world: int) -> dict:
+    """The workload both arms report (the same dict, so the two lines compare like for like)."""
+    return {"workload": WORKLOAD, "microbes": N_MICROBES, "parallelism": f"replicas x{world}",
+            "l2": "flushed: a 512 MiB buffer is written between timed GPU bench steps"}
+
+
 def env_rank():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
@@ -306,14 +316,13 @@ def run_gb300(args):
     launches_per_step = (sum(v["launches"] for v in kernels.values()) / prof_steps) * spg
     if rank == 0:
         line = {
-            "metric": "microbe-steps/s (advect+interact), batched+graphed vs plain, 1 GB300, <=10 m err",
+            "metric": METRIC,
             "value": value, "unit": "microbe-steps/s", "n_gpus": world, "steps": K, "warmup": W,
             "ms_per_step": total_ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32 (positions), f64 (pair-boundary refine), int8 (species)", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "microbes": n, "sim_steps_per_bench_step": spg,
-                       "sim_steps_timed": sim_steps, "parallelism": f"replicas x{world}",
-                       "l2": "512 MiB buffer written between timed bench steps", "form": "cuda-graph, 24 steps/launch",
-                       "tuning": {k: v for k, v in tuned.items() if k != "seconds"}, "autotune_s": tuned["seconds"]},
+            "dtype": DTYPE, "data": "synthetic",
+            "config": bench_config(world),
+            "run": {"sim_steps_per_bench_step": spg, "sim_steps_timed": sim_steps, "form": "cuda-graph, 24 steps/launch",
+                    "tuning": {k: v for k, v in tuned.items() if k != "seconds"}, "autotune_s": tuned["seconds"]},
             "pairs_per_step": pairs_per_step,
             "plain": {"value": plain_value, "unit": "microbe-steps/s", "sim_steps": plain_steps,
                       "graph_speedup": value / world / plain_value},
@@ -866,11 +875,12 @@ def run_reference(args):
         times.append(time.perf_counter() - t0)
     total = sum(times)
     value = lons.size * K / total
-    line = {"impl": "reference", "metric": "microbe-steps/s (advect+interact), batched+graphed vs plain, 1 GB300, <=10 m err",
+    line = {"impl": "reference", "metric": METRIC,
             "value": value, "unit": "microbe-steps/s", "n_gpus": world, "steps": K, "warmup": W,
             "ms_per_step": 1e3 * total / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32 (positions), f64 (pair test), int8 (species)", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "microbes": lons.size, "sim_steps_per_bench_step": 1},
+            "dtype": DTYPE, "data": "synthetic",
+            "config": bench_config(world),
+            "run": {"sim_steps_per_bench_step": 1, "form": "the oracle's fused CPU step on all host threads"},
             "cpu_baseline": {"value": value, "unit": "microbe-steps/s", "cores": threads, "kind": "port",
                              "sample": f"{K} fused steps of the full 490k workload (one step per bench step)"},
             "e2e": {"value": value, "unit": "microbe-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
