@@ -1,7 +1,7 @@
 """Generate the golden fixtures of tests/golden/ by running the reference's own code.
 
-Run in a container where the reference checkout is available (default /root/reference, or the
-LM_REFERENCE_DIR environment variable). The reference's Python modules are imported unmodified
+Run where a checkout of the reference is available, named by the LM_REFERENCE_DIR environment
+variable (there is no default). The reference's Python modules are imported unmodified
 with stub modules for the packages that are absent here (xarray, parcels); scipy's cKDTree is
 the installed one. Outputs (small .npz files) are committed and read by the CPU tests; nothing at
 test time reads the reference.

@@ -45,22 +45,6 @@ def test_python_binding_matches_the_header(lm):
         assert len(argtypes) == protos[name], name
 
 
-def test_integration_notes_binding_matches_the_library(lm):
-    # the ctypes stubs a maintainer would paste into the reference declare the
-    # same argument types as the package's own binding
-    from lagrangian_microbes_gb300 import _lib
-    env = {"P": ctypes.c_void_p, "I32": ctypes.c_int, "I64": ctypes.c_int64, "U32": ctypes.c_uint32,
-           "U64": ctypes.c_uint64, "F64": ctypes.c_double, "ctypes": ctypes}
-    with open(os.path.join(REPO, "INTEGRATION.md")) as f:
-        stubs = re.findall(r"_L\.(lm_\w+)\.argtypes = (\[.*?\])\n", f.read())
-    assert len(stubs) >= 10
-    for name, expr in stubs:
-        got, want = eval(expr, env), _lib.SIGNATURES[name]
-        assert len(got) == len(want), name
-        for a, b in zip(got, want):
-            assert a == b or getattr(a, "_type_", 0) == getattr(b, "_type_", 1), (name, a, b)
-
-
 def test_stats_struct_matches_the_header(lm):
     from lagrangian_microbes_gb300 import _lib
     body = re.search(r"typedef struct lm_stats \{(.*?)\} lm_stats;", _header_text(), flags=re.S).group(1)
