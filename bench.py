@@ -389,8 +389,7 @@ def run_dropin(fld, lons, lats, species, local: int, stream):
     sim.step(0.0, DT, 2, step0=0)  # warm-up (list capacities, the record ring)
     sim.upload_particles(lons, lats, species)
     sim.snapshot()
-    bufs = {"lon": np.zeros((steps, n), np.float32), "lat": np.zeros((steps, n), np.float32),
-            "species": np.zeros((steps, n), np.int8)}
+    bufs = sim.record_buffers(steps)
     walls = {}
     for mode in ("plain", "reused", "fresh", "plain", "reused", "fresh"):
         sim.restore()
@@ -413,8 +412,9 @@ def run_dropin(fld, lons, lats, species, local: int, stream):
                             "recorded_over_unrecorded": walls["reused"] / walls["plain"],
                             "recorded_into_fresh_arrays_ms_per_step": 1e3 * walls["fresh"] / steps,
                             "record_bytes_per_step": 9 * n,
-                            "note": "records copied on a second stream into reused host arrays; fresh arrays pay "
-                                    "the page faults of new host memory on every call"}}
+                            "note": "records copied on a second stream into reused page-locked host arrays "
+                                    "(Simulation.record_buffers); fresh pageable arrays pay the page faults of new "
+                                    "host memory and hold the host thread for every copy"}}
 
 
 def dependency_depth(sim, step: int) -> int:

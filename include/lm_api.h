@@ -80,6 +80,12 @@ int lm_version(void);
  * (cudaFuncAttributes::binaryVersion: 103 for sm_103a). LM_ERR_CUDA when no GPU can load them. */
 int lm_kernel_arch(int* sm);
 
+/* Page-locked host memory (cudaHostAlloc, portable across contexts) for step records: device-to-host
+ * copies into it run asynchronously on the context's copy stream, overlapping the next steps, where
+ * copies into pageable memory hold the calling thread for each record. Free with lm_host_free. */
+int lm_host_alloc(size_t bytes, void** ptr);
+int lm_host_free(void* ptr);
+
 /* Create a context on CUDA device `device` with its own non-blocking stream. */
 int lm_ctx_create(int device, lm_ctx** out);
 int lm_ctx_destroy(lm_ctx* ctx);

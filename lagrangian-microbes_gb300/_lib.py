@@ -100,6 +100,8 @@ F64 = ctypes.c_double
 SIGNATURES = {
     "lm_version": [],
     "lm_kernel_arch": [ctypes.POINTER(I32)],
+    "lm_host_alloc": [ctypes.c_size_t, ctypes.POINTER(P)],
+    "lm_host_free": [P],
     "lm_ctx_create": [I32, ctypes.POINTER(P)],
     "lm_ctx_destroy": [P],
     "lm_last_error": [P, ctypes.c_char_p, ctypes.c_size_t],
@@ -169,6 +171,35 @@ def load(build_if_missing: bool = True):
             fn.restype = ctypes.c_int
         _lib = lib
         return lib
+
+
+class _HostBlock:
+    """Owns one lm_host_alloc block; freed when the last array viewing it is gone."""
+
+    def __init__(self, lib, nbytes: int):
+        self._lib = lib
+        p = ctypes.c_void_p()
+        rc = lib.lm_host_alloc(nbytes, ctypes.byref(p))
+        if rc != LM_OK:
+            raise _error(rc, f"page-locked allocation of {nbytes} bytes failed")
+        self.addr = p.value
+        self.nbytes = nbytes
+
+    def __del__(self):
+        if getattr(self, "addr", None):
+            self._lib.lm_host_free(ctypes.c_void_p(self.addr))
+            self.addr = None
+
+
+def host_empty(shape, dtype) -> np.ndarray:
+    """A C-contiguous numpy array in page-locked host memory (for step records: their copies then
+    overlap the following steps instead of holding the calling thread)."""
+    dtype = np.dtype(dtype)
+    nbytes = int(np.prod(shape, dtype=np.int64)) * dtype.itemsize
+    block = _HostBlock(load(), nbytes)
+    raw = (ctypes.c_uint8 * max(nbytes, 1)).from_address(block.addr)
+    raw._block = block  # the ctypes buffer keeps the block alive; numpy keeps the buffer
+    return np.frombuffer(raw, dtype=np.uint8, count=nbytes).view(dtype).reshape(shape)
 
 
 def ptr(a: np.ndarray | None):

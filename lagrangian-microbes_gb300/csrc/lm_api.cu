@@ -748,6 +748,33 @@ extern "C" {
 
 int lm_version(void) { return LM_API_VERSION; }
 
+int lm_host_alloc(size_t bytes, void** ptr) {
+  if (!ptr) {
+    set_thread_error("NULL argument");
+    return LM_ERR_ARG;
+  }
+  *ptr = nullptr;
+  const cudaError_t e = cudaHostAlloc(ptr, bytes ? bytes : 1, cudaHostAllocPortable);
+  if (e != cudaSuccess) {
+    *ptr = nullptr;
+    cudaGetLastError();
+    set_thread_error(cudaGetErrorString(e));
+    return LM_ERR_OOM;
+  }
+  return LM_OK;
+}
+
+int lm_host_free(void* ptr) {
+  if (!ptr) return LM_OK;
+  const cudaError_t e = cudaFreeHost(ptr);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    set_thread_error(cudaGetErrorString(e));
+    return LM_ERR_CUDA;
+  }
+  return LM_OK;
+}
+
 int lm_kernel_arch(int* sm) {
   if (!sm) {
     set_thread_error("NULL argument");

@@ -252,6 +252,14 @@ class Simulation:
             out["census"] = rec_c
         return out
 
+    def record_buffers(self, n_steps: int) -> dict:
+        """Record arrays for ``step(..., record=True, out=...)`` in page-locked host memory:
+        {"lon", "lat"} float32 and {"species"} int8 of [n_steps, N]. Copies into them run on the
+        context's copy stream while the next steps compute; reuse them from call to call."""
+        shape = (int(n_steps), self.n)
+        return {"lon": _lib.host_empty(shape, np.float32), "lat": _lib.host_empty(shape, np.float32),
+                "species": _lib.host_empty(shape, np.int8)}
+
     def capture(self, t_start, dt, steps_per_graph: int, interact: bool = True, census: bool = False,
                 step0: int | None = None, count_pairs: bool = False) -> None:
         """Capture steps_per_graph fused steps as one CUDA graph (time origin t_start at step0)."""

@@ -128,12 +128,10 @@ class ParticleAdvecter:
         logger.info("Starting time stepping: %s -> %s (dt=%s) on the GPU.", start_time, end_time, dt)
         t = start_time
         iteration = self.iteration
-        # two record buffers, reused from chunk to chunk: the GPU fills one while the writer pickles
-        # the other (fresh host memory would be page-faulted in by every chunk's copies)
+        # two page-locked record buffers, reused from chunk to chunk: the GPU fills one while the
+        # writer pickles the other, and each step's copy overlaps the next steps
         if self._records is None:
-            shape = (self.output_chunk_iters, self.N_particles)
-            self._records = [{"lon": np.zeros(shape, np.float32), "lat": np.zeros(shape, np.float32),
-                              "species": np.zeros(shape, np.int8)} for _ in range(2)]
+            self._records = [sim.record_buffers(self.output_chunk_iters) for _ in range(2)]
         chunk = 0
         with ThreadPoolExecutor(max_workers=1) as writer:
             pending = None

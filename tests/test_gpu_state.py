@@ -131,3 +131,21 @@ def test_launch_shape_knobs_change_speed_only(lm, orc, small_field):
     for x, y in zip(want, sim.state()):
         np.testing.assert_array_equal(x, y)
     sim.close()
+
+
+def test_page_locked_record_buffers_hold_the_same_records(lm, orc, small_field):
+    """Records copied into page-locked buffers (asynchronous copies on the copy stream) equal the
+    records copied into fresh numpy arrays, step by step, over calls that reuse the buffers."""
+    t0 = float(small_field.times[0])
+    a, _ = _sim(lm, orc, small_field)
+    b, _ = _sim(lm, orc, small_field)
+    bufs = b.record_buffers(4)
+    assert all(not v.flags["OWNDATA"] and v.flags["C_CONTIGUOUS"] for v in bufs.values())
+    for call in range(3):
+        want = a.step(t0 + 4 * call * 3600.0, 3600.0, 4, record=True, step0=4 * call)
+        got = b.step(t0 + 4 * call * 3600.0, 3600.0, 4, record=True, step0=4 * call, out=bufs)
+        for k in ("lon", "lat", "species"):
+            np.testing.assert_array_equal(got[k], want[k], err_msg=f"call {call}, {k}")
+    a.close()
+    b.close()
+    del bufs, got  # the blocks are freed with the last array that views them
