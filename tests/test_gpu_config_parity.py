@@ -8,7 +8,8 @@
   (rock_paper_scissors_example.py:22-36): 10k lattice, 0.25 deg 6-hourly field, 48 hourly steps,
   r = 0.01 with interaction;
 * the batching configuration: all 256 ensembles of the benchmark in one context against each
-  ensemble run alone, and the densest ensemble against the oracle.
+  ensemble run alone, and the densest ensemble against the oracle, on its first steps and on its
+  last simulated day (reached through one-day field windows).
 
 The oracle replays each step's pairs in the GPU's application order with a restatement of the
 reference's pair rule (interaction_simulator.py:98-105, interactions.py:13-40), so equal species
@@ -139,3 +140,50 @@ def test_batching_configuration_all_256_ensembles(lm, orc):
     for s in range(2):
         sp, _ = orc.interact_step(lon_e[e][s], lat_e[e][s], sp, bench.RADIUS, 2, ps[e], ps[e], ps[e], int(seeds[e]), s)
         np.testing.assert_array_equal(sp_e[e][s], sp, err_msg=f"densest ensemble {e}, step {s}")
+
+
+def test_batching_configuration_last_simulated_day(lm, orc):
+    """The batching configuration at the end of its 240 steps: the batch advanced to step 216
+    through one-day field windows, then two recorded steps. The densest ensembles (and two others)
+    run alone from the batch's exported state give the same records bit for bit, and the densest
+    ensemble that kept all its microbes on the grid matches the oracle's replay."""
+    from lagrangian_microbes_gb300 import engine
+    bench = _bench()
+    bases = bench.ensemble_bases(bench.B_ENSEMBLES)
+    fields, ens, ps, seeds = bench.make_ensembles(bench.B_ENSEMBLES, bench.B_STEPS + 1, bases=bases)
+    bat = engine.EnsembleSimulation(fields, ens, radius=bench.RADIUS, p_rs=ps, p_pr=ps, p_sp=ps, seeds=seeds)
+    late, dt = bench.B_TOTAL_STEPS - bench.B_STEPS, bench.DT
+    for d in range(0, late, bench.B_STEPS):
+        if d:
+            bat.upload_fields([b.frames(d, bench.B_STEPS + 1) for b in bases])
+        bench._oob_ok(bat.step, d * dt, dt, bench.B_STEPS, step0=d)
+    bat.upload_fields([b.frames(late, 4) for b in bases])
+    state = bat.export_state()
+    assert state["step"] == late
+    bufs = bat.record_buffers(2)
+    bench._oob_ok(bat.step, late * dt, dt, 2, record=True, step0=late, out=bufs)  # records kept in bufs
+    lon_e, lat_e, sp_e = bat.split(bufs["lon"]), bat.split(bufs["lat"]), bat.split(bufs["species"])
+    edges = np.concatenate([[0], np.cumsum([x[0].size for x in ens])])
+    on_grid = [bool((state["status"][edges[e]:edges[e + 1]] == 0).all()) for e in range(len(ens))]
+    dens = np.array([x[0].size / max(np.ptp(x[0]) * np.ptp(x[1]), 1e-9) for x in ens])
+    order = [int(e) for e in np.argsort(-dens)]
+    chosen = order[:3] + order[len(order) // 2:len(order) // 2 + 2]
+    for e in chosen:
+        a, b = edges[e], edges[e + 1]
+        one = engine.Simulation(bases[e].frames(late, 4), ens[e][0], ens[e][1], ens[e][2], radius=bench.RADIUS,
+                                p_rs=ps[e], p_pr=ps[e], p_sp=ps[e], seed=int(seeds[e]))
+        one.import_state({k: (v[a:b] if k != "step" else v) for k, v in state.items()})
+        ob = one.record_buffers(2)
+        bench._oob_ok(one.step, late * dt, dt, 2, record=True, step0=late, out=ob)
+        one.close()
+        np.testing.assert_array_equal(lon_e[e], ob["lon"], err_msg=f"ensemble {e}")
+        np.testing.assert_array_equal(lat_e[e], ob["lat"], err_msg=f"ensemble {e}")
+        np.testing.assert_array_equal(sp_e[e], ob["species"], err_msg=f"ensemble {e}")
+    bat.close()
+    e = next(e for e in order if on_grid[e])
+    sp = state["species"][edges[e]:edges[e + 1]].copy()
+    for s in range(2):
+        sp, m = orc.interact_step(lon_e[e][s], lat_e[e][s], sp, bench.RADIUS, 2, ps[e], ps[e], ps[e], int(seeds[e]),
+                                  late + s)
+        assert m > 0
+        np.testing.assert_array_equal(sp_e[e][s], sp, err_msg=f"densest on-grid ensemble {e}, step {late + s}")
