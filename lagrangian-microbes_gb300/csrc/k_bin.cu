@@ -24,16 +24,20 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
 // Cells of one ensemble's grid at cell size c (1 for an empty ensemble). Float32 throughout: the
 // grid only has to be consistent within the step (any c >= r gives the same pairs), and float64 is
 // slow on this GPU.
-__device__ __forceinline__ float grid_dims(const uint32_t* box, float c, float* ncx, float* ncy) {
+__device__ __forceinline__ float grid_dims(const uint32_t* box, float c, float n, float* ncx, float* ncy,
+                                           uint32_t* tshift) {
   const float mnx = dec_f(box[0]), mny = dec_f(box[1]), mxx = dec_f(box[2]), mxy = dec_f(box[3]);
   if (!(mnx <= mxx && mny <= mxy)) {
     *ncx = *ncy = 1.f;
+    *tshift = 3u;
     return 1.f;
   }
   *ncx = floorf((mxx - mnx) / c) + 3.f;
   *ncy = floorf((mxy - mny) / c) + 3.f;
-  // the key range covers whole TILE x TILE tiles
-  return ceilf(*ncx / (float)TILE) * ceilf(*ncy / (float)TILE) * (float)(TILE * TILE);
+  *tshift = tile_shift(n, *ncx * *ncy);
+  // the key range covers whole tiles
+  const float t = (float)(1u << *tshift);
+  return ceilf(*ncx / t) * ceilf(*ncy / t) * (t * t);
 }
 
 // Key ranges in ensemble index order (batches of more ensembles than the block has threads).
@@ -42,8 +46,8 @@ __device__ __forceinline__ void grid_in_order(const Bufs& b, float c, unsigned l
   for (uint32_t e0 = 0; e0 < b.n_ens; e0 += GRID_THREADS) {
     const uint32_t e = e0 + threadIdx.x;
     float nx = 0.f, ny = 0.f;
-    uint32_t cells = 0;
-    if (e < b.n_ens) cells = (uint32_t)fminf(grid_dims(b.ebox + 4 * e, c, &nx, &ny), 4.0e9f);
+    uint32_t cells = 0, ts = 3u;
+    if (e < b.n_ens) cells = (uint32_t)fminf(grid_dims(b.ebox + 4 * e, c, (float)b.ens[e].n, &nx, &ny, &ts), 4.0e9f);
     uint32_t y = cells;
     for (int o = 1; o < 32; o <<= 1) {
       const uint32_t t = __shfl_up_sync(0xffffffffu, y, o);
@@ -68,7 +72,7 @@ __device__ __forceinline__ void grid_in_order(const Bufs& b, float c, unsigned l
       g.ncx = (int)nx;
       g.ncy = (int)ny;
       g.cell_base = (uint32_t)(base > 0xffffffffull ? 0xffffffffull : base);
-      g.pad = 0;
+      g.tshift = ts;
       b.grids[e] = g;
     }
     __syncthreads();
@@ -91,10 +95,10 @@ __device__ __forceinline__ void grid_ranked(const Bufs& b, float c, unsigned lon
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const uint32_t E = b.n_ens, e = threadIdx.x;
   float nx = 0.f, ny = 0.f, dens = -1.f;
-  uint32_t cells = 0;
+  uint32_t cells = 0, ts = 3u;
   if (e < E) {
     const uint32_t* box = b.ebox + 4 * e;
-    cells = (uint32_t)fminf(grid_dims(box, c, &nx, &ny), 4.0e9f);
+    cells = (uint32_t)fminf(grid_dims(box, c, (float)b.ens[e].n, &nx, &ny, &ts), 4.0e9f);
     const float w = dec_f(box[2]) - dec_f(box[0]), h = dec_f(box[3]) - dec_f(box[1]);
     dens = (w >= 0.f && h >= 0.f) ? (float)b.ens[e].n / ((w + c) * (h + c)) : 0.f;  // also NaN -> 0
   }
@@ -139,7 +143,7 @@ __device__ __forceinline__ void grid_ranked(const Bufs& b, float c, unsigned lon
     g.ncx = (int)nx;
     g.ncy = (int)ny;
     g.cell_base = (uint32_t)(base > 0xffffffffull ? 0xffffffffull : base);
-    g.pad = 0;
+    g.tshift = ts;
     b.grids[e] = g;
   }
   if (threadIdx.x == 0) *carry_sh = tot;
@@ -162,7 +166,8 @@ __global__ void __launch_bounds__(GRID_THREADS) k_grid(Bufs b, PairParams pp, Ct
     float t = 0.f;
     for (uint32_t e = threadIdx.x; e < b.n_ens; e += GRID_THREADS) {
       float nx, ny;
-      t += grid_dims(b.ebox + 4 * e, c, &nx, &ny);
+      uint32_t ts;
+      t += grid_dims(b.ebox + 4 * e, c, (float)b.ens[e].n, &nx, &ny, &ts);
     }
     for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
     if (lane == 0) ws[wid] = t;
@@ -211,13 +216,15 @@ __device__ __forceinline__ EnsGrid single_grid(const Bufs& b, const PairParams& 
   float c = pp.cell_factor * (float)pp.r;
   if (!(c > 0.f)) c = 1e-3f;
   const float cap = (float)b.cells_cap;
+  const float n = (float)b.ens[0].n;
   float nx, ny, total = 0.f;
+  uint32_t ts = 3u;
   for (int attempt = 0; attempt < 16; ++attempt) {
-    total = grid_dims(b.ebox, c, &nx, &ny);
+    total = grid_dims(b.ebox, c, n, &nx, &ny, &ts);
     if (total <= cap * 0.999f) break;
     c = c * sqrtf(total / cap) * 1.02f;
   }
-  total = grid_dims(b.ebox, c, &nx, &ny);
+  total = grid_dims(b.ebox, c, n, &nx, &ny, &ts);
   EnsGrid g;
   const bool empty = !(dec_f(b.ebox[0]) <= dec_f(b.ebox[2]));
   g.c = c;
@@ -227,7 +234,7 @@ __device__ __forceinline__ EnsGrid single_grid(const Bufs& b, const PairParams& 
   g.ncx = (int)nx;
   g.ncy = (int)ny;
   g.cell_base = 0;
-  g.pad = 0;
+  g.tshift = ts;
   *cells = (uint32_t)fminf(total, 4.0e9f);
   *fits = *cells <= b.cells_cap;
   return g;

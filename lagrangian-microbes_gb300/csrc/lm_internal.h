@@ -107,22 +107,32 @@ struct EnsGrid {
   float x0, y0, inv_c, c;
   int ncx, ncy;
   uint32_t cell_base;
-  uint32_t pad;
+  uint32_t tshift;  // tiles of (1 << tshift) x (1 << tshift) cells
 };
 
-// Cell numbering inside an ensemble's key range is tile-major: TILE x TILE cells form a tile,
-// tiles are numbered row by row, cells inside a tile row by row. Cell-ordered particles of one
-// tile are then contiguous, so a contiguous range of them is a compact 2D patch (the interaction
-// kernel gives such ranges to its blocks). A grid's key range is padded to whole tiles.
-constexpr uint32_t TILE = 16;
-__host__ __device__ inline uint32_t tiles_x(const EnsGrid& g) { return ((uint32_t)g.ncx + TILE - 1) / TILE; }
+// Cell numbering inside an ensemble's key range is tile-major: T x T cells form a tile, tiles are
+// numbered row by row, cells inside a tile row by row. Cell-ordered particles of one tile are
+// then contiguous, so a contiguous range of them is a compact 2D patch (the interaction kernel
+// gives such ranges, 2,048 vertices each, to its blocks). A grid's key range is padded to whole
+// tiles. T is chosen per ensemble and step from its microbes per cell rho (tile_shift): the
+// interaction's ranges come out nearest to square when a tile holds about as many microbes as a
+// block owns, T ~ sqrt(2048 / rho): T = 32 below 4 microbes per cell, 16 below 16, else 8.
+__host__ __device__ inline uint32_t tile_shift(float n, float cells) {
+  const float rho = n / fmaxf(cells, 1.f);
+  return rho < 4.f ? 5u : rho < 16.f ? 4u : 3u;
+}
+__host__ __device__ inline uint32_t tiles_x(const EnsGrid& g) {
+  return ((uint32_t)g.ncx + (1u << g.tshift) - 1u) >> g.tshift;
+}
 __host__ __device__ inline uint32_t cell_index(const EnsGrid& g, uint32_t cx, uint32_t cy) {
-  return ((cy / TILE) * tiles_x(g) + cx / TILE) * (TILE * TILE) + (cy % TILE) * TILE + (cx % TILE);
+  const uint32_t s = g.tshift, m = (1u << s) - 1u;
+  return ((((cy >> s) * tiles_x(g) + (cx >> s)) << s) + (cy & m)) << s | (cx & m);
 }
 __host__ __device__ inline void cell_coords(const EnsGrid& g, uint32_t k, uint32_t* cx, uint32_t* cy) {
-  const uint32_t t = k / (TILE * TILE), in = k % (TILE * TILE), ntx = tiles_x(g);
-  *cx = (t % ntx) * TILE + in % TILE;
-  *cy = (t / ntx) * TILE + in / TILE;
+  const uint32_t s = g.tshift, m = (1u << s) - 1u;
+  const uint32_t t = k >> (2u * s), ntx = tiles_x(g);
+  *cx = ((t % ntx) << s) + (k & m);
+  *cy = ((t / ntx) << s) + ((k >> s) & m);
 }
 // The keys of cells x0..x1 (at most three) of row ry: one contiguous run, or two when the cells
 // straddle a tile edge. Fixed-size, so the callers' loops unroll with static indices.
@@ -132,7 +142,8 @@ struct RowRuns {
 };
 __device__ __forceinline__ RowRuns row_runs(const EnsGrid& g, int x0, int x1, int ry) {
   RowRuns r;
-  const int split = (x0 / (int)TILE) != (x1 / (int)TILE) ? (x0 / (int)TILE) * (int)TILE + (int)TILE - 1 : x1;
+  const int s = (int)g.tshift;
+  const int split = (x0 >> s) != (x1 >> s) ? (((x0 >> s) + 1) << s) - 1 : x1;
   r.lo[0] = g.cell_base + cell_index(g, (uint32_t)x0, (uint32_t)ry);
   r.hi[0] = g.cell_base + cell_index(g, (uint32_t)split, (uint32_t)ry);
   r.n = 1;
