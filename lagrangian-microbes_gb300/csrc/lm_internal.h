@@ -116,10 +116,12 @@ struct EnsGrid {
 // gives such ranges, 2,048 vertices each, to its blocks). A grid's key range is padded to whole
 // tiles. T is chosen per ensemble and step from its microbes per cell rho (tile_shift): the
 // interaction's ranges come out nearest to square when a tile holds about as many microbes as a
-// block owns, T ~ sqrt(2048 / rho): T = 32 below 4 microbes per cell, 16 below 16, else 8.
+// block owns, T ~ sqrt(2048 / rho), rounded down (rho is an average over the bounding box, and
+// clustered microbes are denser than that where they are): T = 32 below 2 microbes per cell, 16
+// below 8, else 8.
 __host__ __device__ inline uint32_t tile_shift(float n, float cells) {
   const float rho = n / fmaxf(cells, 1.f);
-  return rho < 4.f ? 5u : rho < 16.f ? 4u : 3u;
+  return rho < 2.f ? 5u : rho < 8.f ? 4u : 3u;
 }
 __host__ __device__ inline uint32_t tiles_x(const EnsGrid& g) {
   return ((uint32_t)g.ncx + (1u << g.tshift) - 1u) >> g.tshift;
