@@ -165,7 +165,9 @@ __device__ __forceinline__ uint32_t tl_entry(const Bufs& b, const TileSmem& t, u
 }
 
 // The pairs among cell-order vertices [g_lo, g_hi) (a group of whole ensembles, so no pair leaves
-// it), at most TL_VMAX per block: each block owns an equal share of whole RD_THREADS-vertex columns.
+// it), at most TL_VMAX per block: each block owns an equal share, in whole warps. Every block of the
+// grid takes part (whole 1,024-vertex columns left 64 of the 304 blocks idle at 490k, and all but a
+// few idle for a small ensemble run alone).
 template <int RD_THREADS>
 __device__ void tl_group(const Bufs& b, uint32_t step, Ctrl* ctrl, unsigned long long t0, uint32_t g_lo,
                          uint32_t g_hi) {
@@ -177,8 +179,9 @@ __device__ void tl_group(const Bufs& b, uint32_t step, Ctrl* ctrl, unsigned long
   t.deg = t.sid + TL_VMAX;
   t.lst = t.deg + TL_VMAX;
   const uint32_t n_g = g_hi - g_lo;
-  const uint32_t vpt = (n_g + gridDim.x * RD_THREADS - 1) / (gridDim.x * RD_THREADS);
-  const uint32_t V = max(vpt, 1u) * RD_THREADS;
+  // every block gets an equal share, rounded up to whole warps (at most TL_VMAX: the caller checked
+  // that the group fits the grid's shared memory)
+  const uint32_t V = min(TL_VMAX, max(32u, (((n_g + gridDim.x - 1) / gridDim.x) + 31u) & ~31u));
   const uint32_t lo = min(g_hi, g_lo + blockIdx.x * V);
   const uint32_t hi = min(g_hi, lo + V);
   const uint32_t nloc = hi - lo;
