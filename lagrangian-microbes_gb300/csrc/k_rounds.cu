@@ -131,7 +131,7 @@ constexpr int POLL_BATCH = 2;  // vertices whose state words one thread loads be
 // ---- tile-local interaction: block-owned vertex ranges with handshakes in shared memory ----
 //
 // Cell keys are tile-major, so a contiguous range of cell-ordered vertices is a compact 2D patch.
-// Block b owns the vertices [b V, b V + V) (V <= TL_VMAX, whole columns of the block's threads) and keeps their state words,
+// Block b owns the vertices [b V, b V + V) (V <= TL_VMAX: an equal share in whole warps) and keeps their state words,
 // slot ids, degrees and list entries in shared memory. A pair whose two microbes the block owns
 // hands off through shared memory (tens of cycles instead of an L2 round trip); a pair that
 // crosses blocks goes through the global state words: the vertex's word is published there while
