@@ -900,10 +900,23 @@ int lm_field_upload_batch(lm_ctx* c, int n_fields, const float* u, const float* 
     if ((r = dalloc(c, &c->uv, n))) return r;
     c->uv_n = n;
   }
-  // stage u and v through the context's staging buffer (allocated once, 2 x 16M floats), one chunk
-  // of values at a time: no field-sized temporary is allocated and freed per upload
+  // page-locked u and v (mapped into the device's address space): one kernel reads both over the
+  // host link and writes the interleaved field, with no copies through a staging buffer
+  cudaPointerAttributes pa_u, pa_v;
+  const bool mapped = cudaPointerGetAttributes(&pa_u, u) == cudaSuccess &&
+                      cudaPointerGetAttributes(&pa_v, v) == cudaSuccess && pa_u.type == cudaMemoryTypeHost &&
+                      pa_v.type == cudaMemoryTypeHost && pa_u.devicePointer && pa_v.devicePointer;
+  cudaGetLastError();  // an unregistered pointer is not an error here
+  if (mapped) {
+    launch_interleave(static_cast<const float*>(pa_u.devicePointer), static_cast<const float*>(pa_v.devicePointer),
+                      c->uv, n, c->st);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->st));
+  }
+  // otherwise stage u and v through the context's staging buffer (allocated once, 2 x 16M floats),
+  // one chunk of values at a time: no field-sized temporary is allocated and freed per upload
   const size_t chunk = (size_t)16 << 20;
-  if (!c->stage_uv) {
+  if (!mapped && !c->stage_uv) {
     const cudaError_t e = cudaMalloc(&c->stage_uv, 2 * chunk * sizeof(float));
     if (e != cudaSuccess) {
       c->stage_uv = nullptr;
@@ -911,7 +924,7 @@ int lm_field_upload_batch(lm_ctx* c, int n_fields, const float* u, const float* 
       return fail(c, LM_ERR_OOM, "cudaMalloc of the field staging buffer failed: %s", cudaGetErrorString(e));
     }
   }
-  for (size_t o = 0; o < n; o += chunk) {
+  for (size_t o = 0; !mapped && o < n; o += chunk) {
     const size_t m = std::min(chunk, n - o);
     CK(cudaMemcpyAsync(c->stage_uv, u + o, m * sizeof(float), cudaMemcpyDefault, c->st));
     CK(cudaMemcpyAsync(c->stage_uv + chunk, v + o, m * sizeof(float), cudaMemcpyDefault, c->st));
