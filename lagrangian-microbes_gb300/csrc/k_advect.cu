@@ -32,6 +32,37 @@ void launch_interleave(const float* u, const float* v, float2* uv, size_t n, cud
   k_interleave<<<grid, 256, 0, st>>>(u, v, uv, n);
 }
 
+// Caller-order particles (float64 positions, int8 species) into the padded slot layout: offsets
+// from the float32 field origin with the same single rounding as the host path, status OK, and pad
+// slots (map < 0) zeroed with status PAD. Reads the caller's page-locked arrays directly.
+__global__ void k_particles_in(const double* __restrict__ lon, const double* __restrict__ lat,
+                               const int8_t* __restrict__ sp, const int32_t* __restrict__ map, uint32_t S,
+                               double org_lon, double org_lat, float* __restrict__ xo, float* __restrict__ yo,
+                               int8_t* __restrict__ species, uint8_t* __restrict__ status) {
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < S; k += gridDim.x * blockDim.x) {
+    const int32_t q = map[k];
+    if (q < 0) {
+      xo[k] = yo[k] = 0.f;
+      species[k] = 0;
+      status[k] = STATUS_PAD;
+      continue;
+    }
+    xo[k] = (float)__dsub_rn(lon[q], org_lon);
+    yo[k] = (float)__dsub_rn(lat[q], org_lat);
+    species[k] = sp ? sp[q] : (int8_t)0;
+    status[k] = STATUS_OK;
+  }
+}
+
+void launch_particles_in(const double* lon, const double* lat, const int8_t* sp, const int32_t* map, uint32_t S,
+                         double org_lon, double org_lat, float* xo, float* yo, int8_t* species, uint8_t* status,
+                         cudaStream_t st) {
+  int grid = (int)((S + 255) / 256);
+  if (grid > 152 * 16) grid = 152 * 16;
+  if (grid < 1) grid = 1;
+  k_particles_in<<<grid, 256, 0, st>>>(lon, lat, sp, map, S, org_lon, org_lat, xo, yo, species, status);
+}
+
 // Block-level bounding box of valid positions, merged into the ensemble's box (blocks of B threads).
 template <int B = SLOT_BLOCK>
 __device__ __forceinline__ void block_bbox(bool valid, float x, float y, uint32_t* ebox_e) {

@@ -969,10 +969,29 @@ int lm_ensembles_upload(lm_ctx* c, int n_ens, const int64_t* counts, const doubl
   int r;
   if ((r = layout(c, (uint32_t)n_ens, counts))) return r;
   const uint32_t S = c->nslots;
-  std::vector<float> xo(S, 0.f), yo(S, 0.f);
-  std::vector<int8_t> sp(S, 0);
-  std::vector<uint8_t> st(S, STATUS_PAD);
-  for (uint32_t k = 0; k < S; ++k) {
+  // page-locked caller arrays (mapped into the device's address space): one kernel converts them
+  // into the slot layout; otherwise the conversion runs here and the slots are copied
+  const void* dev_in[3] = {nullptr, nullptr, nullptr};
+  const void* host_in[3] = {lon, lat, species};
+  bool mapped = total > 0;
+  for (int i = 0; i < 3 && mapped; ++i) {
+    if (!host_in[i]) continue;
+    cudaPointerAttributes pa;
+    mapped = cudaPointerGetAttributes(&pa, host_in[i]) == cudaSuccess && pa.type == cudaMemoryTypeHost &&
+             pa.devicePointer;
+    if (mapped) dev_in[i] = pa.devicePointer;
+  }
+  cudaGetLastError();  // an unregistered pointer is not an error here
+  if (mapped) {
+    launch_particles_in(static_cast<const double*>(dev_in[0]), static_cast<const double*>(dev_in[1]),
+                        static_cast<const int8_t*>(dev_in[2]), c->map_d, S, c->org_lon, c->org_lat, c->xo, c->yo,
+                        c->species, c->status, c->st);
+    CK(cudaGetLastError());
+  }
+  std::vector<float> xo(mapped ? 0 : S, 0.f), yo(mapped ? 0 : S, 0.f);
+  std::vector<int8_t> sp(mapped ? 0 : S, 0);
+  std::vector<uint8_t> st(mapped ? 0 : S, STATUS_PAD);
+  for (uint32_t k = 0; !mapped && k < S; ++k) {
     const int32_t q = c->hmap[k];
     if (q < 0) continue;
     xo[k] = (float)(lon[q] - c->org_lon);
@@ -980,7 +999,7 @@ int lm_ensembles_upload(lm_ctx* c, int n_ens, const int64_t* counts, const doubl
     sp[k] = species ? species[q] : 0;
     st[k] = STATUS_OK;
   }
-  if (S) {
+  if (S && !mapped) {
     CK(cudaMemcpyAsync(c->xo, xo.data(), S * sizeof(float), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(c->yo, yo.data(), S * sizeof(float), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(c->species, sp.data(), S, cudaMemcpyHostToDevice, c->st));

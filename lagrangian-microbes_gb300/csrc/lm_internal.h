@@ -287,6 +287,9 @@ inline void launch_dep(void (*kernel)(KArgs...), dim3 grid, dim3 block, cudaStre
 
 // ---- launchers (each enqueues on `st`) ----
 void launch_interleave(const float* u, const float* v, float2* uv, size_t n, cudaStream_t st);
+void launch_particles_in(const double* lon, const double* lat, const int8_t* sp, const int32_t* map, uint32_t S,
+                         double org_lon, double org_lat, float* xo, float* yo, int8_t* species, uint8_t* status,
+                         cudaStream_t st);
 // step_begin also brackets the stage times of the step in the field's frames when `f` is given.
 void launch_step_begin(const Bufs& b, const FieldView* f, const StepArgs& a, Ctrl* ctrl, cudaStream_t st);
 void launch_step_end(Ctrl* ctrl, bool interact, cudaStream_t st);
